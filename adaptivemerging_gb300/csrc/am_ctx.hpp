@@ -1,0 +1,158 @@
+// am_ctx.hpp -- device data layout and the internal kernel entry points of
+// libam.  Not part of the public ABI (include/am.h).
+//
+// HBM layout (FP64 drop-in):
+//   bodies   : per-body records, vectors stored xyz-contiguous (x[3i+k]),
+//              matrices row-major 9 doubles (R[9i+k]); a body slot exists for
+//              every scene body and every collection the host creates.
+//   nodes    : sphere-tree nodes (cB, r, child0, nchild, owner, cW).
+//   contacts : structure of arrays with a per-field stride of `cap`
+//              (J[k*cap + c] for k = 0..35) so that a warp reading one field
+//              of 32 consecutive contacts issues one coalesced 256 B request.
+//              Two buffers alternate every step (the previous step's
+//              contacts are the warm-start donors, as ContactPool.swapPools
+//              keeps them).
+//   pairs    : body-pair groups of the current step; contacts of one pair are
+//              a contiguous run [poff, poff + pcount) in list order.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/am.h"
+
+namespace am {
+
+enum : int { F_PINNED = 1, F_SLEEPING = 2, F_COLLECTION = 4 };
+
+struct DBodies {
+    int n;
+    int* type;
+    int* flags;
+    int* parent;     // collection slot or -1
+    int* root;       // sphere-tree root node or -1
+    double* x;       // 3
+    double* R;       // 9
+    double* v;       // 3
+    double* w;       // 3
+    double* mass;    // massLinear
+    double* minv;
+    double* jinv;    // 9
+    double* jinv0;   // 9
+    double* M;       // massAngular 9
+    double* M0;      // massAngular0 9
+    double* force;   // 3
+    double* torque;  // 3
+    double* dv;      // 6 (v then w)
+    double* size;    // 3 (box)
+    double* radius;
+    double* friction;
+    double* restitution;
+    double* plane;   // 4: n, d
+    double* pp;      // 3: plane point p
+    double* bbB;     // 24
+    double* hist;    // sleep metric history (HIST per body, ring)
+    int* hist_n;     // number of valid entries
+    int* hist_h;     // ring head
+    double* B2C;     // 12: R(9) t(3) body-to-collection
+};
+static const int HIST = 16;
+
+struct DNodes {
+    int n;
+    double* cB;      // 3
+    double* cW;      // 3
+    double* r;
+    int* child0;
+    int* nchild;
+    int* body;
+};
+
+struct DContacts {
+    int cap;
+    int *b1, *b2, *bv1, *bv2, *info, *pair, *state, *fresh;
+    double* f;       // 12 * cap : contactB1, normalB1, tangent1B1, tangent2B1
+    double* J;       // 36 * cap : jna.v jna.w jnb.v jnb.w jt1a.v ... (k*cap + c)
+    double* cv;      // constraintViolation
+    double* pcv;     // prevConstraintViolation
+    double* lam;     // 3 * cap
+    double* lamw;    // 3 * cap (warm-start copy)
+    double* bD;      // 6 * cap : bn bt1 bt2 D00 D11 D22
+    double* Ia;      // 9 * cap : jinv_1 * J_row.w for the three rows (solve body 1)
+    double* Ib;      // 9 * cap
+    int *sb1, *sb2;  // solve bodies (parent collection when merged, else the body)
+};
+
+struct DPairs {
+    int cap;
+    int *a, *b;      // body slots (sub-bodies for collection pairs)
+    int* count;      // contacts of the pair
+    int* off;        // first contact
+    int* keep;       // pair survives clearBodyPairContacts
+};
+
+struct Scratch {
+    int cap_int;
+    int* tmp;        // scan input scratch
+    int* tmp2;       // scan output scratch
+    int* block;      // block sums
+};
+
+// device-side counters and flags (one struct in device memory)
+struct DCount {
+    int n_cand;      // broad-phase candidate pairs
+    int n_pairs;     // narrow-phase pairs (sub-body pairs)
+    int n_contacts;  // contacts emitted
+    int overflow;    // capacity exceeded (required size in need_*)
+    int need_contacts;
+    int need_pairs;
+    int sweeps;
+    int error;       // AM_E_* raised on device
+    unsigned long long maxchg[2];  // max |delta lambda| (bits of a non-negative double) per sweep parity
+    int n_colours;
+    int bar_count;
+    int bar_gen;
+    double res_abs;  // residual
+    double lam_max;
+    int n_prev;      // contacts in the previous buffer
+};
+
+// ---- kernels / launchers (defined in the .cu files) ----------------------
+void launch_begin_step(const DBodies& B, const int* top, int ntop, double gx, double gy, double gz,
+                       int mergingReapply, cudaStream_t s);
+void launch_bv_update(const DBodies& B, const DNodes& N, cudaStream_t s);
+int launch_broadphase(const DBodies& B, const DNodes& N, const int* top, int ntop, int* candA, int* candB,
+                      int candCap, int* rowCount, int* rowOff, Scratch& sc, DCount* dc, cudaStream_t s);
+void launch_expand_pairs(const DBodies& B, const int* sub_off, const int* sub_ids, const int* candA,
+                         const int* candB, int ncand, DPairs& P, Scratch& sc, DCount* dc, cudaStream_t s);
+void launch_narrow(const DBodies& B, const DNodes& N, DPairs& P, DContacts& C, Scratch& sc, DCount* dc,
+                   bool emit, cudaStream_t s);
+void launch_scan(const int* in, int* out, int n, Scratch& sc, int* total, cudaStream_t s);
+
+// solve.cu
+struct DHash {
+    int cap;         // power of two
+    int* slot;       // contact index in the previous buffer or -1
+};
+void launch_ws_build(const DContacts& prev, int nprev, DHash& H, cudaStream_t s);
+void launch_warm_start(const DBodies& B, DContacts& cur, DContacts& prev, const DHash& H, DPairs& P,
+                       int npairs, int nprev, cudaStream_t s);
+void launch_solve_prep(const DBodies& B, DContacts& C, int nc, double dt, double fb, bool inColl,
+                       int restOv, double restVal, int redoWarm, cudaStream_t s);
+void launch_pgs_exact(DBodies& B, DContacts& C, int nc, const int* order, int iters, double omega,
+                      double comp, double tol, bool inColl, int frictionOv, double frictionVal, double slide,
+                      DCount* dc, cudaStream_t s);
+void colour_groups(const DBodies& B, const DContacts& C, DPairs& P, int npairs, int* colourOf, int* colourCnt,
+                   int* colourOff, int* fill, int* groupOrder, int maxC, unsigned long long* bodyMax, int nbodies,
+                   DCount* dc, Scratch& sc, cudaStream_t s);
+void launch_pgs_coloured(DBodies& B, DContacts& C, DPairs& P, const int* groupOrder, const int* colourOff,
+                         int ncolours, int iters, double omega, double comp, double tol, bool early,
+                         int frictionOv, double frictionVal, double slide, DCount* dc, int gridBlocks,
+                         cudaStream_t s);
+void launch_residual(const DBodies& B, DContacts& C, int nc, double comp, int frictionOv, double frictionVal,
+                     DCount* dc, cudaStream_t s);
+void launch_bpc_keep(const DContacts& C, DPairs& P, int npairs, cudaStream_t s);
+
+}  // namespace am

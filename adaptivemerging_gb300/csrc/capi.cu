@@ -1,0 +1,218 @@
+// capi.cu -- the extern "C" entry points declared in include/am.h.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "collections.hpp"
+
+using am::Ctx;
+
+namespace am {
+
+int Ctx::stepWithMerging(double dt) {
+    (void)dt;
+    err = "merging is not available in this build (set enable_merging = 0)";
+    return AM_E_ARG;
+}
+
+int Ctx::getBodies(am_body_state* o) {
+    int n = nScene, cap = host.cap;
+    std::vector<double> x(3 * cap), R(9 * cap), v(3 * cap), w(3 * cap);
+    std::vector<int> fl(cap), par(cap);
+    cudaMemcpyAsync(x.data(), B.x, sizeof(double) * 3 * cap, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(R.data(), B.R, sizeof(double) * 9 * cap, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(v.data(), B.v, sizeof(double) * 3 * cap, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(w.data(), B.w, sizeof(double) * 3 * cap, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(fl.data(), B.flags, sizeof(int) * cap, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(par.data(), B.parent, sizeof(int) * cap, cudaMemcpyDeviceToHost, stream);
+    int r = syncErr();
+    if (r) return r;
+    for (int i = 0; i < n; i++) {
+        if (o->x) std::memcpy(o->x + 3 * i, &x[3 * i], sizeof(double) * 3);
+        if (o->R) std::memcpy(o->R + 9 * i, &R[9 * i], sizeof(double) * 9);
+        if (o->v) std::memcpy(o->v + 3 * i, &v[3 * i], sizeof(double) * 3);
+        if (o->omega) std::memcpy(o->omega + 3 * i, &w[3 * i], sizeof(double) * 3);
+        if (o->sleeping) o->sleeping[i] = (fl[i] & F_SLEEPING) ? 1 : 0;
+        if (o->parent) o->parent[i] = par[i];
+    }
+    return AM_OK;
+}
+
+int Ctx::getContacts(am_contacts* o, int capacity, int* n) {
+    *n = nContacts;
+    if (capacity < nContacts) return AM_E_CAPACITY;
+    int nc = nContacts;
+    if (nc == 0) return AM_OK;
+    const DContacts& c = C[cur];
+    int cap = c.cap;
+    auto geti = [&](int* dst, const int* src) {
+        if (dst) cudaMemcpyAsync(dst, src, sizeof(int) * nc, cudaMemcpyDeviceToHost, stream);
+    };
+    geti(o->body1, c.b1); geti(o->body2, c.b2); geti(o->bv1, c.bv1); geti(o->bv2, c.bv2);
+    geti(o->info, c.info); geti(o->state, c.state); geti(o->fresh, c.fresh);
+    std::vector<double> f(12 * (size_t)cap), J(36 * (size_t)cap), cv(cap), pcv(cap), lam(3 * (size_t)cap),
+        bD(6 * (size_t)cap);
+    cudaMemcpyAsync(f.data(), c.f, sizeof(double) * 12 * cap, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(J.data(), c.J, sizeof(double) * 36 * cap, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(cv.data(), c.cv, sizeof(double) * cap, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(pcv.data(), c.pcv, sizeof(double) * cap, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(lam.data(), c.lam, sizeof(double) * 3 * cap, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(bD.data(), c.bD, sizeof(double) * 6 * cap, cudaMemcpyDeviceToHost, stream);
+    int r = syncErr();
+    if (r) return r;
+    for (int i = 0; i < nc; i++) {
+        if (o->frame) for (int k = 0; k < 12; k++) o->frame[12 * i + k] = f[(size_t)k * cap + i];
+        if (o->jac) for (int k = 0; k < 36; k++) o->jac[36 * i + k] = J[(size_t)k * cap + i];
+        if (o->violation) { o->violation[2 * i] = cv[i]; o->violation[2 * i + 1] = pcv[i]; }
+        if (o->lambda) for (int k = 0; k < 3; k++) o->lambda[3 * i + k] = lam[(size_t)k * cap + i];
+        if (o->bD) for (int k = 0; k < 6; k++) o->bD[6 * i + k] = bD[(size_t)k * cap + i];
+    }
+    return AM_OK;
+}
+
+}  // namespace am
+
+extern "C" {
+
+void am_params_default(am_params* p) {
+    std::memset(p, 0, sizeof(*p));
+    p->iterations = 30; p->tolerance = 1e-5; p->omega = 1.0; p->iterations_in_collection = 1;
+    p->feedback_stiffness = 0.5; p->enable_compliance = 1; p->compliance = 1e-3;
+    p->restitution_override = 0; p->restitution = 0.5; p->friction_override = 0; p->friction = 0.1;
+    p->warm_start = 1; p->use_gravity = 1; p->gravity_amount = 1.0; p->gravity_angle = 90.0;
+    p->viscous_linear = 1.0; p->viscous_angular = 1.0;
+    p->enable_merging = 1; p->enable_merge_pinned = 1; p->enable_merge_cycle = 0;
+    p->enable_merge_stable_contact = 1; p->enable_merge_let_it_breathe = 1; p->enable_unmerging = 1;
+    p->enable_unmerge_friction = 1; p->enable_unmerge_normal = 1; p->enable_unmerge_relative_motion = 1;
+    p->update_contacts_in_collections = 1; p->organize_contacts = 1; p->metric_position_level = 0;
+    p->step_accum_merging = 3; p->step_accum_unmerging = 3; p->steps_between_merge_events = 10;
+    p->threshold_merge = 1e-2; p->threshold_unmerge = 2e-2; p->threshold_breath = 1e-5;
+    p->enable_sleeping = 1; p->sleep_step_accum = 10; p->sleep_threshold = 1e-5;
+    p->sliding_threshold = 0.01; p->solver_order = AM_ORDER_REFERENCE;
+}
+
+static int check_params(const am_params* p, std::string& err) {
+    if (p->enable_merge_cycle) { err = "cycle merge condition is not supported"; return AM_E_ARG; }
+    if (p->metric_position_level) { err = "position-level motion metric is not supported"; return AM_E_ARG; }
+    if (!p->organize_contacts && p->enable_merging) { err = "organize_contacts = 0 is not supported"; return AM_E_ARG; }
+    if (p->sleep_step_accum > am::HIST || p->sleep_step_accum < 0) { err = "sleep_step_accum > 16"; return AM_E_ARG; }
+    if (p->iterations < 0) { err = "iterations < 0"; return AM_E_ARG; }
+    return AM_OK;
+}
+
+int32_t am_create(const am_params* p, void** ctx) {
+    if (!p || !ctx) return AM_E_ARG;
+    *ctx = nullptr;
+    std::string e;
+    if (check_params(p, e)) return AM_E_ARG;
+    Ctx* c = new (std::nothrow) Ctx(*p);
+    if (!c) return AM_E_ARG;
+    *ctx = c;
+    return AM_OK;
+}
+
+int32_t am_destroy(void* ctx) {
+    delete (Ctx*)ctx;
+    return AM_OK;
+}
+
+const char* am_last_error(void* ctx) { return ctx ? ((Ctx*)ctx)->err.c_str() : "null context"; }
+
+int32_t am_set_params(void* ctx, const am_params* p) {
+    if (!ctx || !p) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (check_params(p, c->err)) return AM_E_ARG;
+    c->P = *p;
+    c->host.P = &c->P;
+    return AM_OK;
+}
+
+int32_t am_set_scene(void* ctx, const am_scene* s) {
+    if (!ctx || !s) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    for (int i = 0; i < s->n_bodies; i++) {
+        int t = s->type[i];
+        if (t < AM_BOX || t > AM_TREE) { c->err = "unknown body type"; return AM_E_ARG; }
+        if ((t == AM_SPHERE || t == AM_TREE) && (s->body_root[i] < 0 || s->body_root[i] >= s->n_nodes)) {
+            c->err = "sphere / tree body without a valid root node";
+            return AM_E_ARG;
+        }
+    }
+    return c->setScene(*s);
+}
+
+int32_t am_step(void* ctx, double dt) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) { c->err = "no scene loaded"; return AM_E_STATE; }
+    return c->step(dt);
+}
+
+int32_t am_collide(void* ctx, double dt) {
+    (void)dt;
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) { c->err = "no scene loaded"; return AM_E_STATE; }
+    c->totalSteps++;
+    int r = c->beginStep(0);
+    if (!r) r = c->collisionDetection();
+    if (!r) r = c->syncErr();
+    return r;
+}
+
+int32_t am_warm_start(void* ctx) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    int r = c->warmStart();
+    return r ? r : c->syncErr();
+}
+
+int32_t am_solve(void* ctx, double dt, am_solve_stats* st) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    int r = c->solveLCP(dt, c->P.warm_start != 0);
+    if (!r) r = c->readCounts();
+    if (!r) r = c->collectStats();
+    if (!r && st) *st = c->stats;
+    return r;
+}
+
+int32_t am_integrate(void* ctx, double dt) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    int r = c->finishStep(dt);
+    return r ? r : c->syncErr();
+}
+
+int32_t am_get_bodies(void* ctx, am_body_state* out) {
+    if (!ctx || !out) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    return c->getBodies(out);
+}
+
+int32_t am_num_contacts(void* ctx, int32_t* n) {
+    if (!ctx || !n) return AM_E_ARG;
+    *n = ((Ctx*)ctx)->nContacts;
+    return AM_OK;
+}
+
+int32_t am_get_contacts(void* ctx, am_contacts* out, int32_t capacity, int32_t* n) {
+    if (!ctx || !out || !n) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    return c->getContacts(out, capacity, n);
+}
+
+int32_t am_get_stats(void* ctx, am_solve_stats* out) {
+    if (!ctx || !out) return AM_E_ARG;
+    *out = ((Ctx*)ctx)->stats;
+    return AM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,138 @@
+"""ctypes binding of libam.so and a host-side mirror of the reference's
+system / collision-processor call surface.
+
+`System` follows RigidBodySystem (step = advanceTime) and exposes the
+CollisionProcessor phases (collisionDetection, warmStart, solveLCP) with the
+reference's names.  Errors from the C ABI raise `AmError` with the context's
+last error string; there is no CPU fallback: if libam.so cannot be loaded the
+import fails loudly.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libam.so")
+
+EXPORTS = [
+    "am_params_default", "am_create", "am_destroy", "am_last_error", "am_set_params", "am_set_scene",
+    "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
+    "am_num_contacts", "am_get_contacts", "am_get_stats",
+]
+
+_lib = None
+
+
+class AmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"am status {code}: {msg}")
+        self.code = code
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -m adaptivemerging_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.am_params_default.argtypes = [C.POINTER(abi.am_params)]
+        L.am_params_default.restype = None
+        L.am_create.argtypes = [C.POINTER(abi.am_params), C.POINTER(vp)]
+        L.am_destroy.argtypes = [vp]
+        L.am_last_error.argtypes = [vp]
+        L.am_last_error.restype = C.c_char_p
+        L.am_set_params.argtypes = [vp, C.POINTER(abi.am_params)]
+        L.am_set_scene.argtypes = [vp, C.POINTER(abi.am_scene)]
+        L.am_step.argtypes = [vp, C.c_double]
+        L.am_collide.argtypes = [vp, C.c_double]
+        L.am_warm_start.argtypes = [vp]
+        L.am_solve.argtypes = [vp, C.c_double, C.POINTER(abi.am_solve_stats)]
+        L.am_integrate.argtypes = [vp, C.c_double]
+        L.am_get_bodies.argtypes = [vp, C.POINTER(abi.am_body_state)]
+        L.am_num_contacts.argtypes = [vp, C.POINTER(C.c_int32)]
+        L.am_get_contacts.argtypes = [vp, C.POINTER(abi.am_contacts), C.c_int32, C.POINTER(C.c_int32)]
+        L.am_get_stats.argtypes = [vp, C.POINTER(abi.am_solve_stats)]
+        for f in EXPORTS:
+            if f not in ("am_params_default", "am_last_error"):
+                getattr(L, f).restype = C.c_int32
+        _lib = L
+    return _lib
+
+
+class System:
+    """One simulation context on the current CUDA device."""
+
+    def __init__(self, scene, params):
+        self.params = params
+        self.scene = scene
+        self.h = C.c_void_p()
+        self._check(lib().am_create(C.byref(params), C.byref(self.h)))
+        self._s = scene.struct()
+        self._check(lib().am_set_scene(self.h, C.byref(self._s)))
+        self.n = scene.n
+
+    def _check(self, r):
+        if r != 0:
+            msg = lib().am_last_error(self.h).decode() if self.h else ""
+            raise AmError(r, msg)
+
+    def close(self):
+        if self.h:
+            lib().am_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # RigidBodySystem.advanceTime
+    def advance_time(self, dt, n=1):
+        for _ in range(n):
+            self._check(lib().am_step(self.h, dt))
+
+    step = advance_time
+
+    # CollisionProcessor phases
+    def collision_detection(self, dt=0.0):
+        self._check(lib().am_collide(self.h, dt))
+
+    def warm_start(self):
+        self._check(lib().am_warm_start(self.h))
+
+    def solve_lcp(self, dt):
+        st = abi.am_solve_stats()
+        self._check(lib().am_solve(self.h, dt, C.byref(st)))
+        return st
+
+    def integrate(self, dt):
+        self._check(lib().am_integrate(self.h, dt))
+
+    def stats(self):
+        st = abi.am_solve_stats()
+        self._check(lib().am_get_stats(self.h, C.byref(st)))
+        return st
+
+    def num_contacts(self):
+        n = C.c_int32()
+        self._check(lib().am_num_contacts(self.h, C.byref(n)))
+        return n.value
+
+    def contacts(self):
+        n = self.num_contacts()
+        buf = abi.Contacts(n)
+        s = buf.struct()
+        got = C.c_int32()
+        self._check(lib().am_get_contacts(self.h, C.byref(s), buf.n, C.byref(got)))
+        return buf.view(got.value)
+
+    def bodies(self):
+        st = abi.BodyState(self.n)
+        s = st.struct()
+        self._check(lib().am_get_bodies(self.h, C.byref(s)))
+        return {"x": st.x.reshape(-1, 3), "R": st.R.reshape(-1, 9), "v": st.v.reshape(-1, 3),
+                "omega": st.omega.reshape(-1, 3), "sleeping": st.sleeping, "parent": st.parent}

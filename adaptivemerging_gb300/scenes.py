@@ -1,0 +1,185 @@
+"""Seeded synthetic scenes (structure-of-arrays am_scene inputs).
+
+Mass properties follow the reference scene loader (XMLParser.java:360-447):
+box mass = sx*sy*sz*density, inertia = m/12 diag(sy^2+sz^2, sx^2+sz^2,
+sx^2+sy^2); sphere mass = 4/3 pi r^3 density, inertia = 2/5 m r^2 I.  The
+reference's benchmark scenes are not public datasets; these generators build
+the BASELINE workloads (tower, brick wall + projectile, batched bins, clumps)
+from a seed with the sizes and distributions the benchmark names.
+"""
+import math
+
+import numpy as np
+
+from .abi import AM_BOX, AM_PLANE, AM_SPHERE, AM_TREE, SceneArrays
+
+
+def yaw(theta):
+    """Rotation about +y (row-major)."""
+    c, s = math.cos(theta), math.sin(theta)
+    return [c, 0.0, s, 0.0, 1.0, 0.0, -s, 0.0, c]
+
+
+def axis_angle(ax, theta):
+    ax = np.asarray(ax, float)
+    ax = ax / np.linalg.norm(ax)
+    x, y, z = ax
+    c, s = math.cos(theta), math.sin(theta)
+    t = 1 - c
+    return [t * x * x + c, t * x * y - s * z, t * x * z + s * y,
+            t * x * y + s * z, t * y * y + c, t * y * z - s * x,
+            t * x * z - s * y, t * y * z + s * x, t * z * z + c]
+
+
+IDENT = [1.0, 0, 0, 0, 1.0, 0, 0, 0, 1.0]
+
+
+class Builder:
+    def __init__(self):
+        self.b = []          # per-body dicts
+        self.nodes = []      # (c, r, child0, nchild)
+
+    def _add(self, **kw):
+        d = dict(type=AM_BOX, pinned=0, x=(0, 0, 0), R=IDENT, v=(0, 0, 0), omega=(0, 0, 0),
+                 mass=0.0, inertia=[0.0] * 9, friction=0.8, restitution=0.0,
+                 shape=(0, 0, 0, 0), root=-1)
+        d.update(kw)
+        self.b.append(d)
+        return len(self.b) - 1
+
+    def box(self, size, x, R=IDENT, density=1.0, pinned=False, v=(0, 0, 0), omega=(0, 0, 0),
+            friction=0.8, restitution=0.0):
+        sx, sy, sz = size
+        m = sx * sy * sz * density
+        I = [1.0 / 12 * m * (sy * sy + sz * sz), 0, 0, 0, 1.0 / 12 * m * (sx * sx + sz * sz), 0,
+             0, 0, 1.0 / 12 * m * (sx * sx + sy * sy)]
+        return self._add(type=AM_BOX, pinned=int(pinned), x=x, R=R, v=v, omega=omega, mass=m,
+                         inertia=I, friction=friction, restitution=restitution,
+                         shape=(sx, sy, sz, 0.0))
+
+    def sphere(self, r, x, density=1.0, mass=None, pinned=False, v=(0, 0, 0), omega=(0, 0, 0),
+               friction=0.8, restitution=0.0, R=IDENT):
+        m = 4.0 / 3 * math.pi * r * r * r * density if mass is None else float(mass)
+        i = 2.0 / 5 * m * r * r
+        root = len(self.nodes)
+        self.nodes.append(((0.0, 0.0, 0.0), r, -1, 0))
+        return self._add(type=AM_SPHERE, pinned=int(pinned), x=x, R=R, v=v, omega=omega, mass=m,
+                         inertia=[i, 0, 0, 0, i, 0, 0, 0, i], friction=friction,
+                         restitution=restitution, shape=(r, 0, 0, 0), root=root)
+
+    def plane(self, p, n, friction=0.8, restitution=0.0):
+        return self._add(type=AM_PLANE, pinned=1, x=p, shape=(n[0], n[1], n[2], 0.0),
+                         friction=friction, restitution=restitution)
+
+    def clump(self, centres, radii, x, density=1.0, R=IDENT, v=(0, 0, 0), friction=0.8,
+              restitution=0.0):
+        """Sphere-tree body: a root sphere enclosing leaf spheres (2-level
+        BVNode tree).  Mass and inertia sum the leaf spheres with the
+        parallel-axis theorem about their mass-weighted centre, and the leaf
+        centres are re-expressed about that centre."""
+        centres = np.asarray(centres, float)
+        radii = np.asarray(radii, float)
+        ms = 4.0 / 3 * math.pi * radii ** 3 * density
+        m = float(ms.sum())
+        com = (ms[:, None] * centres).sum(0) / m
+        c = centres - com
+        I = np.zeros((3, 3))
+        for k in range(len(radii)):
+            I += 2.0 / 5 * ms[k] * radii[k] ** 2 * np.eye(3)
+            d = c[k]
+            I += ms[k] * (np.dot(d, d) * np.eye(3) - np.outer(d, d))
+        rr = float(max(np.linalg.norm(c[k]) + radii[k] for k in range(len(radii))))
+        root = len(self.nodes)
+        self.nodes.append(((0.0, 0.0, 0.0), rr, root + 1, len(radii)))
+        for k in range(len(radii)):
+            self.nodes.append((tuple(c[k]), float(radii[k]), -1, 0))
+        return self._add(type=AM_TREE, x=tuple(np.asarray(x, float) + 0.0), R=R, v=v, mass=m,
+                         inertia=list(I.reshape(-1)), friction=friction,
+                         restitution=restitution, root=root)
+
+    def build(self):
+        n = len(self.b)
+        f = lambda k, w: np.array([d[k] for d in self.b], float).reshape(n * w)
+        nodes = self.nodes if self.nodes else []
+        return SceneArrays(
+            type=[d["type"] for d in self.b], pinned=[d["pinned"] for d in self.b],
+            x=f("x", 3), R=f("R", 9), v=f("v", 3), omega=f("omega", 3),
+            mass=[d["mass"] for d in self.b], inertia=f("inertia", 9),
+            friction=[d["friction"] for d in self.b], restitution=[d["restitution"] for d in self.b],
+            shape=f("shape", 4), body_root=[d["root"] for d in self.b],
+            node_c=np.array([c for c, _, _, _ in nodes], float).reshape(-1),
+            node_r=np.array([r for _, r, _, _ in nodes], float),
+            node_child0=[c0 for _, _, c0, _ in nodes], node_nchild=[nc for _, _, _, nc in nodes],
+        )
+
+
+# --------------------------------------------------------------------------
+# Benchmark workloads
+def tower(n_boxes=25, seed=1, size=(1.0, 0.5, 1.0), density=1000.0):
+    """Tower of `n_boxes` boxes (1.0 x 0.5 x 1.0 m, density 1000) stacked on a
+    static ground plane; each box offset by U(+-0.01) m in x/z and U(+-0.5)
+    degrees of yaw."""
+    rng = np.random.default_rng(seed)
+    B = Builder()
+    B.plane((0, 0, 0), (0, 1, 0))
+    h = size[1]
+    for i in range(n_boxes):
+        dx, dz = rng.uniform(-0.01, 0.01, 2)
+        th = math.radians(rng.uniform(-0.5, 0.5))
+        B.box(size, (dx, h / 2 + h * i, dz), R=yaw(th), density=density)
+    return B.build()
+
+
+def wall(cols=40, rows=25, seed=2, brick=(0.4, 0.2, 0.2), density=1000.0, gap=0.01,
+         projectile=True):
+    """Running-bond wall of cols x rows bricks (0.4 x 0.2 x 0.2 m, density
+    1000, positions jittered U(+-2 mm) in x/z) on a ground plane, and a sphere
+    projectile (r = 0.3 m, 50 kg) fired at 15 m/s at a seeded height."""
+    rng = np.random.default_rng(seed)
+    B = Builder()
+    B.plane((0, 0, 0), (0, 1, 0))
+    bx, by, bz = brick
+    pitch = bx + gap
+    for j in range(rows):
+        off = 0.5 * pitch * (j % 2)
+        for i in range(cols):
+            dx, dz = rng.uniform(-0.002, 0.002, 2)
+            x = -0.5 * cols * pitch + (i + 0.5) * pitch + off + dx
+            B.box(brick, (x, by / 2 + by * j, dz), density=density)
+    if projectile:
+        hgt = float(rng.uniform(0.5, rows * by * 0.8))
+        B.sphere(0.3, (0.0, hgt, -3.0), mass=50.0, v=(0.0, 0.0, 15.0))
+    return B.build()
+
+
+def random_pile(n=30, seed=0, kinds=("box", "sphere"), extent=3.0, height=4.0):
+    """Small random scene for parity tests: boxes and spheres over a plane,
+    dropped from a jittered grid (no initial overlaps)."""
+    rng = np.random.default_rng(seed)
+    B = Builder()
+    B.plane((0, 0, 0), (0, 1, 0))
+    side = int(math.ceil(n ** (1 / 3)))
+    k = 0
+    for iy in range(side * 4):
+        for ix in range(side):
+            for iz in range(side):
+                if k >= n:
+                    break
+                p = (-extent / 2 + (ix + 0.5) * extent / side + rng.uniform(-0.05, 0.05),
+                     0.6 + iy * 0.9 + rng.uniform(0, 0.05),
+                     -extent / 2 + (iz + 0.5) * extent / side + rng.uniform(-0.05, 0.05))
+                kind = kinds[int(rng.integers(len(kinds)))]
+                if kind == "box":
+                    s = tuple(rng.uniform(0.2, 0.6, 3))
+                    B.box(s, p, R=axis_angle(rng.normal(size=3), rng.uniform(0, math.pi)),
+                          density=rng.uniform(500, 2000), friction=float(rng.uniform(0.3, 0.9)))
+                elif kind == "sphere":
+                    B.sphere(float(rng.uniform(0.1, 0.3)), p, density=rng.uniform(500, 2000),
+                             friction=float(rng.uniform(0.3, 0.9)))
+                else:
+                    m = int(rng.integers(4, 9))
+                    cs = rng.uniform(-0.12, 0.12, (m, 3))
+                    rs = rng.uniform(0.06, 0.12, m)
+                    B.clump(cs, rs, p, density=rng.uniform(500, 2000))
+                k += 1
+    return B.build()

@@ -1,0 +1,207 @@
+/*
+ * am.h -- C ABI of the GB300 contact hot path (collision, contact setup,
+ * warm start, projected Gauss-Seidel with box friction, single sweep inside
+ * merged collections, integration).
+ *
+ * Plain C types only; every call returns an int32 status (AM_OK = 0, negative
+ * on error) and never aborts.  Host arrays passed in are borrowed for the
+ * duration of the call.  One am_ctx owns its device buffers and one CUDA
+ * stream; calls on one context are serialised by the caller (the reference is
+ * single threaded).
+ *
+ * Each entry point names the reference method it replaces (paths are relative
+ * to the reference project root, EulalieCoevoet/AdaptiveMerging).
+ */
+#ifndef AM_H
+#define AM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define AM_OK            0
+#define AM_E_ARG        (-1)  /* bad argument or unsupported scene feature   */
+#define AM_E_CAPACITY   (-2)  /* output buffer too small; *n holds the need  */
+#define AM_E_NONFINITE  (-3)  /* a multiplier or velocity became NaN/Inf      */
+#define AM_E_TIMEOUT    (-4)  /* a bounded device wait gave up               */
+#define AM_E_CUDA       (-5)  /* CUDA runtime error (see am_last_error)      */
+#define AM_E_STATE      (-6)  /* call order violated (e.g. no scene loaded)  */
+
+/* ---- body geometry types (RigidBodyGeom* / PlaneRigidBody) ------------- */
+#define AM_BOX     0   /* RigidBodyGeomBox: shape = (sx, sy, sz, 0)          */
+#define AM_SPHERE  1   /* RigidBodyGeomSphere: shape = (r, 0, 0, 0); 1-node tree */
+#define AM_PLANE   2   /* PlaneRigidBody: x = point p, shape = (nx, ny, nz, 0) */
+#define AM_TREE    3   /* sphere-tree body (mesh / clump), shape unused      */
+
+/* ---- contact state (Contact.ContactState) ------------------------------- */
+#define AM_STATE_BROKEN 0
+#define AM_STATE_ONEDGE 1
+#define AM_STATE_CLEAR  2
+
+/* ---- bounding-volume ids carried in contact keys ----------------------- */
+#define AM_BV_NULL (-1)            /* no bounding volume (box colliders)      */
+#define AM_BV_PLANE(b) (-2 - (b))  /* PlaneRigidBody.dummyBV of plane body b  */
+
+/* ---- Gauss-Seidel ordering on the device -------------------------------- */
+#define AM_ORDER_REFERENCE 0  /* contacts in list order: bit-exact to PGS.java */
+#define AM_ORDER_COLOURED  1  /* body-pair groups coloured, colours in parallel */
+
+/*
+ * Solver / system parameters.  Field names and defaults follow the reference
+ * parameter objects:
+ *   CollisionProcessor.java:1058-1083, Merging.java:30-54, Sleeping.java:25-30,
+ *   Contact.java:518, RigidBodySystem.java:544-567.
+ * am_params_default() fills the reference defaults.
+ */
+typedef struct am_params {
+    /* CollisionProcessor */
+    int32_t iterations;               /* 30   */
+    double  tolerance;                /* 1e-5 */
+    double  omega;                    /* 1    */
+    int32_t iterations_in_collection; /* 1    */
+    double  feedback_stiffness;       /* 0.5  */
+    int32_t enable_compliance;        /* 1    */
+    double  compliance;               /* 1e-3 */
+    int32_t restitution_override;     /* 0    */
+    double  restitution;              /* 0.5 (used only with override) */
+    int32_t friction_override;        /* 0    */
+    double  friction;                 /* 0.1 (used only with override) */
+    int32_t warm_start;               /* 1    */
+    /* RigidBodySystem */
+    int32_t use_gravity;              /* 1    */
+    double  gravity_amount;           /* 1    */
+    double  gravity_angle;            /* 90 (degrees) */
+    double  viscous_linear;           /* 1    */
+    double  viscous_angular;          /* 1    */
+    /* Merging.MergeParameters */
+    int32_t enable_merging;           /* 1 */
+    int32_t enable_merge_pinned;      /* 1 */
+    int32_t enable_merge_cycle;       /* 0 (cycle condition: unsupported, must stay 0) */
+    int32_t enable_merge_stable_contact; /* 1 */
+    int32_t enable_merge_let_it_breathe; /* 1 */
+    int32_t enable_unmerging;         /* 1 */
+    int32_t enable_unmerge_friction;  /* 1 */
+    int32_t enable_unmerge_normal;    /* 1 */
+    int32_t enable_unmerge_relative_motion; /* 1 */
+    int32_t update_contacts_in_collections; /* 1 */
+    int32_t organize_contacts;        /* 1 */
+    int32_t metric_position_level;    /* 0 (must stay 0) */
+    int32_t step_accum_merging;       /* 3 */
+    int32_t step_accum_unmerging;     /* 3 */
+    int32_t steps_between_merge_events; /* 10 */
+    double  threshold_merge;          /* 1e-2 */
+    double  threshold_unmerge;        /* 2e-2 */
+    double  threshold_breath;         /* 1e-5 */
+    /* Sleeping.SleepParameters */
+    int32_t enable_sleeping;          /* 1 */
+    int32_t sleep_step_accum;         /* 10 */
+    double  sleep_threshold;          /* 1e-5 */
+    /* Contact */
+    double  sliding_threshold;        /* 0.01 */
+    /* device solver ordering (no reference counterpart) */
+    int32_t solver_order;             /* AM_ORDER_REFERENCE */
+} am_params;
+
+/*
+ * Scene description (structure of arrays, body index = stable body id, which
+ * replaces Java object identity in contact keys).  Mass properties follow
+ * XMLParser.java:360-447: box inertia m/12 (sy^2+sz^2, ...), sphere 2/5 m r^2.
+ * Pinned bodies: mass 0 and zero inertia.  Rotations are row-major
+ * (m00 m01 m02 m10 ...).
+ */
+typedef struct am_scene {
+    int32_t        n_bodies;
+    const int32_t* type;        /* [n] AM_BOX / AM_SPHERE / AM_PLANE / AM_TREE */
+    const int32_t* pinned;      /* [n] */
+    const double*  x;           /* [3n] centre of mass (plane: point p)        */
+    const double*  R;           /* [9n] orientation (theta)                     */
+    const double*  v;           /* [3n] */
+    const double*  omega;       /* [3n] */
+    const double*  mass;        /* [n]  massLinear                              */
+    const double*  inertia;     /* [9n] massAngular0 (rest pose)                */
+    const double*  friction;    /* [n]  default 0.8                             */
+    const double*  restitution; /* [n]  default 0                               */
+    const double*  shape;       /* [4n] see AM_BOX ... AM_TREE                  */
+    /* sphere trees (BVNode / BVSphere); spheres own a single leaf node */
+    int32_t        n_nodes;
+    const int32_t* body_root;   /* [n] root node index or -1                    */
+    const double*  node_c;      /* [3*n_nodes] centre in body frame (cB)        */
+    const double*  node_r;      /* [n_nodes]                                    */
+    const int32_t* node_child0; /* [n_nodes] first child index or -1 (leaf)     */
+    const int32_t* node_nchild; /* [n_nodes] children are contiguous            */
+} am_scene;
+
+/* Per-body state read back after a step. */
+typedef struct am_body_state {
+    double*  x;       /* [3n] */
+    double*  R;       /* [9n] */
+    double*  v;       /* [3n] */
+    double*  omega;   /* [3n] */
+    int32_t* sleeping;/* [n]  */
+    int32_t* parent;  /* [n]  collection id or -1 */
+} am_body_state;
+
+/*
+ * Contacts read back in list order.  Frame quantities are stored as the
+ * reference stores them (Contact.java:199-224): contact point, normal and
+ * tangents in body-1 coordinates; Jacobian rows in world coordinates.
+ */
+typedef struct am_contacts {
+    int32_t* body1;      /* [c] */
+    int32_t* body2;      /* [c] */
+    int32_t* bv1;        /* [c] node id / AM_BV_NULL / AM_BV_PLANE(b) */
+    int32_t* bv2;        /* [c] */
+    int32_t* info;       /* [c] */
+    double*  frame;      /* [12c] contactB1, normalB1, tangent1B1, tangent2B1 */
+    double*  jac;        /* [36c] jna, jnb, jt1a, jt1b, jt2a, jt2b (v then w) */
+    double*  violation;  /* [2c] constraintViolation, prevConstraintViolation */
+    double*  lambda;     /* [3c] lambda0..2 */
+    double*  bD;         /* [6c] bn, bt1, bt2, D00, D11, D22 */
+    int32_t* state;      /* [c] AM_STATE_* */
+    int32_t* fresh;      /* [c] newThisTimeStep */
+} am_contacts;
+
+typedef struct am_solve_stats {
+    int32_t n_contacts;      /* contacts in the full solve                       */
+    int32_t sweeps;          /* PGS iterations run (early exit on tolerance)     */
+    double  last_change;     /* max |delta lambda| of the last sweep             */
+    double  residual_abs;    /* natural-map LCP residual, inf-norm               */
+    double  residual_rel;    /* residual_abs / max(1, |lambda|_inf)              */
+} am_solve_stats;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+void        am_params_default(am_params* p);
+/* new context on the current CUDA device */
+int32_t     am_create(const am_params* p, void** ctx);
+int32_t     am_destroy(void* ctx);
+const char* am_last_error(void* ctx);
+int32_t     am_set_params(void* ctx, const am_params* p);
+
+/* Load a scene (replaces RigidBodySystem.bodies + reset(), RigidBodySystem.java:78,390-426). */
+int32_t am_set_scene(void* ctx, const am_scene* scene);
+
+/* One full step: RigidBodySystem.advanceTime(dt), RigidBodySystem.java:102-185. */
+int32_t am_step(void* ctx, double dt);
+
+/* CollisionProcessor.updateContactsMap + collisionDetection (CollisionProcessor.java:443-448, 91-102). */
+int32_t am_collide(void* ctx, double dt);
+/* CollisionProcessor.warmStart(false) (CollisionProcessor.java:481-640). */
+int32_t am_warm_start(void* ctx);
+/* CollisionProcessor.solveLCP(dt,false) -> PGS.solve (CollisionProcessor.java:108-137, PGS.java:73-194). */
+int32_t am_solve(void* ctx, double dt, am_solve_stats* stats);
+/* RigidBody.advanceVelocities + advancePositions for all bodies (RigidBody.java:409-441). */
+int32_t am_integrate(void* ctx, double dt);
+
+/* Read back. */
+int32_t am_get_bodies(void* ctx, am_body_state* out);
+int32_t am_num_contacts(void* ctx, int32_t* n);
+int32_t am_get_contacts(void* ctx, am_contacts* out, int32_t capacity, int32_t* n);
+int32_t am_get_stats(void* ctx, am_solve_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AM_H */

@@ -1,0 +1,104 @@
+"""Test-side ctypes binding of the oracle (oracle/liboracle.so).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load the
+oracle; the product never does.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from adaptivemerging_gb300 import abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB = os.path.join(ROOT, "oracle", "liboracle.so")
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        L.or_create.restype = C.c_void_p
+        L.or_create.argtypes = [C.POINTER(abi.am_params), C.POINTER(abi.am_scene)]
+        for f in ("or_destroy", "or_begin_step", "or_collide", "or_warm_start"):
+            getattr(L, f).argtypes = [C.c_void_p]
+        L.or_step.argtypes = [C.c_void_p, C.c_double]
+        L.or_solve.argtypes = [C.c_void_p, C.c_double]
+        L.or_run.argtypes = [C.c_void_p, C.c_double, C.c_int]
+        L.or_num_contacts.argtypes = [C.c_void_p]
+        L.or_num_contacts.restype = C.c_int
+        L.or_get_contacts.argtypes = [C.c_void_p, C.POINTER(abi.am_contacts)]
+        L.or_get_bodies.argtypes = [C.c_void_p, C.POINTER(abi.am_body_state)]
+        L.or_get_counters.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_double)]
+        L.or_top_ids.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_int]
+        L.or_top_ids.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+class Oracle:
+    def __init__(self, scene, params):
+        self.scene = scene
+        self.params = params
+        self._s = scene.struct()
+        self.h = lib().or_create(C.byref(params), C.byref(self._s))
+        self.n = scene.n
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_destroy(self.h)
+            self.h = None
+
+    def step(self, dt, n=1):
+        lib().or_run(self.h, dt, n)
+
+    def begin_step(self):
+        lib().or_begin_step(self.h)
+
+    def collide(self):
+        lib().or_collide(self.h)
+
+    def warm_start(self):
+        lib().or_warm_start(self.h)
+
+    def solve(self, dt):
+        lib().or_solve(self.h, dt)
+
+    def num_contacts(self):
+        return lib().or_num_contacts(self.h)
+
+    def contacts(self):
+        n = self.num_contacts()
+        buf = abi.Contacts(n)
+        s = buf.struct()
+        lib().or_get_contacts(self.h, C.byref(s))
+        return buf.view(n)
+
+    def bodies(self):
+        st = abi.BodyState(self.n)
+        s = st.struct()
+        lib().or_get_bodies(self.h, C.byref(s))
+        return {"x": st.x.reshape(-1, 3), "R": st.R.reshape(-1, 9), "v": st.v.reshape(-1, 3),
+                "omega": st.omega.reshape(-1, 3), "sleeping": st.sleeping, "parent": st.parent}
+
+    def counters(self):
+        out = (C.c_int64 * 6)()
+        ch = C.c_double()
+        lib().or_get_counters(self.h, out, C.byref(ch))
+        return {"sweeps": out[0], "merges": out[1], "unmerges": out[2], "top": out[3],
+                "bpcs": out[4], "collections": out[5], "last_change": ch.value}
+
+    def top_ids(self):
+        buf = np.zeros(self.n * 2 + 16, np.int32)
+        k = lib().or_top_ids(self.h, buf.ctypes.data_as(C.POINTER(C.c_int32)), len(buf))
+        return buf[:k].copy()
