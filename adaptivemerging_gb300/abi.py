@@ -108,6 +108,12 @@ class am_solve_stats(C.Structure):
                 ("residual_abs", _f64), ("residual_rel", _f64)]
 
 
+class am_perf(C.Structure):
+    _fields_ = [("launches", C.c_int64), ("pgs_launches", C.c_int64), ("pgs_ms", _f64),
+                ("contact_sweeps", C.c_int64), ("steps", C.c_int64), ("merge_events", C.c_int64),
+                ("unmerge_events", C.c_int64)]
+
+
 def ptr(a, ctype):
     """Borrowed pointer to a contiguous numpy array (None -> NULL)."""
     if a is None:

@@ -15,7 +15,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libam.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["collide.cu", "solve.cu", "step.cu", "capi.cu"]
+SOURCES = ["collide.cu", "solve.cu", "step.cu", "capi.cu", "pgs_fast.cu", "merging.cu"]
+# translation units that may contract a*b+c (not part of the bit-exact path)
+FMA_OK = {"pgs_fast.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
          "-diag-suppress", "550"]
@@ -46,7 +48,8 @@ def build(verbose=False, force=False):
         o = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc()] + FLAGS + ARCH + ["-c", s, "-o", o])
+            fl = [f if not (src in FMA_OK and f == "--fmad=false") else "--fmad=true" for f in FLAGS]
+            jobs.append([nvcc()] + fl + ARCH + ["-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -25,6 +25,10 @@
 
 namespace am {
 
+// kernels launched by this library since load (read by am_get_perf)
+extern long long g_launches;
+#define AM_LAUNCHED(n) (::am::g_launches += (n))
+
 enum : int { F_PINNED = 1, F_SLEEPING = 2, F_COLLECTION = 4 };
 
 struct DBodies {
@@ -147,10 +151,10 @@ void launch_pgs_exact(DBodies& B, DContacts& C, int nc, const int* order, int it
 void colour_groups(const DBodies& B, const DContacts& C, DPairs& P, int npairs, int* colourOf, int* colourCnt,
                    int* colourOff, int* fill, int* groupOrder, int maxC, unsigned long long* bodyMax, int nbodies,
                    DCount* dc, Scratch& sc, cudaStream_t s);
-void launch_pgs_coloured(DBodies& B, DContacts& C, DPairs& P, const int* groupOrder, const int* colourOff,
-                         int ncolours, int iters, double omega, double comp, double tol, bool early,
-                         int frictionOv, double frictionVal, double slide, DCount* dc, int gridBlocks,
-                         cudaStream_t s);
+void launch_pgs_fast(const DBodies& B, DContacts& C, DPairs& P, const int* groupOrder, const int* colourOff,
+                     int ncol, int nc, int iters, double omega, double comp, double tol, bool early, int fo,
+                     double fv, double slide, double* Mj, double* invD, int mcap, DCount* dc, int gridBlocks,
+                     cudaStream_t s);
 void launch_residual(const DBodies& B, DContacts& C, int nc, double comp, int frictionOv, double frictionVal,
                      DCount* dc, cudaStream_t s);
 void launch_bpc_keep(const DContacts& C, DPairs& P, int npairs, cudaStream_t s);

@@ -11,12 +11,6 @@ using am::Ctx;
 
 namespace am {
 
-int Ctx::stepWithMerging(double dt) {
-    (void)dt;
-    err = "merging is not available in this build (set enable_merging = 0)";
-    return AM_E_ARG;
-}
-
 int Ctx::getBodies(am_body_state* o) {
     int n = nScene, cap = host.cap;
     std::vector<double> x(3 * cap), R(9 * cap), v(3 * cap), w(3 * cap);
@@ -38,6 +32,31 @@ int Ctx::getBodies(am_body_state* o) {
         if (o->parent) o->parent[i] = par[i];
     }
     return AM_OK;
+}
+
+// Host-owned state: overwrite x / R / v / omega of the scene bodies that are
+// free top-level bodies (bodies inside a collection follow their collection).
+// The arrays are expected in pinned host memory for full-speed copies.
+int Ctx::putBodies(const am_body_state* in) {
+    int n = nScene;
+    bool anyColl = false;
+    for (int i = 0; i < n; i++) if (host.parent[i] >= 0) { anyColl = true; break; }
+    if (!anyColl) {
+        if (in->x) cudaMemcpyAsync(B.x, in->x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, stream);
+        if (in->R) cudaMemcpyAsync(B.R, in->R, sizeof(double) * 9 * n, cudaMemcpyHostToDevice, stream);
+        if (in->v) cudaMemcpyAsync(B.v, in->v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, stream);
+        if (in->omega) cudaMemcpyAsync(B.w, in->omega, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, stream);
+    } else {
+        for (int i = 0; i < n; i++) {
+            if (host.parent[i] >= 0) continue;
+            if (in->x) cudaMemcpyAsync(B.x + 3 * i, in->x + 3 * i, sizeof(double) * 3, cudaMemcpyHostToDevice, stream);
+            if (in->R) cudaMemcpyAsync(B.R + 9 * i, in->R + 9 * i, sizeof(double) * 9, cudaMemcpyHostToDevice, stream);
+            if (in->v) cudaMemcpyAsync(B.v + 3 * i, in->v + 3 * i, sizeof(double) * 3, cudaMemcpyHostToDevice, stream);
+            if (in->omega) cudaMemcpyAsync(B.w + 3 * i, in->omega + 3 * i, sizeof(double) * 3, cudaMemcpyHostToDevice, stream);
+        }
+    }
+    if (in->R) launch_refresh_inertia(B, n, stream);
+    return syncErr();
 }
 
 int Ctx::getContacts(am_contacts* o, int capacity, int* n) {
@@ -176,6 +195,7 @@ int32_t am_solve(void* ctx, double dt, am_solve_stats* st) {
     if (!c->stream) return AM_E_STATE;
     int r = c->solveLCP(dt, c->P.warm_start != 0);
     if (!r) r = c->readCounts();
+    if (!r) c->foldTiming();
     if (!r) r = c->collectStats();
     if (!r && st) *st = c->stats;
     return r;
@@ -196,6 +216,13 @@ int32_t am_get_bodies(void* ctx, am_body_state* out) {
     return c->getBodies(out);
 }
 
+int32_t am_put_bodies(void* ctx, const am_body_state* in) {
+    if (!ctx || !in) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    return c->putBodies(in);
+}
+
 int32_t am_num_contacts(void* ctx, int32_t* n) {
     if (!ctx || !n) return AM_E_ARG;
     *n = ((Ctx*)ctx)->nContacts;
@@ -207,6 +234,36 @@ int32_t am_get_contacts(void* ctx, am_contacts* out, int32_t capacity, int32_t* 
     Ctx* c = (Ctx*)ctx;
     if (!c->stream) return AM_E_STATE;
     return c->getContacts(out, capacity, n);
+}
+
+int32_t am_get_perf(void* ctx, am_perf* out) {
+    if (!ctx || !out) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    *out = c->perf;
+    out->launches = am::g_launches;
+    out->merge_events = c->mergeEvents;
+    out->unmerge_events = c->unmergeEvents;
+    return AM_OK;
+}
+
+int32_t am_get_topology(void* ctx, int32_t* items, int32_t* item_off, int32_t cap_items, int32_t* n_top,
+                        int32_t* n_items) {
+    if (!ctx || !n_top || !n_items) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    return c->getTopology(items, item_off, cap_items, n_top, n_items);
+}
+
+int32_t am_reset_perf(void* ctx) {
+    if (!ctx) return AM_E_ARG;
+    std::memset(&((Ctx*)ctx)->perf, 0, sizeof(am_perf));
+    return AM_OK;
+}
+
+int32_t am_get_stream(void* ctx, void** stream) {
+    if (!ctx || !stream) return AM_E_ARG;
+    *stream = (void*)((Ctx*)ctx)->stream;
+    return AM_OK;
 }
 
 int32_t am_get_stats(void* ctx, am_solve_stats* out) {

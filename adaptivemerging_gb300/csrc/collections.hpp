@@ -10,6 +10,8 @@
 
 #include <cstring>
 #include <string>
+#include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "am_ctx.hpp"
@@ -32,6 +34,7 @@ struct HostWorld {
         plane, pp, bbB, B2C;
     std::vector<int> top;                 // top-level list in reference order
     std::vector<std::vector<int>> subs;   // collection members in order
+    std::vector<int> nbb;                 // bounding-box corners stored (0 for planes)
 
     bool anyMerging() const { return P && P->enable_merging; }
 
@@ -47,6 +50,7 @@ struct HostWorld {
         friction.assign(cap, 0.8); restitution.assign(cap, 0); plane.assign(4 * cap, 0); pp.assign(3 * cap, 0);
         bbB.assign(24 * cap, 0); B2C.assign(12 * cap, 0);
         subs.assign(cap, {});
+        nbb.assign(cap, 8);
         top.clear();
         for (int i = 0; i < n; i++) {
             type[i] = s.type[i];
@@ -64,6 +68,7 @@ struct HostWorld {
                 plane[4 * i + 3] = -(q.x * nn.x + q.y * nn.y + q.z * nn.z);
                 stv(&pp[3 * i], q);
                 flags[i] = F_PINNED;
+                nbb[i] = 0;
                 continue;
             }
             for (int k = 0; k < 3; k++) {
@@ -116,6 +121,43 @@ struct HostWorld {
     }
 };
 
+// insertion-ordered set of ints (LinkedHashSet order: remove + add moves to the end)
+struct OSetI {
+    std::vector<int> v;
+    std::unordered_set<int> s;
+    bool contains(int x) const { return s.count(x) != 0; }
+    bool add(int x) { if (s.count(x)) return false; s.insert(x); v.push_back(x); return true; }
+    bool remove(int x) {
+        if (!s.erase(x)) return false;
+        for (size_t i = 0; i < v.size(); i++) if (v[i] == x) { v.erase(v.begin() + i); break; }
+        return true;
+    }
+    void clear() { v.clear(); s.clear(); }
+    size_t size() const { return v.size(); }
+    bool empty() const { return v.empty(); }
+};
+
+// host record of a BodyPairContact (BodyPairContact.java:14-45)
+struct HBPC {
+    int a = -1, b = -1;
+    std::vector<int> list;      // contact refs: >= 0 current buffer, < 0 ~slot in the collection store
+    std::vector<double> mm;     // motionMetricHist
+    std::vector<int> sh;        // contactStateHist
+    bool inCollection = false;
+    bool checked = false;
+};
+
+struct HostMerge {
+    std::vector<HBPC> bpc;
+    OSetI coll;                                 // CollisionProcessor.bodyPairContacts
+    std::vector<OSetI> bodyBpcs;                // RigidBody.bodyPairContacts per body slot
+    std::unordered_map<uint64_t, int> index;    // pair -> body-pair contact (checkExists)
+    std::vector<int> freeSlots;                 // free slots of the collection contact store
+    int nSlots = 0;
+    void reset(int cap);
+    int findOrCreate(int a, int b);
+};
+
 // The step context behind the C ABI.
 struct Ctx {
     am_params P;
@@ -149,11 +191,36 @@ struct Ctx {
     int* colourFill = nullptr;
     static const int MAXC = 256;
     int coopBlocks = 0;
+    double* Mj = nullptr;     // coloured sweep: M^-1 J^T per row and lane (36 per contact)
+    double* invD = nullptr;   // 1/(D + c) per row
+    int mjCap = 0;
     int nScene = 0, ntop = 0, nContacts = 0, nPrev = 0, nPairs = 0;
     int totalSteps = 0;
     bool mergingEvent = false;
     am_solve_stats stats{};
+    am_perf perf{};
+    cudaEvent_t evA = nullptr, evB = nullptr;
+    bool pgsPending = false;
     std::vector<void*> allocs;
+    // merging state
+    HostMerge M;
+    DContacts I{};      // contacts living inside collections
+    DContacts Sw{};     // gathered single-sweep list
+    int* idxA = nullptr;
+    int* idxB = nullptr;
+    int idxCap = 0;
+    int* metA = nullptr;
+    int* metB = nullptr;
+    int* metM = nullptr;
+    double* metOut = nullptr;
+    int metCap = 0;
+    int* nbbDev = nullptr;
+    std::vector<double> devDv;
+    std::vector<int> keyB1, keyB2, freshH, stateH, istateH;
+    std::vector<double> lam0H, cvH, icvH, ipcvH;
+    std::vector<int> apA, apB, apOff, apCnt;   // pairs handed back by unmerge this step
+    int appended = 0;
+    long long mergeEvents = 0, unmergeEvents = 0;
 
     explicit Ctx(const am_params& p);
     ~Ctx();
@@ -181,10 +248,79 @@ struct Ctx {
     int step(double dt);
     int stepWithMerging(double dt);
     int collectStats();
+    void foldTiming();
     int getBodies(am_body_state* out);
+    // merging (merging.cu)
+    void addToBodyLists(int p);
+    void addToBodyListsParent(int p);
+    void removeFromBodyLists(int p);
+    void removeFromBodyListsParent(int p);
+    void removeEmptyBodyPairContacts();
+    int updateBodyPairContacts();
+    int pullBodies();
+    int pushBodies();
+    int ensureStore(int need);
+    int copyContacts(const DContacts& S, const std::vector<int>& si, DContacts& D, const std::vector<int>& di, int mode);
+    int newSlot();
+    int toInternal(int p);
+    int ensureSweep(int need);
+    void nextLayer(std::vector<int>& layer, std::vector<int>& ordered);
+    int singleSweep(double dt);
+    int metrics(const std::vector<int>& a, const std::vector<int>& b, const std::vector<int>& mode, std::vector<double>& out);
+    int accumulateForUnmerging();
+    int pullStates(bool internalToo);
+    int newCollectionSlot();
+    void collApplyVelocitiesTo(int c, int b);
+    void collUpdateState(int c, int b);
+    void collUpdateBB(int c, int b);
+    void setBB(int c, amd::v3 mn, amd::v3 mx);
+    void collUpdateBBAll(int c);
+    void collAddInternal(int c, int b);
+    void collInertiaRestInvert(int c);
+    void rotInertia(int b);
+    void collBodiesTransforms(int c);
+    void collAddBody(int c, int b);
+    void collAddBodies(int c, const std::vector<int>& bs);
+    void collAddCollection(int c, int o);
+    void freeCollection(int c);
+    int newCollection(int b1, int b2);
+    void collRemoveBodies(int c, const std::vector<int>& rm);
+    void collAddBPCs(int p);
+    void collFillInternal(int c);
+    int collAddIncomplete(int body, std::vector<int>& removal);
+    void collUnmergeBody(int c, int b);
+    bool checkMergeCondition(int p);
+    int merge();
+    void buildNeighbor(int b, OSetI& sub, OSetI& handled);
+    int unmergeSelected(int coll, OSetI& sel, std::vector<int>& newBodies, bool& removeCollection);
+    int unmerge();
+    int clearBodyPairContacts();
+    int accumulateForMerging();
+    int uploadExternalFlags();
+    int appendFromStore(const std::vector<int>& slots, std::vector<int>& newIdx);
+    int ensurePairsKeep(int need);
+    int flushAppendedPairs();
+    void advVel(double dt);
+    void advPos(double dt);
+    int sleepDecay();
+    int getTopology(int* items, int* itemOff, int capItems, int* nTop, int* nItems);
+    int putBodies(const am_body_state* in);
     int getContacts(am_contacts* out, int capacity, int* n);
 };
 
-const void* pgs_coloured_kernel();
+// device allocation owned by the context (freed in release())
+template <class T>
+int Ctx::alloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    if (cudaMalloc((void**)p, sizeof(T) * n) != cudaSuccess) { err = "cudaMalloc failed"; return AM_E_CUDA; }
+    allocs.push_back((void*)*p);
+    return AM_OK;
+}
+
+const void* pgs_fast_kernel();
+void launch_refresh_inertia(const DBodies& B, int n, cudaStream_t s);
+void launch_sub_adv_vel(const DBodies& B, const int* top, int ntop, const int* so, const int* si, double dt,
+                        cudaStream_t s);
 
 }  // namespace am

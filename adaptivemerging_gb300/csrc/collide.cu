@@ -24,6 +24,8 @@
 namespace am {
 using namespace amd;
 
+long long g_launches = 0;
+
 // ---------------------------------------------------------------------------
 // exclusive scan of int32 (block-local scan, scan of block sums, add)
 static const int SCAN_T = 256, SCAN_E = 4, SCAN_B = SCAN_T * SCAN_E;
@@ -80,8 +82,10 @@ void launch_scan(const int* in, int* out, int n, Scratch& sc, int* total, cudaSt
     int nb = (n + SCAN_B - 1) / SCAN_B;
     // nb <= SCAN_B is guaranteed by the callers' capacities (n <= 2^20)
     k_scan_block<<<nb, SCAN_T, 0, s>>>(in, out, n, sc.block);
+    AM_LAUNCHED(1);
     k_scan_sums<<<1, SCAN_T, 0, s>>>(sc.block, nb, total);
-    if (nb > 1) k_scan_add<<<nb, SCAN_T, 0, s>>>(out, n, sc.block);
+    AM_LAUNCHED(1);
+    if (nb > 1) { k_scan_add<<<nb, SCAN_T, 0, s>>>(out, n, sc.block); AM_LAUNCHED(1); }
 }
 
 // ---------------------------------------------------------------------------
@@ -100,6 +104,7 @@ __global__ void k_bv_update(DBodies B, DNodes N) {
 void launch_bv_update(const DBodies& B, const DNodes& N, cudaStream_t s) {
     if (N.n == 0) return;
     k_bv_update<<<(N.n + 255) / 256, 256, 0, s>>>(B, N);
+    AM_LAUNCHED(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -175,8 +180,9 @@ int launch_broadphase(const DBodies& B, const DNodes& N, const int* top, int nto
     int warps = ntop - 1;
     int blocks = (warps * 32 + 255) / 256;
     k_broad_rows<false><<<blocks, 256, 0, s>>>(B, N, top, ntop, rowCount, nullptr, nullptr, nullptr, 0);
+    AM_LAUNCHED(1);
     launch_scan(rowCount, rowOff, ntop - 1, sc, &dc->n_cand, s);
-    if (candA) k_broad_rows<true><<<blocks, 256, 0, s>>>(B, N, top, ntop, nullptr, rowOff, candA, candB, candCap);
+    if (candA) { k_broad_rows<true><<<blocks, 256, 0, s>>>(B, N, top, ntop, nullptr, rowOff, candA, candB, candCap); AM_LAUNCHED(1); }
     return 0;
 }
 
@@ -213,8 +219,10 @@ void launch_expand_pairs(const DBodies& B, const int* sub_off, const int* sub_id
                          const int* candB, int ncand, DPairs& P, Scratch& sc, DCount* dc, cudaStream_t s) {
     if (ncand <= 0) { cudaMemsetAsync(&dc->n_pairs, 0, sizeof(int), s); return; }
     k_expand_count<<<(ncand + 255) / 256, 256, 0, s>>>(B, sub_off, candA, candB, dc, sc.tmp);
+    AM_LAUNCHED(1);
     launch_scan(sc.tmp, sc.tmp2, ncand, sc, &dc->n_pairs, s);
     k_expand_write<<<(ncand + 255) / 256, 256, 0, s>>>(B, sub_off, sub_ids, candA, candB, dc, sc.tmp2, P);
+    AM_LAUNCHED(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -745,6 +753,7 @@ void launch_narrow(const DBodies& B, const DNodes& N, DPairs& P, DContacts& C, S
     (void)sc;
     if (!emit) k_narrow_count<<<4 * 152, 128, 0, s>>>(B, N, P, dc);
     else k_narrow_emit<<<4 * 152, 128, 0, s>>>(B, N, P, C, dc);
+    AM_LAUNCHED(1);
 }
 
 }  // namespace am

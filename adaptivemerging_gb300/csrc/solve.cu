@@ -14,10 +14,8 @@
 //      - AM_ORDER_REFERENCE: one thread walks the contacts in list order --
 //        bit-identical to the reference;
 //      - AM_ORDER_COLOURED: body-pair groups are greedily coloured so that no
-//        two groups of one colour share a dynamic body; a persistent
-//        cooperative kernel sweeps colour by colour with a bounded grid
-//        barrier between colours.  Contacts of one pair stay sequential in
-//        list order inside their group.
+//        two groups of one colour share a dynamic body (colouring here; the
+//        sweep kernel is in pgs_fast.cu).
 //
 // Compiled with --fmad=false (see am_dev.cuh).
 #include <cooperative_groups.h>
@@ -65,7 +63,7 @@ __global__ void k_ws_build(DContacts P, int nprev, DHash H) {
 
 void launch_ws_build(const DContacts& prev, int nprev, DHash& H, cudaStream_t s) {
     cudaMemsetAsync(H.slot, 0xff, sizeof(int) * H.cap, s);
-    if (nprev > 0) k_ws_build<<<(nprev + 255) / 256, 256, 0, s>>>(prev, nprev, H);
+    if (nprev > 0) { k_ws_build<<<(nprev + 255) / 256, 256, 0, s>>>(prev, nprev, H); AM_LAUNCHED(1); }
 }
 
 __device__ int ws_lookup(const DContacts& cur, int c, int info, const DContacts& P, const DHash& H) {
@@ -160,6 +158,7 @@ void launch_warm_start(const DBodies& B, DContacts& cur, DContacts& prev, const 
                        int npairs, int nprev, cudaStream_t s) {
     if (npairs <= 0) return;
     k_warm_start<<<(npairs + 127) / 128, 128, 0, s>>>(B, cur, prev, H, P, npairs, nprev);
+    AM_LAUNCHED(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -218,6 +217,7 @@ void launch_solve_prep(const DBodies& B, DContacts& C, int nc, double dt, double
                        double restVal, int redoWarm, cudaStream_t s) {
     if (nc <= 0) return;
     k_solve_prep<<<(nc + 127) / 128, 128, 0, s>>>(B, C, nc, dt, fb, inColl ? 1 : 0, restOv, restVal, redoWarm);
+    AM_LAUNCHED(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -347,6 +347,7 @@ void launch_pgs_exact(DBodies& B, DContacts& C, int nc, const int* order, int it
                       double tol, bool inColl, int fo, double fv, double slide, DCount* dc, cudaStream_t s) {
     if (nc <= 0) return;
     k_pgs_exact<<<1, 32, 0, s>>>(B, C, nc, order, iters, omega, comp, tol, inColl ? 0 : 1, fo, fv, slide, dc);
+    AM_LAUNCHED(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -418,9 +419,11 @@ void colour_groups(const DBodies& B, const DContacts& C, DPairs& P, int npairs, 
     if (npairs <= 0) { cudaMemsetAsync(&dc->n_colours, 0, sizeof(int), s); return; }
     cudaMemsetAsync(colourCnt, 0, sizeof(int) * (maxC + 1), s);
     k_colour<<<1, 1024, 0, s>>>(B, C, P, npairs, colourOf, colourCnt, maxC, bodyMax, nbodies, dc);
+    AM_LAUNCHED(1);
     launch_scan(colourCnt, colourOff, maxC + 1, sc, nullptr, s);
     cudaMemsetAsync(fill, 0, sizeof(int) * maxC, s);
     k_colour_place<<<(npairs + 255) / 256, 256, 0, s>>>(P, npairs, colourOf, colourOff, fill, groupOrder);
+    AM_LAUNCHED(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -455,63 +458,6 @@ __device__ __forceinline__ bool grid_barrier(DCount* dc, int nblocks) {
 __device__ __forceinline__ double warp_max(double v) {
     for (int o = 16; o > 0; o >>= 1) v = jmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
-}
-
-__global__ void k_pgs_coloured(DBodies B, DContacts C, DPairs P, const int* groupOrder, const int* colourOff,
-                               int ncol, int iters, double omega, double comp, double tol, int early, int fo,
-                               double fv, double slide, DCount* dc) {
-    int nblocks = gridDim.x;
-    int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    int nth = nblocks * blockDim.x;
-    // confidentWarmStart, colour by colour
-    for (int col = 0; col < ncol; col++) {
-        for (int k = colourOff[col] + tid; k < colourOff[col + 1]; k += nth) {
-            int g = groupOrder[k];
-            for (int c = P.off[g]; c < P.off[g] + P.count[g]; c++) warm_apply(B, C, c);
-        }
-        if (!grid_barrier(dc, nblocks)) return;
-    }
-    int done = 0;
-    double change = 0;
-    for (int it = 0; it < iters; it++) {
-        int par = it & 1;
-        bool last = (it == iters - 1);
-        double mx = 0;
-        for (int col = 0; col < ncol; col++) {
-            for (int k = colourOff[col] + tid; k < colourOff[col + 1]; k += nth) {
-                int g = groupOrder[k];
-                for (int c = P.off[g]; c < P.off[g] + P.count[g]; c++)
-                    mx = jmax(mx, contact_sweep(B, C, c, omega, comp, fo, fv, last, slide));
-            }
-            if (col == ncol - 1) {
-                double wm = warp_max(mx);
-                if ((threadIdx.x & 31) == 0 && wm > 0) atomicMax(&dc->maxchg[par], (unsigned long long)__double_as_longlong(wm));
-            }
-            if (!grid_barrier(dc, nblocks)) return;
-        }
-        change = __longlong_as_double((long long)*(volatile unsigned long long*)&dc->maxchg[par]);
-        done = it + 1;
-        if (tid == 0) dc->maxchg[par ^ 1] = 0ull;
-        if (early && change < tol) break;
-    }
-    if (tid == 0) {
-        dc->sweeps = done;
-        dc->maxchg[0] = __double_as_longlong(change);
-    }
-}
-
-const void* pgs_coloured_kernel() { return (const void*)k_pgs_coloured; }
-
-void launch_pgs_coloured(DBodies& B, DContacts& C, DPairs& P, const int* groupOrder, const int* colourOff,
-                         int ncol, int iters, double omega, double comp, double tol, bool early, int fo,
-                         double fv, double slide, DCount* dc, int gridBlocks, cudaStream_t s) {
-    if (ncol <= 0) return;
-    cudaMemsetAsync(&dc->maxchg, 0, sizeof(unsigned long long) * 2, s);
-    cudaMemsetAsync(&dc->bar_count, 0, sizeof(int) * 2, s);
-    int earlyI = early ? 1 : 0;
-    void* args[] = {&B, &C, &P, (void*)&groupOrder, (void*)&colourOff, &ncol, &iters, &omega, &comp, &tol,
-                    &earlyI, &fo, &fv, &slide, &dc};
-    cudaLaunchCooperativeKernel((void*)k_pgs_coloured, dim3(gridBlocks), dim3(128), args, 0, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -555,6 +501,7 @@ void launch_residual(const DBodies& B, DContacts& C, int nc, double comp, int fo
     cudaMemsetAsync(&dc->res_abs, 0, sizeof(double) * 2, s);
     if (nc <= 0) return;
     k_residual<<<(nc + 255) / 256, 256, 0, s>>>(B, C, nc, comp, fo, fv, dc);
+    AM_LAUNCHED(1);
 }
 
 // CollisionProcessor.clearBodyPairContacts: a pair survives when one of its
@@ -571,6 +518,7 @@ __global__ void k_bpc_keep(DContacts C, DPairs P, int npairs) {
 void launch_bpc_keep(const DContacts& C, DPairs& P, int npairs, cudaStream_t s) {
     if (npairs <= 0) return;
     k_bpc_keep<<<(npairs + 255) / 256, 256, 0, s>>>(C, P, npairs);
+    AM_LAUNCHED(1);
 }
 
 }  // namespace am

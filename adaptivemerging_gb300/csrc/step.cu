@@ -166,6 +166,13 @@ __global__ void k_sub_adv_vel(DBodies B, const int* top, int ntop, const int* so
     for (int k = 0; k < 6; k++) B.dv[6 * b + k] = 0.0;
 }
 
+void launch_sub_adv_vel(const DBodies& B, const int* top, int ntop, const int* so, const int* si, double dt,
+                        cudaStream_t s) {
+    if (ntop <= 0) return;
+    k_sub_adv_vel<<<(ntop + 127) / 128, 128, 0, s>>>(B, top, ntop, so, si, dt);
+    AM_LAUNCHED(1);
+}
+
 // MotionMetricProcessor.getLargestVelocityNorm(body) (MotionMetricProcessor.java:64-73)
 __device__ double metric1(const DBodies& B, int b) {
     double largest = 0;
@@ -250,6 +257,22 @@ __global__ void k_sleep_decay(DBodies B, const int* top, int ntop, int* ext, int
     stv(B.w + 3 * b, w);
 }
 
+// am_put_bodies: after x / R / v / omega of free bodies were overwritten from
+// the host, refresh the rotated inertia as RigidBody.updateRotationalInertiaFromTransformation does
+__global__ void k_refresh_inertia(DBodies B, int n) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n || (B.flags[b] & F_PINNED)) return;
+    m3 R = ldm(B.R + 9 * b);
+    stm(B.M + 9 * b, rm0rt(R, ldm(B.M0 + 9 * b)));
+    stm(B.jinv + 9 * b, rm0rt(R, ldm(B.jinv0 + 9 * b)));
+}
+
+void launch_refresh_inertia(const DBodies& B, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_refresh_inertia<<<(n + 127) / 128, 128, 0, s>>>(B, n);
+    AM_LAUNCHED(1);
+}
+
 // ---------------------------------------------------------------------------
 static int g_numSMs = 0;
 
@@ -262,12 +285,6 @@ static int g_numSMs = 0;
         }                                                                           \
     } while (0)
 
-template <class T>
-static cudaError_t dalloc(T** p, size_t n) {
-    *p = nullptr;
-    if (n == 0) n = 1;
-    return cudaMalloc((void**)p, sizeof(T) * n);
-}
 
 Ctx::Ctx(const am_params& p) : P(p) {
     std::memset(&B, 0, sizeof(B));
@@ -291,12 +308,6 @@ void Ctx::release() {
     stream = nullptr;
 }
 
-template <class T>
-int Ctx::alloc(T** p, size_t n) {
-    if (dalloc(p, n) != cudaSuccess) { err = "cudaMalloc failed"; return AM_E_CUDA; }
-    allocs.push_back((void*)*p);
-    return AM_OK;
-}
 
 int Ctx::allocContacts(DContacts& c, int cap) {
     c.cap = cap;
@@ -427,6 +438,15 @@ int Ctx::setScene(const am_scene& s) {
     totalSteps = 0;
     mergingEvent = false;
     if (allocContacts(C[0], 1024) || allocContacts(C[1], 1024)) return AM_E_CUDA;
+    std::memset(&I, 0, sizeof(I));
+    std::memset(&Sw, 0, sizeof(Sw));
+    idxCap = metCap = 0;
+    M.reset(host.cap);
+    devDv.assign(6 * (size_t)host.cap, 0.0);
+    mergeEvents = unmergeEvents = 0;
+    appended = 0;
+    if (alloc(&nbbDev, host.cap)) return AM_E_CUDA;
+    CK(cudaMemcpyAsync(nbbDev, host.nbb.data(), sizeof(int) * host.cap, cudaMemcpyHostToDevice, stream));
     H.cap = 0;
     if (ensurePairs(1024) || ensureCand(1024)) return AM_E_CUDA;
     return syncErr();
@@ -512,9 +532,11 @@ void Ctx::gravityDir(double g[3]) const {
 int Ctx::beginStep(int mode) {
     double g[3];
     gravityDir(g);
-    if (ntop > 0)
+    if (ntop > 0) {
         k_begin<<<(ntop + 127) / 128, 128, 0, stream>>>(B, top, ntop, subOff, subIds, mk(g[0], g[1], g[2]),
                                                         P.use_gravity, mode);
+        AM_LAUNCHED(1);
+    }
     return AM_OK;
 }
 
@@ -575,7 +597,9 @@ int Ctx::warmStart() {
 int Ctx::wake() {
     if (!P.enable_sleeping || nPairs <= 0) return AM_OK;
     k_wake_mark<<<(nPairs + 255) / 256, 256, 0, stream>>>(B, PR, nPairs, wakeFlag);
+    AM_LAUNCHED(1);
     k_wake_apply<<<(host.cap + 255) / 256, 256, 0, stream>>>(B, host.cap, wakeFlag);
+    AM_LAUNCHED(1);
     return AM_OK;
 }
 
@@ -585,6 +609,11 @@ int Ctx::runPGS(int nc, const int* order, int iters, bool inColl, double dt, boo
     DContacts& c = C[cur];
     launch_solve_prep(B, c, nc, dt, P.feedback_stiffness, inColl, P.restitution_override, P.restitution,
                       redoWarm ? 1 : 0, stream);
+    bool timed = !inColl;
+    if (timed) {
+        if (!evA) { cudaEventCreate(&evA); cudaEventCreate(&evB); }
+        cudaEventRecord(evA, stream);
+    }
     if (P.solver_order == AM_ORDER_REFERENCE || inColl) {
         launch_pgs_exact(B, c, nc, order, iters, P.omega, comp, P.tolerance, inColl, P.friction_override,
                          P.friction, P.sliding_threshold, dc, stream);
@@ -596,14 +625,34 @@ int Ctx::runPGS(int nc, const int* order, int iters, bool inColl, double dt, boo
         int ncol = hc->n_colours;
         if (!coopBlocks) {
             int per = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)pgs_coloured_kernel(), 128, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pgs_fast_kernel(), 128, 0);
             coopBlocks = std::max(1, std::min(per, 4)) * g_numSMs;
         }
-        int blocks = std::min(coopBlocks, std::max(1, (nPairs + 127) / 128 * 2));
-        launch_pgs_coloured(B, c, PR, groupOrder, colourOff, ncol, iters, P.omega, comp, P.tolerance, !inColl,
-                            P.friction_override, P.friction, P.sliding_threshold, dc, blocks, stream);
+        if (nc > mjCap) {
+            int cap2 = std::max(nc + nc / 2, 1024);
+            if (alloc(&Mj, 36 * (size_t)cap2) || alloc(&invD, 3 * (size_t)cap2)) return AM_E_CUDA;
+            mjCap = cap2;
+        }
+        // 8 half-warp groups per block; enough blocks for every group of the largest colour
+        int blocks = std::min(coopBlocks, std::max(1, (nPairs + 7) / 8));
+        if (timed) cudaEventRecord(evA, stream);   // time the sweep (prep + persistent kernel)
+        launch_pgs_fast(B, c, PR, groupOrder, colourOff, ncol, nc, iters, P.omega, comp, P.tolerance, !inColl,
+                        P.friction_override, P.friction, P.sliding_threshold, Mj, invD, mjCap, dc, blocks, stream);
     }
+    if (timed) { cudaEventRecord(evB, stream); pgsPending = true; }
     return AM_OK;
+}
+
+// after a synchronising read: fold the timed PGS launch into the counters
+void Ctx::foldTiming() {
+    if (!pgsPending) return;
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, evA, evB) == cudaSuccess) {
+        perf.pgs_ms += ms;
+        perf.pgs_launches += 1;
+        perf.contact_sweeps += (long long)nContacts * (long long)hc->sweeps;
+    }
+    pgsPending = false;
 }
 
 // CollisionProcessor.solveLCP (+ the redoWarmStart that precedes it)
@@ -615,16 +664,38 @@ int Ctx::solveLCP(double dt, bool redoWarm) {
     return AM_OK;
 }
 
+void Ctx::advVel(double dt) {
+    if (ntop <= 0) return;
+    k_adv_vel<<<(ntop + 127) / 128, 128, 0, stream>>>(B, top, ntop, subOff, subIds, dt);
+    AM_LAUNCHED(1);
+}
+
+void Ctx::advPos(double dt) {
+    if (ntop <= 0) return;
+    k_adv_pos<<<(ntop + 127) / 128, 128, 0, stream>>>(B, top, ntop, subOff, subIds, dt);
+    AM_LAUNCHED(1);
+}
+
+int Ctx::sleepDecay() {
+    if (ntop <= 0) return AM_OK;
+    k_sleep_decay<<<(ntop + 127) / 128, 128, 0, stream>>>(B, top, ntop, extFlag, P.enable_sleeping,
+                                                          P.sleep_step_accum, P.sleep_threshold,
+                                                          P.viscous_linear, P.viscous_angular);
+    AM_LAUNCHED(1);
+    return AM_OK;
+}
+
+// clearBodyPairContacts, advanceBodiesVelocities / Positions, sleep, viscous
+// decay of the step without merging (pairs are this step's contact runs)
 int Ctx::finishStep(double dt) {
     launch_bpc_keep(C[cur], PR, nPairs, stream);
-    if (ntop > 0) k_adv_vel<<<(ntop + 127) / 128, 128, 0, stream>>>(B, top, ntop, subOff, subIds, dt);
-    if (ntop > 0) k_adv_pos<<<(ntop + 127) / 128, 128, 0, stream>>>(B, top, ntop, subOff, subIds, dt);
-    if (nPairs > 0) k_ext_mark<<<(nPairs + 255) / 256, 256, 0, stream>>>(B, PR, nPairs, extFlag);
-    if (ntop > 0)
-        k_sleep_decay<<<(ntop + 127) / 128, 128, 0, stream>>>(B, top, ntop, extFlag, P.enable_sleeping,
-                                                              P.sleep_step_accum, P.sleep_threshold,
-                                                              P.viscous_linear, P.viscous_angular);
-    return AM_OK;
+    advVel(dt);
+    advPos(dt);
+    if (nPairs > 0) {
+        k_ext_mark<<<(nPairs + 255) / 256, 256, 0, stream>>>(B, PR, nPairs, extFlag);
+        AM_LAUNCHED(1);
+    }
+    return sleepDecay();
 }
 
 int Ctx::step(double dt) {
@@ -637,7 +708,10 @@ int Ctx::step(double dt) {
     if ((r = wake())) return r;
     if ((r = solveLCP(dt, P.warm_start != 0))) return r;
     if ((r = finishStep(dt))) return r;
-    return readCounts() ? AM_E_CUDA : collectStats();
+    if ((r = readCounts())) return r;
+    foldTiming();
+    perf.steps++;
+    return collectStats();
 }
 
 int Ctx::collectStats() {

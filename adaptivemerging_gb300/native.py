@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libam.so")
 EXPORTS = [
     "am_params_default", "am_create", "am_destroy", "am_last_error", "am_set_params", "am_set_scene",
     "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
-    "am_num_contacts", "am_get_contacts", "am_get_stats",
+    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology",
 ]
 
 _lib = None
@@ -55,6 +55,12 @@ def lib():
         L.am_num_contacts.argtypes = [vp, C.POINTER(C.c_int32)]
         L.am_get_contacts.argtypes = [vp, C.POINTER(abi.am_contacts), C.c_int32, C.POINTER(C.c_int32)]
         L.am_get_stats.argtypes = [vp, C.POINTER(abi.am_solve_stats)]
+        L.am_get_perf.argtypes = [vp, C.POINTER(abi.am_perf)]
+        L.am_put_bodies.argtypes = [vp, C.POINTER(abi.am_body_state)]
+        L.am_get_topology.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32,
+                                      C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.am_reset_perf.argtypes = [vp]
+        L.am_get_stream.argtypes = [vp, C.POINTER(vp)]
         for f in EXPORTS:
             if f not in ("am_params_default", "am_last_error"):
                 getattr(L, f).restype = C.c_int32
@@ -117,6 +123,23 @@ class System:
         self._check(lib().am_get_stats(self.h, C.byref(st)))
         return st
 
+    def perf(self):
+        p = abi.am_perf()
+        self._check(lib().am_get_perf(self.h, C.byref(p)))
+        return p
+
+    def reset_perf(self):
+        self._check(lib().am_reset_perf(self.h))
+
+    def stream_handle(self):
+        s = C.c_void_p()
+        self._check(lib().am_get_stream(self.h, C.byref(s)))
+        return s.value
+
+    def set_params(self, params):
+        self.params = params
+        self._check(lib().am_set_params(self.h, C.byref(params)))
+
     def num_contacts(self):
         n = C.c_int32()
         self._check(lib().am_num_contacts(self.h, C.byref(n)))
@@ -129,6 +152,27 @@ class System:
         got = C.c_int32()
         self._check(lib().am_get_contacts(self.h, C.byref(s), buf.n, C.byref(got)))
         return buf.view(got.value)
+
+    def put_bodies_struct(self, st_struct):
+        self._check(lib().am_put_bodies(self.h, C.byref(st_struct)))
+
+    def get_bodies_struct(self, st_struct):
+        self._check(lib().am_get_bodies(self.h, C.byref(st_struct)))
+
+    def topology(self):
+        """RigidBodySystem.bodies: ints for free bodies, tuples of members for collections."""
+        cap = 4 * self.n + 64
+        items = np.zeros(cap, np.int32)
+        off = np.zeros(2 * self.n + 8, np.int32)
+        nt, ni = C.c_int32(), C.c_int32()
+        P32 = C.POINTER(C.c_int32)
+        self._check(lib().am_get_topology(self.h, items.ctypes.data_as(P32), off.ctypes.data_as(P32), cap,
+                                          C.byref(nt), C.byref(ni)))
+        out = []
+        for t in range(nt.value):
+            seg = [int(x) for x in items[off[t]:off[t + 1]]]
+            out.append(tuple(seg[1:]) if seg[0] == -1 else seg[0])
+        return out
 
     def bodies(self):
         st = abi.BodyState(self.n)

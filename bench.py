@@ -1,0 +1,302 @@
+#!/usr/bin/env python3
+"""Headline benchmark: simulated steps per second of the contact hot path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload wall|tower]
+
+A step is one RigidBodySystem.advanceTime of the workload scene: collision
+detection, contact setup, warm start, the projected Gauss-Seidel solve,
+integration and sleeping.  `value` is steps/s with the state resident in HBM
+(device time of K steps measured with CUDA events on the library's stream,
+L2 flushed between steps); `e2e` runs the same steps through the C ABI with
+the body state pushed from and read back into pinned host buffers every step.
+`--impl reference` times the CPU restatement of the reference path (the
+oracle) on the same workload.  The workload is a single scene, so several GPUs
+run independent replicas ("replicas only"): value = all ranks' steps / max time.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from adaptivemerging_gb300 import abi, scenes  # noqa: E402
+
+METRIC = "sim steps/s at LCP residual<=1e-6: warm-start+batched vs plain GPU PGS, 1 GB300"
+FP64_BYTES_PER_CONTACT_SWEEP = 736   # J 288 + b,D 48 + lambda r/w 48 + dv of 2 bodies r/w 192 + minv,jinv 160
+
+
+def workload(name):
+    """Scene, parameters, dt and a description of the named workload."""
+    if name == "wall":
+        sc = scenes.wall(cols=40, rows=25, seed=2)
+        P = abi.default_params(gravity_amount=9.81, friction_override=1, friction=0.5, restitution_override=1,
+                               restitution=0.0, iterations=200, enable_merging=0,
+                               solver_order=abi.AM_ORDER_COLOURED)
+        return sc, P, 0.005, {
+            "workload": "brick wall 40x25 (0.4x0.2x0.2 m, 1000 kg/m3) + 50 kg sphere at 15 m/s",
+            "bodies": int(sc.n), "dt": 0.005, "pgs_iterations": 200, "mu": 0.5,
+            "merging": "off", "pgs_order": "coloured", "precision": "fp64"}
+    if name == "tower":
+        sc = scenes.tower(25, seed=1)
+        P = abi.default_params(gravity_amount=9.81, friction_override=1, friction=0.6, restitution_override=1,
+                               restitution=0.0, iterations=100, enable_merging=0,
+                               solver_order=abi.AM_ORDER_COLOURED)
+        return sc, P, 0.01, {"workload": "tower of 25 boxes 1.0x0.5x1.0 m", "bodies": int(sc.n), "dt": 0.01,
+                             "pgs_iterations": 100, "mu": 0.6, "merging": "off", "pgs_order": "coloured",
+                             "precision": "fp64"}
+    raise SystemExit(f"unknown workload {name}")
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("AM_BENCH_GLOO") is None else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x, device=None):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(name, max_seconds=15.0, max_steps=400):
+    """Oracle (single-threaded CPU restatement of the reference path) on the
+    same workload: steps/s over a bounded sample from the initial scene."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_binding import Oracle
+    sc, P, dt, _ = workload(name)
+    P.solver_order = abi.AM_ORDER_REFERENCE
+    o = Oracle(sc, P)
+    o.step(dt, 2)
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps and time.perf_counter() - t0 < max_seconds:
+        o.step(dt)
+        n += 1
+    el = time.perf_counter() - t0
+    return {"value": n / el, "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": f"{n} steps of the same scene from its initial state after 2 warm-up steps "
+                      f"({el:.1f} s, single thread)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_init()
+    if rank != 0:
+        return
+    sc, P, dt, cfg = workload(args.workload)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_binding import Oracle
+    P.solver_order = abi.AM_ORDER_REFERENCE
+    o = Oracle(sc, P)
+    o.step(dt, args.warmup)
+    t0 = time.perf_counter()
+    o.step(dt, args.steps)
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    out = {"metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+           "config": cfg,
+           "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
+                            "sample": f"{args.steps} steps after {args.warmup} warm-up steps, single thread"},
+           "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+    from adaptivemerging_gb300 import build, native
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    build.build()
+    sc, P, dt, cfg = workload(args.workload)
+    sysm = native.System(sc, P)
+    stream = torch.cuda.ExternalStream(sysm.stream_handle())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        sysm.step(dt)
+    sysm.reset_perf()
+    p0 = sysm.perf()
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    total_ms = 0.0
+    sweeps, contacts, res = [], [], []
+    for _ in range(args.steps):
+        flush.fill_(1.0)                     # L2 flush between timed steps
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sysm.step(dt)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        st = sysm.stats()
+        sweeps.append(st.sweeps); contacts.append(st.n_contacts); res.append(st.residual_rel)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(ws)
+    p1 = sysm.perf()
+    t_max = max_over_ranks(ws, total_ms / 1e3, "cuda")
+    value = ws * args.steps / t_max
+
+    # end to end through the C ABI: host-owned state pushed and read back every step
+    n = sc.n
+    pin = {k: torch.zeros(m * n, dtype=torch.float64, pin_memory=True) for k, m in
+           (("x", 3), ("R", 9), ("v", 3), ("omega", 3))}
+    pin_i = {k: torch.zeros(n, dtype=torch.int32, pin_memory=True) for k in ("sleeping", "parent")}
+    st_s = abi.am_body_state()
+    for k, t in pin.items():
+        setattr(st_s, k, C.cast(t.data_ptr(), C.POINTER(C.c_double)))
+    for k, t in pin_i.items():
+        setattr(st_s, k, C.cast(t.data_ptr(), C.POINTER(C.c_int32)))
+    sysm.get_bodies_struct(st_s)
+    h2d = sum(t.numel() * 8 for t in pin.values())
+    d2h = h2d + sum(t.numel() * 4 for t in pin_i.values())
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sysm.put_bodies_struct(st_s)
+        sysm.step(dt)
+        sysm.get_bodies_struct(st_s)
+    e2e_t = max_over_ranks(ws, time.perf_counter() - t0, "cuda")
+    e2e = ws * args.steps / e2e_t
+
+    pgs_l = p1.pgs_launches - p0.pgs_launches
+    pgs_ms = p1.pgs_ms - p0.pgs_ms
+    cs = p1.contact_sweeps - p0.contact_sweeps
+    peak, peak_kind = measured_peak()
+    achieved = (cs * FP64_BYTES_PER_CONTACT_SWEEP / pgs_l) / (pgs_ms / pgs_l / 1e3) / 1e9 if pgs_l and pgs_ms else 0.0
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "pgs_traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f).get(args.workload)
+    if rank != 0:
+        return
+    cfg.update({"contacts_mean": float(np.mean(contacts)), "pgs_sweeps_mean": float(np.mean(sweeps)),
+                "residual_rel_mean": float(np.mean(res)), "residual_rel_max": float(np.max(res)),
+                "frac_steps_residual_le_1e-6": float(np.mean(np.array(res) <= 1e-6)),
+                "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas only"})
+    out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+           "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "gpu_launches": int(p1.launches - p0.launches),
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak if peak else None, "traffic": traffic,
+                        "kernel": "k_pgs_coloured", "peak_source": peak_kind,
+                        "bytes_per_contact_sweep": FP64_BYTES_PER_CONTACT_SWEEP,
+                        "pgs_ms_per_launch": pgs_ms / pgs_l if pgs_l else None},
+           "clocks": clk}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args.workload)
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="wall")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

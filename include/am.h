@@ -172,6 +172,18 @@ typedef struct am_solve_stats {
     double  residual_rel;    /* residual_abs / max(1, |lambda|_inf)              */
 } am_solve_stats;
 
+/* Performance counters of one context (no reference counterpart; used by the
+ * benchmark to compute the roofline of the PGS sweep kernel). */
+typedef struct am_perf {
+    int64_t launches;        /* kernels launched by libam since it was loaded   */
+    int64_t pgs_launches;    /* full-solve PGS sweep launches of this context  */
+    double  pgs_ms;          /* their summed device time (CUDA events on the context stream) */
+    int64_t contact_sweeps;  /* sum of contacts x sweeps over those launches    */
+    int64_t steps;           /* am_step calls                                   */
+    int64_t merge_events;    /* body pairs merged since the scene was loaded    */
+    int64_t unmerge_events;  /* collections split since the scene was loaded    */
+} am_perf;
+
 /* ---- lifecycle ---------------------------------------------------------- */
 void        am_params_default(am_params* p);
 /* new context on the current CUDA device */
@@ -197,9 +209,28 @@ int32_t am_integrate(void* ctx, double dt);
 
 /* Read back. */
 int32_t am_get_bodies(void* ctx, am_body_state* out);
+/* Write x / R / v / omega of the free scene bodies (a caller that owns the
+ * body objects, as the Java RigidBody list does, pushes its state before a
+ * step); bodies inside a collection follow their collection and are skipped.
+ * Replaces the state the reference keeps in RigidBody.x/theta/v/omega
+ * (RigidBody.java:89-96). */
+int32_t am_put_bodies(void* ctx, const am_body_state* in);
 int32_t am_num_contacts(void* ctx, int32_t* n);
 int32_t am_get_contacts(void* ctx, am_contacts* out, int32_t capacity, int32_t* n);
 int32_t am_get_stats(void* ctx, am_solve_stats* out);
+
+/* Top-level body list (RigidBodySystem.bodies, RigidBodySystem.java:31) with
+ * collection membership (RigidCollection.bodies, RigidCollection.java:28):
+ * entry t spans items[item_off[t] .. item_off[t+1]); a free body is [id], a
+ * collection is [-1, member ids in order].  item_off needs n_top + 1 slots. */
+int32_t am_get_topology(void* ctx, int32_t* items, int32_t* item_off, int32_t cap_items, int32_t* n_top,
+                        int32_t* n_items);
+
+/* Instrumentation (no reference counterpart). */
+int32_t am_get_perf(void* ctx, am_perf* out);
+int32_t am_reset_perf(void* ctx);
+/* the context's cudaStream_t, for callers that order their own work after a step */
+int32_t am_get_stream(void* ctx, void** stream);
 
 #ifdef __cplusplus
 }

@@ -16,6 +16,8 @@ void* or_create(const am_params* p, const am_scene* s) {
 
 void or_destroy(void* h) { delete (World*)h; }
 
+void or_set_params(void* h, const am_params* p) { ((World*)h)->P = *p; }
+
 void or_step(void* h, double dt) { ((World*)h)->step(dt); }
 
 void or_run(void* h, double dt, int n) {
@@ -101,6 +103,28 @@ void or_get_counters(void* h, int64_t* out, double* change) {
     out[0] = w->stats.sweeps; out[1] = w->mergeEvents; out[2] = w->unmergeEvents;
     out[3] = (int64_t)w->bodies.size(); out[4] = (int64_t)w->bodyPairContacts.size(); out[5] = ncol;
     if (change) *change = w->stats.last_change;
+}
+
+/* Top-level list with collection members: a body is [id], a collection is
+   [-1, member ids in order]; returns the number of items. */
+int or_topology(void* h, int32_t* items, int32_t* off, int cap, int32_t* ntop) {
+    World* w = (World*)h;
+    int k = 0, t = 0;
+    for (Body* b : w->bodies) {
+        if (off) off[t] = k;
+        if (b->isCollection) {
+            if (items && k < cap) items[k] = -1;
+            k++;
+            for (Body* s : b->bodies) { if (items && k < cap) items[k] = s->id; k++; }
+        } else {
+            if (items && k < cap) items[k] = b->id;
+            k++;
+        }
+        t++;
+    }
+    if (off) off[t] = k;
+    *ntop = t;
+    return k;
 }
 
 /* Top-level body list (RigidBodySystem.bodies) as ids. */

@@ -33,6 +33,7 @@ def lib():
         for f in ("or_destroy", "or_begin_step", "or_collide", "or_warm_start"):
             getattr(L, f).argtypes = [C.c_void_p]
         L.or_step.argtypes = [C.c_void_p, C.c_double]
+        L.or_set_params.argtypes = [C.c_void_p, C.POINTER(abi.am_params)]
         L.or_solve.argtypes = [C.c_void_p, C.c_double]
         L.or_run.argtypes = [C.c_void_p, C.c_double, C.c_int]
         L.or_num_contacts.argtypes = [C.c_void_p]
@@ -42,8 +43,19 @@ def lib():
         L.or_get_counters.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_double)]
         L.or_top_ids.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_int]
         L.or_top_ids.restype = C.c_int
+        L.or_topology.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int,
+                                  C.POINTER(C.c_int32)]
+        L.or_topology.restype = C.c_int
         _lib = L
     return _lib
+
+
+def decode_topology(items, off):
+    out = []
+    for t in range(len(off) - 1):
+        seg = [int(x) for x in items[off[t]:off[t + 1]]]
+        out.append(tuple(seg[1:]) if seg[0] == -1 else seg[0])
+    return out
 
 
 class Oracle:
@@ -58,6 +70,10 @@ class Oracle:
         if getattr(self, "h", None):
             lib().or_destroy(self.h)
             self.h = None
+
+    def set_params(self, params):
+        self.params = params
+        lib().or_set_params(self.h, C.byref(params))
 
     def step(self, dt, n=1):
         lib().or_run(self.h, dt, n)
@@ -97,6 +113,16 @@ class Oracle:
         lib().or_get_counters(self.h, out, C.byref(ch))
         return {"sweeps": out[0], "merges": out[1], "unmerges": out[2], "top": out[3],
                 "bpcs": out[4], "collections": out[5], "last_change": ch.value}
+
+    def topology(self):
+        """Top-level list: ints for free bodies, tuples of member ids for collections."""
+        cap = 4 * self.n + 64
+        items = np.zeros(cap, np.int32)
+        off = np.zeros(2 * self.n + 8, np.int32)
+        nt = C.c_int32()
+        k = lib().or_topology(self.h, items.ctypes.data_as(C.POINTER(C.c_int32)),
+                              off.ctypes.data_as(C.POINTER(C.c_int32)), cap, C.byref(nt))
+        return decode_topology(items[:k], off[:nt.value + 1])
 
     def top_ids(self):
         buf = np.zeros(self.n * 2 + 16, np.int32)

@@ -1,0 +1,52 @@
+"""Adaptive merging on the device path vs the oracle, bit for bit.
+
+With merging on, every step also runs the single sweep inside collections,
+the motion-metric histories, and the merge / unmerge bookkeeping.  In
+reference order all of it is deterministic (insertion-ordered pair sets), so
+after every step the device path must reproduce the oracle exactly: the
+top-level body list with each collection's members in order, the full-solve
+contact list with its multipliers, every body's state, and the merge and
+unmerge event counts.
+"""
+import numpy as np
+import pytest
+
+from adaptivemerging_gb300 import scenes
+from helpers import compare_bodies, compare_contacts, params
+from oracle_binding import Oracle
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "tower12": (lambda: scenes.tower(12, seed=4, density=1.0), 0.01, 160, dict(friction=0.6, iterations=60)),
+    "pile": (lambda: scenes.random_pile(20, seed=9, kinds=("box", "sphere")), 0.01, 220,
+             dict(friction=0.7, iterations=60)),
+    "wall_small": (lambda: scenes.wall(cols=8, rows=6, seed=13), 0.005, 160, dict(friction=0.5, iterations=80)),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_merging_bit_exact(gpu_lib, name):
+    from adaptivemerging_gb300 import native
+    make, dt, steps, over = CASES[name]
+    sc = make()
+    P = params(enable_merging=1, **over)
+    g = native.System(sc, P)
+    o = Oracle(sc, P)
+    merged = 0
+    for s in range(steps):
+        g.step(dt)
+        o.step(dt)
+        tg, to = g.topology(), o.topology()
+        assert tg == to, f"step {s}: topology differs\n{tg}\n{to}"
+        cg, co = g.contacts(), o.contacts()
+        assert len(cg["body1"]) == len(co["body1"]), f"step {s}: contacts {len(cg['body1'])} vs {len(co['body1'])}"
+        msg = compare_contacts(cg, co)
+        assert msg is None, f"step {s}: {msg}"
+        msg = compare_bodies(g.bodies(), o.bodies())
+        assert msg is None, f"step {s}: {msg}"
+        c = o.counters()
+        pg = g.perf()
+        assert (pg.merge_events, pg.unmerge_events) == (c["merges"], c["unmerges"]), f"step {s}"
+        merged = max(merged, sum(1 for t in to if isinstance(t, tuple)))
+    assert merged > 0, "scenario never formed a collection"
