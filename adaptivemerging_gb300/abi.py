@@ -114,6 +114,11 @@ class am_perf(C.Structure):
                 ("unmerge_events", C.c_int64)]
 
 
+class am_batch_stats(C.Structure):
+    _fields_ = [("n_scenes", _i32), ("converged", _i32), ("sweeps_max", _i32), ("threads", _i32),
+                ("sweeps_sum", C.c_int64), ("contact_sweeps", C.c_int64), ("residual_max", _f64)]
+
+
 def ptr(a, ctype):
     """Borrowed pointer to a contiguous numpy array (None -> NULL)."""
     if a is None:

@@ -128,7 +128,8 @@ void launch_begin_step(const DBodies& B, const int* top, int ntop, double gx, do
                        int mergingReapply, cudaStream_t s);
 void launch_bv_update(const DBodies& B, const DNodes& N, cudaStream_t s);
 int launch_broadphase(const DBodies& B, const DNodes& N, const int* top, int ntop, int* candA, int* candB,
-                      int candCap, int* rowCount, int* rowOff, Scratch& sc, DCount* dc, cudaStream_t s);
+                      int candCap, int* rowCount, int* rowOff, Scratch& sc, DCount* dc, cudaStream_t s,
+                      const int* topEnd = nullptr);
 void launch_expand_pairs(const DBodies& B, const int* sub_off, const int* sub_ids, const int* candA,
                          const int* candB, int ncand, DPairs& P, Scratch& sc, DCount* dc, cudaStream_t s);
 void launch_narrow(const DBodies& B, const DNodes& N, DPairs& P, DContacts& C, Scratch& sc, DCount* dc,
@@ -145,9 +146,6 @@ void launch_warm_start(const DBodies& B, DContacts& cur, DContacts& prev, const 
                        int npairs, int nprev, cudaStream_t s);
 void launch_solve_prep(const DBodies& B, DContacts& C, int nc, double dt, double fb, bool inColl,
                        int restOv, double restVal, int redoWarm, cudaStream_t s);
-void launch_pgs_exact(DBodies& B, DContacts& C, int nc, const int* order, int iters, double omega,
-                      double comp, double tol, bool inColl, int frictionOv, double frictionVal, double slide,
-                      DCount* dc, cudaStream_t s);
 void colour_groups(const DBodies& B, const DContacts& C, DPairs& P, int npairs, int* colourOf, int* colourCnt,
                    int* colourOff, int* fill, int* groupOrder, int maxC, unsigned long long* bodyMax, int nbodies,
                    DCount* dc, Scratch& sc, cudaStream_t s);

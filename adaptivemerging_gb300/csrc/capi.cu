@@ -162,10 +162,46 @@ int32_t am_set_scene(void* ctx, const am_scene* s) {
     return c->setScene(*s);
 }
 
+int32_t am_set_batch(void* ctx, const am_scene* scenes, int32_t n) {
+    if (!ctx || !scenes || n <= 0) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (c->P.enable_merging) { c->err = "batched scenes need enable_merging = 0"; return AM_E_ARG; }
+    for (int s = 0; s < n; s++)
+        for (int i = 0; i < scenes[s].n_bodies; i++) {
+            int t = scenes[s].type[i];
+            if (t < AM_BOX || t > AM_TREE) { c->err = "unknown body type"; return AM_E_ARG; }
+        }
+    return c->setBatch(scenes, n);
+}
+
+int32_t am_set_batch_options(void* ctx, int32_t threads, double residual_target, int32_t check_every) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (threads != 0 && (threads < 32 || threads > 1024 || threads % 32)) { c->err = "threads"; return AM_E_ARG; }
+    c->batchThreads = threads;
+    c->batchTol = residual_target;
+    c->batchCheck = check_every < 0 ? 0 : check_every;
+    return AM_OK;
+}
+
+int32_t am_get_batch_stats(void* ctx, am_batch_stats* o) {
+    if (!ctx || !o) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    o->n_scenes = c->nScenes;
+    o->converged = c->batchConverged;
+    o->sweeps_max = c->stats.sweeps;
+    o->threads = c->batchThreads;
+    o->sweeps_sum = c->batchSweepsTotal;
+    o->contact_sweeps = c->batchContactSweepsLast;
+    o->residual_max = c->stats.residual_rel;
+    return AM_OK;
+}
+
 int32_t am_step(void* ctx, double dt) {
     if (!ctx) return AM_E_ARG;
     Ctx* c = (Ctx*)ctx;
     if (!c->stream) { c->err = "no scene loaded"; return AM_E_STATE; }
+    if (c->nScenes > 0 && c->P.enable_merging) { c->err = "batched scenes need enable_merging = 0"; return AM_E_ARG; }
     return c->step(dt);
 }
 

@@ -220,6 +220,37 @@ struct Ctx {
     std::vector<double> lam0H, cvH, icvH, ipcvH;
     std::vector<int> apA, apB, apOff, apCnt;   // pairs handed back by unmerge this step
     int appended = 0;
+    // level-scheduled exact sweep
+    int* levOrder = nullptr;
+    int* levOff = nullptr;
+    int levCap = 0;
+    int gsBlocksMax = 0;
+    std::vector<int> hS1, hS2, hOrder, hLevOff, hLast;
+    // batched scenes (nScenes > 0): concatenated bodies, one CTA per scene in the solve
+    int nScenes = 0;
+    int maxSceneBodies = 0;
+    int* sceneOfDev = nullptr;
+    int* sceneBodyOffDev = nullptr;
+    int* topEnd = nullptr;
+    int* bPairOff = nullptr;
+    float* bRec = nullptr;
+    int2* bLid = nullptr;
+    float* bLam = nullptr;
+    int bRecCap = 0;
+    int* bColour = nullptr;
+    int* bOrder = nullptr;
+    int bPairCap = 0;
+    int* bColOff = nullptr;
+    int* bSweeps = nullptr;
+    float* bRes = nullptr;
+    int batchThreads = 0;        // 0: autotune on the first solve
+    double batchTol = 1e-6;      // relative natural-map residual target
+    int batchCheck = 10;         // sweeps between residual checks
+    long long batchSweepsTotal = 0;
+    long long batchContactSweepsLast = 0;
+    long long* bCS = nullptr;
+    int batchConverged = 0;
+    std::vector<float> tuneMs;
     long long mergeEvents = 0, unmergeEvents = 0;
 
     explicit Ctx(const am_params& p);
@@ -243,6 +274,7 @@ struct Ctx {
     int warmStart();
     int wake();
     int runPGS(int nc, const int* order, int iters, bool inColl, double dt, bool redoWarm);
+    int exactSweep(DContacts& buf, int n, int iters, bool inColl);
     int solveLCP(double dt, bool redoWarm);
     int finishStep(double dt);
     int step(double dt);
@@ -304,6 +336,11 @@ struct Ctx {
     void advPos(double dt);
     int sleepDecay();
     int getTopology(int* items, int* itemOff, int capItems, int* nTop, int* nItems);
+    int setBatch(const am_scene* scenes, int n);
+    int stepBatch(double dt);
+    int batchSolve(double dt);
+    int batchStats();
+    int batchAutotune(double dt);
     int putBodies(const am_body_state* in);
     int getContacts(am_contacts* out, int capacity, int* n);
 };
@@ -319,6 +356,13 @@ int Ctx::alloc(T** p, size_t n) {
 }
 
 const void* pgs_fast_kernel();
+const void* gs_levels_kernel();
+const void* batch_sweep_kernel();
+int gs_levels(const std::vector<int>& s1, const std::vector<int>& s2, const std::vector<int>& flags,
+              std::vector<int>& order, std::vector<int>& levelOff, std::vector<int>& last);
+void launch_gs_levels(const DBodies& B, DContacts& C, const int* order, const int* levelOff, int nLevels, int iters,
+                      double omega, double comp, double tol, bool early, int fo, double fv, double slide,
+                      DCount* dc, int blocks, cudaStream_t s);
 void launch_refresh_inertia(const DBodies& B, int n, cudaStream_t s);
 void launch_sub_adv_vel(const DBodies& B, const int* top, int ntop, const int* so, const int* si, double dt,
                         cudaStream_t s);

@@ -150,17 +150,18 @@ __device__ bool pair_may_touch(const DBodies& B, const DNodes& N, int a, int b) 
 // one warp per row i of the top-level list; ballot + popc keeps row-major order
 template <bool WRITE>
 __global__ void k_broad_rows(DBodies B, DNodes N, const int* top, int ntop, int* rowCount, const int* rowOff,
-                             int* candA, int* candB, int cap) {
+                             int* candA, int* candB, int cap, const int* topEnd) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (warp >= ntop - 1) return;
     int i = warp;
     int a = top[i];
     int run = WRITE ? rowOff[i] : 0;
-    for (int j0 = i + 1; j0 < ntop; j0 += 32) {
+    int end = topEnd ? topEnd[i] : ntop;   // batched scenes: pairs stay inside one scene
+    for (int j0 = i + 1; j0 < end; j0 += 32) {
         int j = j0 + lane;
         bool hit = false;
-        if (j < ntop) hit = pair_may_touch(B, N, a, top[j]);
+        if (j < end) hit = pair_may_touch(B, N, a, top[j]);
         unsigned m = __ballot_sync(0xffffffffu, hit);
         if (WRITE && hit) {
             int pos = run + __popc(m & ((1u << lane) - 1u));
@@ -172,17 +173,18 @@ __global__ void k_broad_rows(DBodies B, DNodes N, const int* top, int ntop, int*
 }
 
 int launch_broadphase(const DBodies& B, const DNodes& N, const int* top, int ntop, int* candA, int* candB,
-                      int candCap, int* rowCount, int* rowOff, Scratch& sc, DCount* dc, cudaStream_t s) {
+                      int candCap, int* rowCount, int* rowOff, Scratch& sc, DCount* dc, cudaStream_t s,
+                      const int* topEnd) {
     if (ntop < 2) {
         cudaMemsetAsync(&dc->n_cand, 0, sizeof(int), s);
         return 0;
     }
     int warps = ntop - 1;
     int blocks = (warps * 32 + 255) / 256;
-    k_broad_rows<false><<<blocks, 256, 0, s>>>(B, N, top, ntop, rowCount, nullptr, nullptr, nullptr, 0);
+    k_broad_rows<false><<<blocks, 256, 0, s>>>(B, N, top, ntop, rowCount, nullptr, nullptr, nullptr, 0, topEnd);
     AM_LAUNCHED(1);
     launch_scan(rowCount, rowOff, ntop - 1, sc, &dc->n_cand, s);
-    if (candA) { k_broad_rows<true><<<blocks, 256, 0, s>>>(B, N, top, ntop, nullptr, rowOff, candA, candB, candCap); AM_LAUNCHED(1); }
+    if (candA) { k_broad_rows<true><<<blocks, 256, 0, s>>>(B, N, top, ntop, nullptr, rowOff, candA, candB, candCap, topEnd); AM_LAUNCHED(1); }
     return 0;
 }
 

@@ -424,10 +424,8 @@ int Ctx::singleSweep(double dt) {
     if (n > 0) {
         k_recompute_J<<<(n + 127) / 128, 128, 0, stream>>>(B, Sw, n, 1);
         AM_LAUNCHED(1);
-        double comp = P.enable_compliance ? P.compliance : 0.;
         launch_solve_prep(B, Sw, n, dt, P.feedback_stiffness, true, P.restitution_override, P.restitution, 0, stream);
-        launch_pgs_exact(B, Sw, n, nullptr, P.iterations_in_collection, P.omega, comp, P.tolerance, true,
-                         P.friction_override, P.friction, P.sliding_threshold, dc, stream);
+        if ((r = exactSweep(Sw, n, P.iterations_in_collection, true))) return r;
         if ((r = copyContacts(Sw, extPos, C[cur], ext, 2))) return r;
         if ((r = copyContacts(Sw, inPos, I, in, 2))) return r;
     }

@@ -11,8 +11,8 @@
 //    contact, plus jinv * J.w for each row and body (the angular part of
 //    M^-1 J^T used by every delta-v update; same arithmetic as recomputing it).
 //  * PGS (PGS.solve, PGS.java:73-256) in two orders:
-//      - AM_ORDER_REFERENCE: one thread walks the contacts in list order --
-//        bit-identical to the reference;
+//      - AM_ORDER_REFERENCE: list order, bit-identical to the reference
+//        (level-scheduled kernel in gs_exact.cu);
 //      - AM_ORDER_COLOURED: body-pair groups are greedily coloured so that no
 //        two groups of one colour share a dynamic body (colouring here; the
 //        sweep kernel is in pgs_fast.cu).
@@ -317,37 +317,6 @@ __device__ void warm_apply(const DBodies& B, const DContacts& C, int c) {
     int s1 = C.sb1[c], s2 = C.sb2[c];
     for (int r = 0; r < 3; r++)
         apply_dv(B, C, c, r, C.lam[r * cap + c], s1, s2, Jrow(C, c, 4 * r), Jrow(C, c, 4 * r + 2));
-}
-
-// reference order: a single thread, PGS.java line by line
-__global__ void k_pgs_exact(DBodies B, DContacts C, int nc, const int* order, int iters, double omega, double comp,
-                            double tol, int early, int fo, double fv, double slide, DCount* dc) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int k = 0; k < nc; k++) warm_apply(B, C, order ? order[k] : k);   // confidentWarmStart
-    int iter = iters, done = 0;
-    double change = 0;
-    while (iter > 0) {
-        double mx = 0;
-        for (int k = 0; k < nc; k++) {
-            int c = order ? order[k] : k;
-            double m = contact_sweep(B, C, c, omega, comp, fo, fv, iter == 1, slide);
-            // PGS tracks the max over the three rows in row order; max is associative here
-            mx = jmax(mx, m);
-        }
-        iter--;
-        done++;
-        change = mx;
-        if (early && mx < tol) break;
-    }
-    dc->sweeps = done;
-    dc->maxchg[0] = __double_as_longlong(change);
-}
-
-void launch_pgs_exact(DBodies& B, DContacts& C, int nc, const int* order, int iters, double omega, double comp,
-                      double tol, bool inColl, int fo, double fv, double slide, DCount* dc, cudaStream_t s) {
-    if (nc <= 0) return;
-    k_pgs_exact<<<1, 32, 0, s>>>(B, C, nc, order, iters, omega, comp, tol, inColl ? 0 : 1, fo, fv, slide, dc);
-    AM_LAUNCHED(1);
 }
 
 // ---------------------------------------------------------------------------

@@ -371,6 +371,10 @@ int Ctx::ensureCand(int need) {
 // ---- scene upload ------------------------------------------------------------
 int Ctx::setScene(const am_scene& s) {
     release();
+    nScenes = 0;
+    topEnd = nullptr;
+    bRecCap = bPairCap = 0;
+    batchThreads = 0;
     if (s.n_bodies <= 0) { err = "empty scene"; return AM_E_ARG; }
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaMalloc((void**)&dc, sizeof(DCount)));
@@ -547,12 +551,12 @@ int Ctx::collisionDetection() {
     launch_bv_update(B, N, stream);
     int r = ensureCand(1);
     if (r) return r;
-    launch_broadphase(B, N, top, ntop, nullptr, nullptr, 0, rowCount, rowOff, SC, dc, stream);
+    launch_broadphase(B, N, top, ntop, nullptr, nullptr, 0, rowCount, rowOff, SC, dc, stream, topEnd);
     if ((r = readCounts())) return r;
     int ncand = hc->n_cand;
     if ((r = ensureCand(ncand))) return r;
     if (ntop >= 2 && ncand > 0) {
-        launch_broadphase(B, N, top, ntop, candA, candB, candCap, rowCount, rowOff, SC, dc, stream);
+        launch_broadphase(B, N, top, ntop, candA, candB, candCap, rowCount, rowOff, SC, dc, stream, topEnd);
     }
     if ((r = ensureScratch(ncand + 1))) return r;
     launch_expand_pairs(B, subOff, subIds, candA, candB, ncand, PR, SC, dc, stream);
@@ -615,8 +619,9 @@ int Ctx::runPGS(int nc, const int* order, int iters, bool inColl, double dt, boo
         cudaEventRecord(evA, stream);
     }
     if (P.solver_order == AM_ORDER_REFERENCE || inColl) {
-        launch_pgs_exact(B, c, nc, order, iters, P.omega, comp, P.tolerance, inColl, P.friction_override,
-                         P.friction, P.sliding_threshold, dc, stream);
+        (void)order;
+        int r = exactSweep(c, nc, iters, inColl);
+        if (r) return r;
     } else {
         colour_groups(B, c, PR, nPairs, colourOf, colourCnt, colourOff, colourFill, groupOrder, MAXC,
                       (unsigned long long*)bodyMax, host.cap, dc, SC, stream);
@@ -640,6 +645,44 @@ int Ctx::runPGS(int nc, const int* order, int iters, bool inColl, double dt, boo
                         P.friction_override, P.friction, P.sliding_threshold, Mj, invD, mjCap, dc, blocks, stream);
     }
     if (timed) { cudaEventRecord(evB, stream); pgsPending = true; }
+    return AM_OK;
+}
+
+// PGS in list order, bit-exact, level scheduled (gs_exact.cu): the levels come
+// from the contacts' solve bodies, computed here on the host
+int Ctx::exactSweep(DContacts& buf, int n, int iters, bool inColl) {
+    hS1.resize(n);
+    hS2.resize(n);
+    cudaMemcpyAsync(hS1.data(), buf.b1, sizeof(int) * n, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(hS2.data(), buf.b2, sizeof(int) * n, cudaMemcpyDeviceToHost, stream);
+    int r = syncErr();
+    if (r) return r;
+    if (!inColl)
+        for (int i = 0; i < n; i++) {
+            if (host.parent[hS1[i]] >= 0) hS1[i] = host.parent[hS1[i]];
+            if (host.parent[hS2[i]] >= 0) hS2[i] = host.parent[hS2[i]];
+        }
+    hLast.assign(host.cap, 0);
+    int nL = gs_levels(hS1, hS2, host.flags, hOrder, hLevOff, hLast);
+    if (n > levCap || nL + 1 > levCap) {
+        int cap = std::max(2 * std::max(n, nL + 1), 4096);
+        if (alloc(&levOrder, cap) || alloc(&levOff, cap)) return AM_E_CUDA;
+        levCap = cap;
+    }
+    int width = 0;
+    for (int L = 0; L < nL; L++) width = std::max(width, hLevOff[L + 1] - hLevOff[L]);
+    cudaMemcpyAsync(levOrder, hOrder.data(), sizeof(int) * n, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(levOff, hLevOff.data(), sizeof(int) * (nL + 1), cudaMemcpyHostToDevice, stream);
+    if (!gsBlocksMax) {
+        int per = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, gs_levels_kernel(), 128, 0);
+        gsBlocksMax = std::max(1, per) * g_numSMs;
+    }
+    // four warps (contacts) per block: one per SM sub-partition's FP64 pipe
+    int blocks = std::min(gsBlocksMax, std::max(1, (width + 3) / 4));
+    double comp = P.enable_compliance ? P.compliance : 0.;
+    launch_gs_levels(B, buf, levOrder, levOff, nL, iters, P.omega, comp, P.tolerance, !inColl, P.friction_override,
+                     P.friction, P.sliding_threshold, dc, blocks, stream);
     return AM_OK;
 }
 
@@ -701,6 +744,7 @@ int Ctx::finishStep(double dt) {
 int Ctx::step(double dt) {
     totalSteps++;
     int r;
+    if (nScenes > 0) return stepBatch(dt);
     if (host.anyMerging()) return stepWithMerging(dt);
     if ((r = beginStep(0))) return r;
     if ((r = collisionDetection())) return r;

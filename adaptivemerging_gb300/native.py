@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libam.so")
 EXPORTS = [
     "am_params_default", "am_create", "am_destroy", "am_last_error", "am_set_params", "am_set_scene",
     "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
-    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology",
+    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats",
 ]
 
 _lib = None
@@ -57,6 +57,9 @@ def lib():
         L.am_get_stats.argtypes = [vp, C.POINTER(abi.am_solve_stats)]
         L.am_get_perf.argtypes = [vp, C.POINTER(abi.am_perf)]
         L.am_put_bodies.argtypes = [vp, C.POINTER(abi.am_body_state)]
+        L.am_set_batch.argtypes = [vp, C.POINTER(abi.am_scene), C.c_int32]
+        L.am_set_batch_options.argtypes = [vp, C.c_int32, C.c_double, C.c_int32]
+        L.am_get_batch_stats.argtypes = [vp, C.POINTER(abi.am_batch_stats)]
         L.am_get_topology.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32,
                                       C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.am_reset_perf.argtypes = [vp]
@@ -66,6 +69,31 @@ def lib():
                 getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib
+
+
+class BatchSystem:
+    """Many independent scenes in one context (merging off); am_step advances all."""
+
+    def __init__(self, scene_list, params, threads=0, residual_target=1e-6, check_every=10):
+        self.params = params
+        self.scenes = scene_list
+        self.h = C.c_void_p()
+        self._check(lib().am_create(C.byref(params), C.byref(self.h)))
+        arr = (abi.am_scene * len(scene_list))()
+        for k, s in enumerate(scene_list):
+            arr[k] = s.struct()
+        self._arr = arr
+        self._check(lib().am_set_batch(self.h, arr, len(scene_list)))
+        self._check(lib().am_set_batch_options(self.h, threads, residual_target, check_every))
+        self.n = sum(s.n for s in scene_list)
+        self.offsets = np.cumsum([0] + [s.n for s in scene_list])
+
+    _check = None  # filled below
+
+    def batch_stats(self):
+        st = abi.am_batch_stats()
+        self._check(lib().am_get_batch_stats(self.h, C.byref(st)))
+        return st
 
 
 class System:
@@ -180,3 +208,9 @@ class System:
         self._check(lib().am_get_bodies(self.h, C.byref(s)))
         return {"x": st.x.reshape(-1, 3), "R": st.R.reshape(-1, 9), "v": st.v.reshape(-1, 3),
                 "omega": st.omega.reshape(-1, 3), "sleeping": st.sleeping, "parent": st.parent}
+
+
+for _name in ("_check", "close", "__del__", "step", "advance_time", "stats", "num_contacts", "contacts", "bodies",
+              "perf", "reset_perf", "stream_handle", "set_params", "topology", "put_bodies_struct",
+              "get_bodies_struct", "collision_detection", "warm_start", "solve_lcp", "integrate"):
+    setattr(BatchSystem, _name, getattr(System, _name))

@@ -183,3 +183,51 @@ def random_pile(n=30, seed=0, kinds=("box", "sphere"), extent=3.0, height=4.0):
                     B.clump(cs, rs, p, density=rng.uniform(500, 2000))
                 k += 1
     return B.build()
+
+
+def bin_scene(n_bodies, seed, extent=10.0, wall_height=12.0, box_frac=0.5, gap=0.01):
+    """One scene of the batched workload: `n_bodies` boxes (sides U(0.1, 1.0)
+    m) and spheres (r U(0.05, 0.5) m), density U(500, 2000) kg/m3, in a 10 x
+    10 m bin (four pinned box walls on a ground plane).  Bodies are dropped
+    from a jittered grid of columns: each body starts `gap` (1 cm) above the
+    one below it, axis aligned, so no two bodies overlap initially (a negative
+    gap starts them in slight contact).  All bodies of the
+    scene share a friction coefficient mu ~ U(0.3, 0.8) (the reference's
+    friction mixing rule then gives mu for every contact)."""
+    rng = np.random.default_rng(seed)
+    mu = float(rng.uniform(0.3, 0.8))
+    B = Builder()
+    B.plane((0, 0, 0), (0, 1, 0), friction=mu)
+    t = 0.5
+    h = extent / 2 + t / 2
+    for (x, z, sx, sz) in ((h, 0, t, extent + 2 * t), (-h, 0, t, extent + 2 * t),
+                           (0, h, extent, t), (0, -h, extent, t)):
+        B.box((sx, wall_height, sz), (x, wall_height / 2, z), pinned=True, density=1000.0, friction=mu)
+    pitch = 1.05
+    ncol = int(extent / pitch)
+    tops = np.zeros((ncol, ncol))
+    for k in range(n_bodies):
+        c = int(rng.integers(ncol * ncol))
+        i, j = divmod(c, ncol)
+        x = -extent / 2 + (i + 0.5) * pitch + rng.uniform(-0.02, 0.02)
+        z = -extent / 2 + (j + 0.5) * pitch + rng.uniform(-0.02, 0.02)
+        dens = float(rng.uniform(500, 2000))
+        if rng.uniform() < box_frac:
+            s = tuple(float(v) for v in rng.uniform(0.1, 1.0, 3))
+            y = tops[i, j] + gap + s[1] / 2
+            B.box(s, (x, y, z), density=dens, friction=mu)
+            tops[i, j] = y + s[1] / 2
+        else:
+            r = float(rng.uniform(0.05, 0.5))
+            y = tops[i, j] + gap + r
+            B.sphere(r, (x, y, z), density=dens, friction=mu)
+            tops[i, j] = y + r
+    return B.build()
+
+
+def batch_scenes(n_scenes=512, seed=3, n_min=20, n_max=2000):
+    """The batched workload: `n_scenes` independent bins whose body counts are
+    log-uniform in [n_min, n_max] (seeded)."""
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(math.log(n_min), math.log(n_max), n_scenes)).astype(int)
+    return [bin_scene(int(n), seed * 100003 + k) for k, n in enumerate(counts)]

@@ -2,17 +2,20 @@
 """Headline benchmark: simulated steps per second of the contact hot path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload wall|tower]
+                    [--workload batch|wall|wall_nomerge|tower]
 
-A step is one RigidBodySystem.advanceTime of the workload scene: collision
-detection, contact setup, warm start, the projected Gauss-Seidel solve,
-integration and sleeping.  `value` is steps/s with the state resident in HBM
-(device time of K steps measured with CUDA events on the library's stream,
-L2 flushed between steps); `e2e` runs the same steps through the C ABI with
-the body state pushed from and read back into pinned host buffers every step.
-`--impl reference` times the CPU restatement of the reference path (the
-oracle) on the same workload.  The workload is a single scene, so several GPUs
-run independent replicas ("replicas only"): value = all ranks' steps / max time.
+A step is one RigidBodySystem.advanceTime of every scene of the workload:
+collision detection, contact setup, warm start, the projected Gauss-Seidel
+solve, integration and sleeping.  The default workload is the batched one
+(512 independent bins, FP32 solve, each scene iterated until its relative LCP
+residual <= 1e-6 or the iteration cap); `value` is simulated scene-steps per
+second with the state resident in HBM (device time of K steps measured with
+CUDA events on the library's stream); `e2e` runs the same steps through the C
+ABI with the body state pushed from and read back into pinned host buffers
+every step.  `--impl reference` times the CPU restatement of the reference
+path (the oracle) on the same workload.  Scenes are independent, so several
+GPUs each run their own batch ("weak" scaling, no collective): value = all
+ranks' scene-steps / max time.
 """
 import argparse
 import ctypes as C
@@ -33,19 +36,34 @@ from adaptivemerging_gb300 import abi, scenes  # noqa: E402
 
 METRIC = "sim steps/s at LCP residual<=1e-6: warm-start+batched vs plain GPU PGS, 1 GB300"
 FP64_BYTES_PER_CONTACT_SWEEP = 736   # J 288 + b,D 48 + lambda r/w 48 + dv of 2 bodies r/w 192 + minv,jinv 160
+FP32_BYTES_PER_CONTACT_SWEEP = 368   # the same quantities in FP32
+BATCH_SCENES = 512
+BATCH_SAMPLE_STRIDE = 16             # CPU baseline: every 16th scene, scaled by 16
 
 
 def workload(name):
-    """Scene, parameters, dt and a description of the named workload."""
-    if name == "wall":
+    """Scene (or list of scenes), parameters, dt and a description of the named workload."""
+    if name == "batch":
+        sc = scenes.batch_scenes(BATCH_SCENES, seed=3)
+        P = abi.default_params(gravity_amount=9.81, friction_override=0, restitution_override=1,
+                               restitution=0.0, iterations=500, enable_merging=0)
+        return sc, P, 0.005, {
+            "workload": "512 independent bins, body counts log-uniform 20..2000, boxes U(0.1,1.0) m and "
+                        "spheres U(0.05,0.5) m, density U(500,2000), per-scene mu U(0.3,0.8), 4 pinned walls + plane",
+            "scenes": BATCH_SCENES, "bodies": int(sum(x.n for x in sc)), "dt": 0.005,
+            "pgs": "FP32, one CTA per scene, stop at relative residual <= 1e-6 (checked every 10 sweeps), cap 500",
+            "merging": "off", "precision": "fp32 solve, fp64 collision/contact setup/integration"}
+    if name in ("wall", "wall_nomerge"):
+        merging = name == "wall"
         sc = scenes.wall(cols=40, rows=25, seed=2)
         P = abi.default_params(gravity_amount=9.81, friction_override=1, friction=0.5, restitution_override=1,
-                               restitution=0.0, iterations=200, enable_merging=0,
+                               restitution=0.0, iterations=200, enable_merging=int(merging),
                                solver_order=abi.AM_ORDER_COLOURED)
         return sc, P, 0.005, {
             "workload": "brick wall 40x25 (0.4x0.2x0.2 m, 1000 kg/m3) + 50 kg sphere at 15 m/s",
             "bodies": int(sc.n), "dt": 0.005, "pgs_iterations": 200, "mu": 0.5,
-            "merging": "off", "pgs_order": "coloured", "precision": "fp64"}
+            "merging": "on" if merging else "off", "pgs_order": "coloured full solve, exact single sweep",
+            "precision": "fp64"}
     if name == "tower":
         sc = scenes.tower(25, seed=1)
         P = abi.default_params(gravity_amount=9.81, friction_override=1, friction=0.6, restitution_override=1,
@@ -144,12 +162,36 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(name, max_seconds=15.0, max_steps=400):
+def oracle_batch_sample(sc_list, P, dt, warmup, steps):
+    """Oracle on every BATCH_SAMPLE_STRIDE-th scene from the initial state:
+    `warmup` untimed steps, then `steps` timed steps.  Returns scene-steps/s
+    of the full batch estimated from the sample (the scenes are i.i.d.)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_binding import Oracle
+    P.solver_order = abi.AM_ORDER_REFERENCE
+    P.iterations = 100            # the reference algorithm: 100 PGS iterations, early exit on tolerance
+    sample = sc_list[::BATCH_SAMPLE_STRIDE]
+    t = 0.0
+    for s in sample:
+        o = Oracle(s, P)
+        o.step(dt, warmup)
+        t0 = time.perf_counter()
+        o.step(dt, steps)
+        t += time.perf_counter() - t0
+    return steps * len(sample) / t, (f"{len(sample)} of {len(sc_list)} scenes (every {BATCH_SAMPLE_STRIDE}th), "
+                                     f"{steps} timed steps after {warmup} from the initial state, "
+                                     f"{t:.1f} s single thread; reference algorithm (100 iterations, early exit)")
+
+
+def cpu_baseline(name, max_seconds=15.0, max_steps=400, warmup=20, steps=10):
     """Oracle (single-threaded CPU restatement of the reference path) on the
-    same workload: steps/s over a bounded sample from the initial scene."""
+    same workload: steps/s over a bounded sample."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_binding import Oracle
     sc, P, dt, _ = workload(name)
+    if name == "batch":
+        v, desc = oracle_batch_sample(sc, P, dt, warmup, steps)
+        return {"value": v, "unit": "scene-steps/s", "cores": 1, "kind": "port", "sample": desc}
     P.solver_order = abi.AM_ORDER_REFERENCE
     o = Oracle(sc, P)
     o.step(dt, 2)
@@ -172,19 +214,25 @@ def run_reference(args):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_binding import Oracle
     P.solver_order = abi.AM_ORDER_REFERENCE
-    o = Oracle(sc, P)
-    o.step(dt, args.warmup)
-    t0 = time.perf_counter()
-    o.step(dt, args.steps)
-    el = time.perf_counter() - t0
-    v = args.steps / el
-    out = {"metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+    unit = "steps/s"
+    if args.workload == "batch":
+        v, desc = oracle_batch_sample(sc, P, dt, args.warmup, args.steps)
+        el = args.steps * BATCH_SCENES / v
+        unit = "scene-steps/s"
+    else:
+        o = Oracle(sc, P)
+        o.step(dt, args.warmup)
+        t0 = time.perf_counter()
+        o.step(dt, args.steps)
+        el = time.perf_counter() - t0
+        v = args.steps / el
+        desc = f"{args.steps} steps after {args.warmup} warm-up steps, single thread"
+    out = {"metric": METRIC, "value": v, "unit": unit, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
            "config": cfg,
-           "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
-                            "sample": f"{args.steps} steps after {args.warmup} warm-up steps, single thread"},
-           "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "cpu_baseline": {"value": v, "unit": unit, "cores": 1, "kind": "port", "sample": desc},
+           "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
 
@@ -195,7 +243,13 @@ def run_ours(args):
     torch.cuda.set_device(local)
     build.build()
     sc, P, dt, cfg = workload(args.workload)
-    sysm = native.System(sc, P)
+    batch = args.workload == "batch"
+    if batch:
+        sysm = native.BatchSystem(sc, P, threads=0, residual_target=1e-6, check_every=10)
+        n_units = len(sc)
+    else:
+        sysm = native.System(sc, P)
+        n_units = 1
     stream = torch.cuda.ExternalStream(sysm.stream_handle())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
@@ -208,6 +262,7 @@ def run_ours(args):
     clocks.start()
     total_ms = 0.0
     sweeps, contacts, res = [], [], []
+    conv = []
     for _ in range(args.steps):
         flush.fill_(1.0)                     # L2 flush between timed steps
         torch.cuda.synchronize()
@@ -219,16 +274,22 @@ def run_ours(args):
         e1.synchronize()
         total_ms += e0.elapsed_time(e1)
         st = sysm.stats()
-        sweeps.append(st.sweeps); contacts.append(st.n_contacts); res.append(st.residual_rel)
+        contacts.append(st.n_contacts)
+        if batch:
+            bs = sysm.batch_stats()
+            sweeps.append(bs.sweeps_sum / max(1, bs.n_scenes)); res.append(bs.residual_max)
+            conv.append(bs.converged / max(1, bs.n_scenes))
+        else:
+            sweeps.append(st.sweeps); res.append(st.residual_rel)
     torch.cuda.synchronize()
     clk = clocks.stop()
     barrier(ws)
     p1 = sysm.perf()
     t_max = max_over_ranks(ws, total_ms / 1e3, "cuda")
-    value = ws * args.steps / t_max
+    value = ws * args.steps * n_units / t_max
 
     # end to end through the C ABI: host-owned state pushed and read back every step
-    n = sc.n
+    n = sysm.n
     pin = {k: torch.zeros(m * n, dtype=torch.float64, pin_memory=True) for k, m in
            (("x", 3), ("R", 9), ("v", 3), ("omega", 3))}
     pin_i = {k: torch.zeros(n, dtype=torch.int32, pin_memory=True) for k in ("sleeping", "parent")}
@@ -247,13 +308,14 @@ def run_ours(args):
         sysm.step(dt)
         sysm.get_bodies_struct(st_s)
     e2e_t = max_over_ranks(ws, time.perf_counter() - t0, "cuda")
-    e2e = ws * args.steps / e2e_t
+    e2e = ws * args.steps * n_units / e2e_t
 
     pgs_l = p1.pgs_launches - p0.pgs_launches
     pgs_ms = p1.pgs_ms - p0.pgs_ms
     cs = p1.contact_sweeps - p0.contact_sweeps
     peak, peak_kind = measured_peak()
-    achieved = (cs * FP64_BYTES_PER_CONTACT_SWEEP / pgs_l) / (pgs_ms / pgs_l / 1e3) / 1e9 if pgs_l and pgs_ms else 0.0
+    bpcs = FP32_BYTES_PER_CONTACT_SWEEP if batch else FP64_BYTES_PER_CONTACT_SWEEP
+    achieved = (cs * bpcs / pgs_l) / (pgs_ms / pgs_l / 1e3) / 1e9 if pgs_l and pgs_ms else 0.0
     traffic = None
     tf = os.path.join(ROOT, "profiles", "pgs_traffic.json")
     if os.path.exists(tf):
@@ -263,31 +325,39 @@ def run_ours(args):
         return
     cfg.update({"contacts_mean": float(np.mean(contacts)), "pgs_sweeps_mean": float(np.mean(sweeps)),
                 "residual_rel_mean": float(np.mean(res)), "residual_rel_max": float(np.max(res)),
-                "frac_steps_residual_le_1e-6": float(np.mean(np.array(res) <= 1e-6)),
-                "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas only"})
-    out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+                "l2": "flushed between timed steps (256 MB write)",
+                "parallelism": "independent scenes per GPU" if batch else "replicas only",
+                "timed_window": f"steps {args.warmup + 1}..{args.warmup + args.steps} from the initial state"})
+    if batch:
+        cfg["frac_scene_steps_residual_le_1e-6"] = float(np.mean(conv))
+        cfg["cta_threads"] = int(sysm.batch_stats().threads)
+    else:
+        cfg["frac_steps_residual_le_1e-6"] = float(np.mean(np.array(res) <= 1e-6))
+    unit = "scene-steps/s" if batch else "steps/s"
+    out = {"metric": METRIC, "value": value, "unit": unit, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
-           "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32" if batch else "f64", "data": "synthetic",
+           "config": cfg,
+           "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
            "gpu_launches": int(p1.launches - p0.launches),
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak if peak else None, "traffic": traffic,
-                        "kernel": "k_pgs_coloured", "peak_source": peak_kind,
-                        "bytes_per_contact_sweep": FP64_BYTES_PER_CONTACT_SWEEP,
+                        "kernel": "k_batch_sweep" if batch else "k_pgs_fast", "peak_source": peak_kind,
+                        "bytes_per_contact_sweep": bpcs,
                         "pgs_ms_per_launch": pgs_ms / pgs_l if pgs_l else None},
            "clocks": clk}
     if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args.workload)
+        out["cpu_baseline"] = cpu_baseline(args.workload, warmup=args.warmup, steps=min(args.steps, 10))
     print(json.dumps(out))
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="wall")
+    ap.add_argument("--workload", default="batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

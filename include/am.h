@@ -219,6 +219,30 @@ int32_t am_num_contacts(void* ctx, int32_t* n);
 int32_t am_get_contacts(void* ctx, am_contacts* out, int32_t capacity, int32_t* n);
 int32_t am_get_stats(void* ctx, am_solve_stats* out);
 
+/*
+ * Batched scenes (no reference counterpart: the reference simulates one
+ * scene).  n independent scenes are loaded into one context; am_step then
+ * advances all of them (collision per scene, one CTA per scene in the solve).
+ * Body ids in readbacks are global: scene s's body i is at
+ * (number of bodies of scenes < s) + i.  Merging must be off.  The batched
+ * solve runs in FP32 with delta-v in shared memory and stops each scene when
+ * its relative natural-map residual is <= residual_target (checked every
+ * check_every sweeps) or after am_params.iterations sweeps.
+ */
+typedef struct am_batch_stats {
+    int32_t n_scenes;
+    int32_t converged;       /* scenes that reached the residual target        */
+    int32_t sweeps_max;      /* largest sweep count of the last step           */
+    int32_t threads;         /* threads per scene CTA (autotuned when 0 given) */
+    int64_t sweeps_sum;      /* sum of the scenes' sweep counts, last step     */
+    int64_t contact_sweeps;  /* sum of contacts x sweeps, last step            */
+    double  residual_max;    /* worst scene residual, last step                */
+} am_batch_stats;
+int32_t am_set_batch(void* ctx, const am_scene* scenes, int32_t n_scenes);
+/* threads: 0 = autotune on the first step; residual_target <= 0 disables the test */
+int32_t am_set_batch_options(void* ctx, int32_t threads, double residual_target, int32_t check_every);
+int32_t am_get_batch_stats(void* ctx, am_batch_stats* out);
+
 /* Top-level body list (RigidBodySystem.bodies, RigidBodySystem.java:31) with
  * collection membership (RigidCollection.bodies, RigidCollection.java:28):
  * entry t spans items[item_off[t] .. item_off[t+1]); a free body is [id], a

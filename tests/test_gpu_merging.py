@@ -50,3 +50,18 @@ def test_merging_bit_exact(gpu_lib, name):
         assert (pg.merge_events, pg.unmerge_events) == (c["merges"], c["unmerges"]), f"step {s}"
         merged = max(merged, sum(1 for t in to if isinstance(t, tuple)))
     assert merged > 0, "scenario never formed a collection"
+
+
+def test_device_matches_committed_golden(gpu_lib):
+    """The device path reproduces the committed oracle fixture of the tower
+    workload (merging on) step for step."""
+    import json
+    import os
+    from adaptivemerging_gb300 import abi, native
+    from test_oracle_cpu import _digest
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "tower_c1.json")) as f:
+        gold = json.load(f)
+    g = native.System(scenes.tower(**gold["scene"]), abi.default_params(**gold["params"]))
+    for s, want in enumerate(gold["steps"]):
+        g.step(gold["dt"])
+        assert _digest(g) == want, f"step {s}"
