@@ -149,7 +149,7 @@ __device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret
 __global__ void k_batch_sweep(DBodies B, DContacts C, DPairs P, const int* pairOff, const int* sceneBodyOff,
                               const int* gOrder, const int* colOff, const float* rec, const int2* lid, float* lamf,
                               int iters, float omega, float comp, float tolRel, int check, float slide,
-                              int* sceneSweeps, float* sceneRes, DCount* dc) {
+                              int* sceneSweeps, float* sceneRes, DCount* dc, const float* lamAlt, int* sceneFall) {
     extern __shared__ float sm[];
     int s = blockIdx.x;
     int b0 = sceneBodyOff[s], nb = sceneBodyOff[s + 1] - b0;
@@ -158,42 +158,29 @@ __global__ void k_batch_sweep(DBodies B, DContacts C, DPairs P, const int* pairO
     __shared__ float s_res, s_lam;
     __shared__ int s_stop;
     int t = threadIdx.x, T = blockDim.x;
-    for (int b = t; b < nb; b += T) {
-        for (int k = 0; k < 6; k++) dv[6 * b + k] = 0.f;
-        mv[b] = (float)B.minv[b0 + b];
-    }
+    for (int b = t; b < nb; b += T) mv[b] = (float)B.minv[b0 + b];
     const int* co = colOff + s * (MAXCB + 1);
     int ncol = 0;
     while (ncol < MAXCB && co[ncol + 1] > co[ncol]) ncol++;
-    __syncthreads();
-    // confidentWarmStart
-    for (int col = 0; col < ncol; col++) {
-        for (int k = co[col] + t; k < co[col + 1]; k += T) {
-            int g = gOrder[k];
-            for (int c = P.off[g]; c < P.off[g] + P.count[g]; c++) {
-                int2 id = lid[c];
-                const float* R = rec + (size_t)REC * c;
-                float* da = dv + 6 * id.x;
-                float* db = dv + 6 * id.y;
-                float ma = mv[id.x], mb = mv[id.y];
-                for (int q = 0; q < 3; q++) {
-                    float l = lamf[3 * c + q];
-                    float4 j0 = ld4(R + 20 * q), j1 = ld4(R + 20 * q + 4), j2 = ld4(R + 20 * q + 8);
-                    float4 i0 = ld4(R + 20 * q + 12), i1 = ld4(R + 20 * q + 16);
-                    float la = ma * l, lb = mb * l;
-                    da[0] += la * j0.x; da[1] += la * j0.y; da[2] += la * j0.z;
-                    da[3] += l * i0.x; da[4] += l * i0.y; da[5] += l * i0.z;
-                    db[0] += lb * j1.z; db[1] += lb * j1.w; db[2] += lb * j2.x;
-                    db[3] += l * i0.w; db[4] += l * i1.x; db[5] += l * i1.y;
-                }
-            }
-        }
-        __syncthreads();
-    }
-    int done = 0;
+    int total = 0;
     float res = 0.f;
-    for (int it = 0; it < iters; it++) {
-        bool last = (it == iters - 1);
+    // attempt 0 starts from lamf; with lamAlt given, a scene that misses the
+    // residual target starts again from lamAlt (the learned start's fallback)
+    const int attempts = (lamAlt && check > 0 && tolRel > 0.f) ? 2 : 1;
+    for (int attempt = 0; attempt < attempts; attempt++) {
+        if (attempt == 1) {
+            if (res <= tolRel) break;   // uniform: res comes from shared memory
+            for (int g = pairOff[s] + t; g < pairOff[s + 1]; g += T)
+                for (int c = P.off[g]; c < P.off[g] + P.count[g]; c++)
+                    for (int q = 0; q < 3; q++) lamf[3 * c + q] = lamAlt[3 * c + q];
+            if (t == 0 && sceneFall) sceneFall[s] = 1;
+        } else if (t == 0 && sceneFall) {
+            sceneFall[s] = 0;
+        }
+        for (int b = t; b < nb; b += T)
+            for (int k = 0; k < 6; k++) dv[6 * b + k] = 0.f;
+        __syncthreads();
+        // confidentWarmStart
         for (int col = 0; col < ncol; col++) {
             for (int k = co[col] + t; k < co[col + 1]; k += T) {
                 int g = gOrder[k];
@@ -203,72 +190,100 @@ __global__ void k_batch_sweep(DBodies B, DContacts C, DPairs P, const int* pairO
                     float* da = dv + 6 * id.x;
                     float* db = dv + 6 * id.y;
                     float ma = mv[id.x], mb = mv[id.y];
-                    float4 tail = ld4(R + 60);
-                    float l0 = lamf[3 * c];
-                    float lam[3];
                     for (int q = 0; q < 3; q++) {
+                        float l = lamf[3 * c + q];
                         float4 j0 = ld4(R + 20 * q), j1 = ld4(R + 20 * q + 4), j2 = ld4(R + 20 * q + 8);
                         float4 i0 = ld4(R + 20 * q + 12), i1 = ld4(R + 20 * q + 16);
-                        float jd = j0.x * da[0] + j0.y * da[1] + j0.z * da[2] + j0.w * da[3] + j1.x * da[4] +
-                                   j1.y * da[5] + j1.z * db[0] + j1.w * db[1] + j2.x * db[2] + j2.y * db[3] +
-                                   j2.z * db[4] + j2.w * db[5];
-                        float D = q == 0 ? tail.x : (q == 1 ? tail.y : tail.z);
-                        float l = lamf[3 * c + q];
-                        float nl = (D * l - omega * (i1.z + jd)) * i1.w;
-                        if (q == 0) nl = fmaxf(nl, 0.f);
-                        else { float lim = tail.w * l0; nl = fminf(fmaxf(nl, -lim), lim); }
-                        float d = nl - l;
-                        if (q == 0) l0 = nl;
-                        lam[q] = nl;
-                        float la = ma * d, lb = mb * d;
+                        float la = ma * l, lb = mb * l;
                         da[0] += la * j0.x; da[1] += la * j0.y; da[2] += la * j0.z;
-                        da[3] += d * i0.x; da[4] += d * i0.y; da[5] += d * i0.z;
+                        da[3] += l * i0.x; da[4] += l * i0.y; da[5] += l * i0.z;
                         db[0] += lb * j1.z; db[1] += lb * j1.w; db[2] += lb * j2.x;
-                        db[3] += d * i0.w; db[4] += d * i1.x; db[5] += d * i1.y;
+                        db[3] += l * i0.w; db[4] += l * i1.x; db[5] += l * i1.y;
                     }
-                    lamf[3 * c] = lam[0]; lamf[3 * c + 1] = lam[1]; lamf[3 * c + 2] = lam[2];
-                    (void)last;
                 }
             }
             __syncthreads();
         }
-        done = it + 1;
-        if (check > 0 && (done % check == 0 || done == iters)) {
-            // natural-map residual of the scene at the current state
-            if (t == 0) { s_res = 0.f; s_lam = 0.f; }
-            __syncthreads();
-            float rmax = 0.f, lmax = 0.f;
-            for (int g = pairOff[s] + t; g < pairOff[s + 1]; g += T)
-                for (int c = P.off[g]; c < P.off[g] + P.count[g]; c++) {
-                    int2 id = lid[c];
-                    const float* R = rec + (size_t)REC * c;
-                    const float* da = dv + 6 * id.x;
-                    const float* db = dv + 6 * id.y;
-                    float4 tail = ld4(R + 60);
-                    float l0 = lamf[3 * c];
-                    for (int q = 0; q < 3; q++) {
-                        float4 j0 = ld4(R + 20 * q), j1 = ld4(R + 20 * q + 4), j2 = ld4(R + 20 * q + 8);
-                        float4 i1 = ld4(R + 20 * q + 16);
-                        float jd = j0.x * da[0] + j0.y * da[1] + j0.z * da[2] + j0.w * da[3] + j1.x * da[4] +
-                                   j1.y * da[5] + j1.z * db[0] + j1.w * db[1] + j2.x * db[2] + j2.y * db[3] +
-                                   j2.z * db[4] + j2.w * db[5];
-                        float l = lamf[3 * c + q];
-                        float w = i1.z + jd + comp * l;
-                        float z = l - w * i1.w;
-                        if (q == 0) z = fmaxf(z, 0.f);
-                        else { float lim = tail.w * l0; z = fminf(fmaxf(z, -lim), lim); }
-                        rmax = fmaxf(rmax, fabsf(l - z));
-                        lmax = fmaxf(lmax, fabsf(l));
+        int done = 0;
+        for (int it = 0; it < iters; it++) {
+            bool last = (it == iters - 1);
+            for (int col = 0; col < ncol; col++) {
+                for (int k = co[col] + t; k < co[col + 1]; k += T) {
+                    int g = gOrder[k];
+                    for (int c = P.off[g]; c < P.off[g] + P.count[g]; c++) {
+                        int2 id = lid[c];
+                        const float* R = rec + (size_t)REC * c;
+                        float* da = dv + 6 * id.x;
+                        float* db = dv + 6 * id.y;
+                        float ma = mv[id.x], mb = mv[id.y];
+                        float4 tail = ld4(R + 60);
+                        float l0 = lamf[3 * c];
+                        float lam[3];
+                        for (int q = 0; q < 3; q++) {
+                            float4 j0 = ld4(R + 20 * q), j1 = ld4(R + 20 * q + 4), j2 = ld4(R + 20 * q + 8);
+                            float4 i0 = ld4(R + 20 * q + 12), i1 = ld4(R + 20 * q + 16);
+                            float jd = j0.x * da[0] + j0.y * da[1] + j0.z * da[2] + j0.w * da[3] + j1.x * da[4] +
+                                       j1.y * da[5] + j1.z * db[0] + j1.w * db[1] + j2.x * db[2] + j2.y * db[3] +
+                                       j2.z * db[4] + j2.w * db[5];
+                            float D = q == 0 ? tail.x : (q == 1 ? tail.y : tail.z);
+                            float l = lamf[3 * c + q];
+                            float nl = (D * l - omega * (i1.z + jd)) * i1.w;
+                            if (q == 0) nl = fmaxf(nl, 0.f);
+                            else { float lim = tail.w * l0; nl = fminf(fmaxf(nl, -lim), lim); }
+                            float d = nl - l;
+                            if (q == 0) l0 = nl;
+                            lam[q] = nl;
+                            float la = ma * d, lb = mb * d;
+                            da[0] += la * j0.x; da[1] += la * j0.y; da[2] += la * j0.z;
+                            da[3] += d * i0.x; da[4] += d * i0.y; da[5] += d * i0.z;
+                            db[0] += lb * j1.z; db[1] += lb * j1.w; db[2] += lb * j2.x;
+                            db[3] += d * i0.w; db[4] += d * i1.x; db[5] += d * i1.y;
+                        }
+                        lamf[3 * c] = lam[0]; lamf[3 * c + 1] = lam[1]; lamf[3 * c + 2] = lam[2];
+                        (void)last;
                     }
                 }
-            atomicMax(reinterpret_cast<int*>(&s_res), __float_as_int(rmax));
-            atomicMax(reinterpret_cast<int*>(&s_lam), __float_as_int(lmax));
-            __syncthreads();
-            res = s_res / fmaxf(1.f, s_lam);
-            if (t == 0) s_stop = (res <= tolRel) ? 1 : 0;
-            __syncthreads();
-            if (s_stop) break;
+                __syncthreads();
+            }
+            done = it + 1;
+            if (check > 0 && (done % check == 0 || done == iters)) {
+                // natural-map residual of the scene at the current state
+                if (t == 0) { s_res = 0.f; s_lam = 0.f; }
+                __syncthreads();
+                float rmax = 0.f, lmax = 0.f;
+                for (int g = pairOff[s] + t; g < pairOff[s + 1]; g += T)
+                    for (int c = P.off[g]; c < P.off[g] + P.count[g]; c++) {
+                        int2 id = lid[c];
+                        const float* R = rec + (size_t)REC * c;
+                        const float* da = dv + 6 * id.x;
+                        const float* db = dv + 6 * id.y;
+                        float4 tail = ld4(R + 60);
+                        float l0 = lamf[3 * c];
+                        for (int q = 0; q < 3; q++) {
+                            float4 j0 = ld4(R + 20 * q), j1 = ld4(R + 20 * q + 4), j2 = ld4(R + 20 * q + 8);
+                            float4 i1 = ld4(R + 20 * q + 16);
+                            float jd = j0.x * da[0] + j0.y * da[1] + j0.z * da[2] + j0.w * da[3] + j1.x * da[4] +
+                                       j1.y * da[5] + j1.z * db[0] + j1.w * db[1] + j2.x * db[2] + j2.y * db[3] +
+                                       j2.z * db[4] + j2.w * db[5];
+                            float l = lamf[3 * c + q];
+                            float w = i1.z + jd + comp * l;
+                            float z = l - w * i1.w;
+                            if (q == 0) z = fmaxf(z, 0.f);
+                            else { float lim = tail.w * l0; z = fminf(fmaxf(z, -lim), lim); }
+                            rmax = fmaxf(rmax, fabsf(l - z));
+                            lmax = fmaxf(lmax, fabsf(l));
+                        }
+                    }
+                atomicMax(reinterpret_cast<int*>(&s_res), __float_as_int(rmax));
+                atomicMax(reinterpret_cast<int*>(&s_lam), __float_as_int(lmax));
+                __syncthreads();
+                res = s_res / fmaxf(1.f, s_lam);
+                if (t == 0) s_stop = (res <= tolRel) ? 1 : 0;
+                __syncthreads();
+                if (s_stop) break;
+            }
         }
+        total += done;
     }
     // contact state after the final sweep (Contact.updateContactState)
     for (int g = pairOff[s] + t; g < pairOff[s + 1]; g += T)
@@ -296,12 +311,13 @@ __global__ void k_batch_sweep(DBodies B, DContacts C, DPairs P, const int* pairO
         }
     for (int b = t; b < nb; b += T)
         for (int k = 0; k < 6; k++) B.dv[6 * (b0 + b) + k] = (double)dv[6 * b + k];
-    if (t == 0) { sceneSweeps[s] = done; sceneRes[s] = res; }
+    if (t == 0) { sceneSweeps[s] = total; sceneRes[s] = res; }
 }
 
 const void* batch_sweep_kernel() { return (const void*)k_batch_sweep; }
 
 int Ctx::batchSolve(double dt) {
+    int r;
     int nc = nContacts, np = nPairs, S = nScenes;
     if (nc <= 0) return AM_OK;
     double comp = P.enable_compliance ? P.compliance : 0.;
@@ -309,7 +325,9 @@ int Ctx::batchSolve(double dt) {
                       P.warm_start ? 1 : 0, stream);
     if (nc > bRecCap) {
         int cap = std::max(nc + nc / 2, 4096);
-        if (alloc(&bRec, (size_t)REC * cap) || alloc(&bLid, cap) || alloc(&bLam, 3 * (size_t)cap)) return AM_E_CUDA;
+        if (alloc(&bRec, (size_t)REC * cap) || alloc(&bLid, cap) || alloc(&bLam, 3 * (size_t)cap) ||
+            alloc(&bLamL, 3 * (size_t)cap))
+            return AM_E_CUDA;
         bRecCap = cap;
     }
     if (np > bPairCap) {
@@ -326,12 +344,25 @@ int Ctx::batchSolve(double dt) {
     size_t ssm = sizeof(float) * 7 * (size_t)maxSceneBodies;
     int threads = batchThreads > 0 ? batchThreads : 128;
     if (evA) cudaEventRecord(evA, stream);
+    if (lUse || lCollect) {
+        if ((r = learnedFeatures(dt))) return r;
+    }
+    float* lamStart = bLam;
+    const float* lamAlt = nullptr;
+    if (lUse) {
+        // learned start in bLamL; the plain previous-frame start stays in bLam
+        // as the in-kernel fallback
+        if ((r = learnedPredict(lUse == 1))) return r;
+        lamStart = bLamL;
+        lamAlt = bLam;
+    }
     k_batch_sweep<<<S, threads, ssm, stream>>>(B, C[cur], PR, bPairOff, sceneBodyOffDev, bOrder, bColOff, bRec,
-                                               bLid, bLam, P.iterations, (float)P.omega, (float)comp,
+                                               bLid, lamStart, P.iterations, (float)P.omega, (float)comp,
                                                (float)batchTol, batchCheck, (float)P.sliding_threshold,
-                                               bSweeps, bRes, dc);
-    if (evB) { cudaEventRecord(evB, stream); pgsPending = true; }
+                                               bSweeps, bRes, dc, lamAlt, bFall);
     AM_LAUNCHED(4);
+    if (evB) { cudaEventRecord(evB, stream); pgsPending = true; }
+    if (lCollect && (r = learnedRecord())) return r;
     return AM_OK;
 }
 
@@ -346,7 +377,7 @@ __global__ void k_scene_cs(DPairs P, int npairs, int nc, const int* pairOff, con
 }
 
 int Ctx::batchStats() {
-    std::vector<int> sw(nScenes);
+    std::vector<int> sw(nScenes), fl(nScenes);
     std::vector<float> rs(nScenes);
     std::vector<long long> cs(nScenes);
     if (!bCS && alloc(&bCS, nScenes)) return AM_E_CUDA;
@@ -355,18 +386,21 @@ int Ctx::batchStats() {
     cudaMemcpyAsync(cs.data(), bCS, sizeof(long long) * nScenes, cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(sw.data(), bSweeps, sizeof(int) * nScenes, cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(rs.data(), bRes, sizeof(float) * nScenes, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(fl.data(), bFall, sizeof(int) * nScenes, cudaMemcpyDeviceToHost, stream);
     int r = syncErr();
     if (r) return r;
     long long tot = 0;
     int mx = 0;
     float rmax = 0.f;
-    int conv = 0;
+    int conv = 0, fall = 0;
     for (int s = 0; s < nScenes; s++) {
         tot += sw[s];
         mx = std::max(mx, sw[s]);
         rmax = std::max(rmax, rs[s]);
         conv += rs[s] <= batchTol ? 1 : 0;
+        fall += fl[s];
     }
+    lFallbackScenes = lUse ? fall : 0;
     batchSweepsTotal = tot;
     batchContactSweepsLast = 0;
     for (long long v : cs) batchContactSweepsLast += v;
@@ -423,8 +457,10 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     for (int i = 0; i < all.n_bodies; i++) { sOf[i] = sceneOf[i]; tEnd[i] = bodyOff[sceneOf[i] + 1]; }
     bCS = nullptr;
     if (alloc(&sceneOfDev, cap) || alloc(&sceneBodyOffDev, n + 1) || alloc(&topEnd, all.n_bodies) ||
-        alloc(&bPairOff, n + 1) || alloc(&bColOff, (size_t)n * (MAXCB + 1)) || alloc(&bSweeps, n) || alloc(&bRes, n))
+        alloc(&bPairOff, n + 1) || alloc(&bColOff, (size_t)n * (MAXCB + 1)) || alloc(&bSweeps, n) || alloc(&bRes, n) ||
+        alloc(&bFall, n))
         return AM_E_CUDA;
+    cudaMemsetAsync(bFall, 0, sizeof(int) * n, stream);
     cudaMemcpyAsync(sceneOfDev, sOf.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(sceneBodyOffDev, bodyOff.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(topEnd, tEnd.data(), sizeof(int) * all.n_bodies, cudaMemcpyHostToDevice, stream);
@@ -457,7 +493,7 @@ int Ctx::batchAutotune(double dt) {
         cudaEventRecord(e0, stream);
         k_batch_sweep<<<nScenes, T, ssm, stream>>>(B, C[cur], PR, bPairOff, sceneBodyOffDev, bOrder, bColOff, bRec,
                                                    bLid, bLam, 8, (float)P.omega, (float)comp, 0.f, 0,
-                                                   (float)P.sliding_threshold, bSweeps, bRes, dc);
+                                                   (float)P.sliding_threshold, bSweeps, bRes, dc, nullptr, nullptr);
         cudaEventRecord(e1, stream);
         AM_LAUNCHED(1);
         cudaEventSynchronize(e1);

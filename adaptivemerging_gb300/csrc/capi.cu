@@ -197,6 +197,75 @@ int32_t am_get_batch_stats(void* ctx, am_batch_stats* o) {
     return AM_OK;
 }
 
+int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, int32_t* fell_back) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->nScenes || !c->bSweeps) return AM_E_STATE;
+    int n = c->nScenes;
+    if (sweeps) cudaMemcpyAsync(sweeps, c->bSweeps, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream);
+    if (residual) cudaMemcpyAsync(residual, c->bRes, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
+    if (fell_back) cudaMemcpyAsync(fell_back, c->bFall, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream);
+    return c->syncErr();
+}
+
+int32_t am_learned_collect(void* ctx, int32_t enable, int32_t capacity) {
+    if (!ctx || capacity < 0) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    return c->learnedCollect(enable, capacity);
+}
+
+int32_t am_learned_train(void* ctx, int32_t epochs, int32_t batch, double lr, int32_t normalise, double* last_loss) {
+    if (!ctx || epochs < 0 || batch <= 0) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    float l = 0;
+    int r = c->learnedTrain(epochs, batch, (float)lr, &l, normalise);
+    if (last_loss) *last_loss = l;
+    return r;
+}
+
+int32_t am_learned_use(void* ctx, int32_t mode) {
+    if (!ctx || mode < 0 || mode > 2) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    int r = c->learnedInit();
+    if (r) return r;
+    if (mode && (r = c->learnedPackInference())) return r;
+    c->lUse = mode;
+    return AM_OK;
+}
+
+int32_t am_learned_weights(void* ctx, float* get, const float* set, float* norm_get, const float* norm_set) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    return c->learnedWeights(get, set, norm_get, norm_set);
+}
+
+int32_t am_learned_info(void* ctx, int32_t* n_params, int32_t* n_samples, int32_t* fallback_scenes) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (n_params) *n_params = am::learned_num_params();
+    if (n_samples) *n_samples = c->lDn;
+    if (fallback_scenes) *fallback_scenes = c->lFallbackScenes;
+    return AM_OK;
+}
+
+int32_t am_learned_grad(void* ctx, const float* X, const float* Y, int32_t n, float* grad, float* loss) {
+    if (!ctx || !X || !Y || n <= 0 || !grad || !loss) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    return c->learnedGrad(X, Y, n, grad, loss);
+}
+
+int32_t am_learned_infer(void* ctx, const float* X, int32_t n, float* out, int32_t tensor_cores) {
+    if (!ctx || !X || n <= 0 || !out) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    return c->learnedInfer(X, n, out, tensor_cores);
+}
+
 int32_t am_step(void* ctx, double dt) {
     if (!ctx) return AM_E_ARG;
     Ctx* c = (Ctx*)ctx;

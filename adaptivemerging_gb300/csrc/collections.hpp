@@ -6,6 +6,7 @@
 // RigidBody.java:182-206, PlaneRigidBody.java:49-57).  Contacts, pairs and
 // the per-step state live on the device.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -251,6 +252,19 @@ struct Ctx {
     long long* bCS = nullptr;
     int batchConverged = 0;
     std::vector<float> tuneMs;
+    // learned warm start
+    float *lW = nullptr, *lG = nullptr, *lM = nullptr, *lV = nullptr, *lNorm = nullptr, *lBias = nullptr,
+          *lLoss = nullptr;
+    __nv_bfloat16* lWb = nullptr;
+    float *lX = nullptr, *lY = nullptr, *lDX = nullptr, *lDY = nullptr, *lZ1 = nullptr, *lZ2 = nullptr,
+          *lYh = nullptr;
+    int *lKeep = nullptr, *lPos = nullptr, *lIdx = nullptr;
+    int lFeatCap = 0, lDcap = 0, lDn = 0, lTrainCap = 0, lIdxCap = 0;
+    int lCollect = 0, lUse = 0;   // lUse: 0 off, 1 BF16 tensor cores, 2 FP32
+    long long lAdamT = 0;
+    int lFallbackScenes = 0;      // scenes re-solved from the plain warm start, last step
+    float* bLamL = nullptr;       // learned start, packed like bLam
+    int* bFall = nullptr;         // per scene: 1 when it fell back to the plain start
     long long mergeEvents = 0, unmergeEvents = 0;
 
     explicit Ctx(const am_params& p);
@@ -341,6 +355,22 @@ struct Ctx {
     int batchSolve(double dt);
     int batchStats();
     int batchAutotune(double dt);
+    int learnedInit();
+    int ensureFeat(int nc);
+    int learnedFeatures(double dt);
+    int learnedRecord();
+    int learnedPredict(bool tensorCores);
+    int learnedPackInference();
+    int learnedNormalise();
+    int learnedTrain(int epochs, int batch, float lr, float* lastLoss, int normalise);
+    int learnedGrad(const float* X, const float* Y, int n, float* grad, float* loss);
+    int learnedInfer(const float* X, int n, float* out, int tensorCores);
+    int learnedWeights(float* w, const float* in, float* norm, const float* normIn);
+    int learnedCollect(int enable, int capacity);
+    std::vector<void*> tmps;
+    template <class T>
+    int tmpAlloc(T** p, size_t n);
+    int tmpFree(int r);
     int putBodies(const am_body_state* in);
     int getContacts(am_contacts* out, int capacity, int* n);
 };
@@ -358,6 +388,7 @@ int Ctx::alloc(T** p, size_t n) {
 const void* pgs_fast_kernel();
 const void* gs_levels_kernel();
 const void* batch_sweep_kernel();
+int learned_num_params();
 int gs_levels(const std::vector<int>& s1, const std::vector<int>& s2, const std::vector<int>& flags,
               std::vector<int>& order, std::vector<int>& levelOff, std::vector<int>& last);
 void launch_gs_levels(const DBodies& B, DContacts& C, const int* order, const int* levelOff, int nLevels, int iters,

@@ -19,7 +19,9 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libam.so")
 EXPORTS = [
     "am_params_default", "am_create", "am_destroy", "am_last_error", "am_set_params", "am_set_scene",
     "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
-    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats",
+    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats",
+    "am_learned_collect", "am_learned_train", "am_learned_use", "am_learned_weights", "am_learned_info",
+    "am_learned_grad", "am_learned_infer",
 ]
 
 _lib = None
@@ -60,6 +62,16 @@ def lib():
         L.am_set_batch.argtypes = [vp, C.POINTER(abi.am_scene), C.c_int32]
         L.am_set_batch_options.argtypes = [vp, C.c_int32, C.c_double, C.c_int32]
         L.am_get_batch_stats.argtypes = [vp, C.POINTER(abi.am_batch_stats)]
+        fp = C.POINTER(C.c_float)
+        ip = C.POINTER(C.c_int32)
+        L.am_get_batch_scene_stats.argtypes = [vp, ip, fp, ip]
+        L.am_learned_collect.argtypes = [vp, C.c_int32, C.c_int32]
+        L.am_learned_train.argtypes = [vp, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_double)]
+        L.am_learned_use.argtypes = [vp, C.c_int32]
+        L.am_learned_weights.argtypes = [vp, fp, fp, fp, fp]
+        L.am_learned_info.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.am_learned_grad.argtypes = [vp, fp, fp, C.c_int32, fp, fp]
+        L.am_learned_infer.argtypes = [vp, fp, C.c_int32, fp, C.c_int32]
         L.am_get_topology.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32,
                                       C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.am_reset_perf.argtypes = [vp]
@@ -94,6 +106,63 @@ class BatchSystem:
         st = abi.am_batch_stats()
         self._check(lib().am_get_batch_stats(self.h, C.byref(st)))
         return st
+
+    def scene_stats(self):
+        n = len(self.scenes)
+        sw = np.zeros(n, np.int32)
+        rs = np.zeros(n, np.float32)
+        fb = np.zeros(n, np.int32)
+        self._check(lib().am_get_batch_scene_stats(self.h, sw.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                   rs.ctypes.data_as(C.POINTER(C.c_float)),
+                                                   fb.ctypes.data_as(C.POINTER(C.c_int32))))
+        return {"sweeps": sw, "residual": rs, "fell_back": fb}
+
+    # learned warm start
+    def learned_collect(self, enable=True, capacity=2_000_000):
+        self._check(lib().am_learned_collect(self.h, int(enable), int(capacity)))
+
+    def learned_train(self, epochs=20, batch=8192, lr=3e-3, normalise=True):
+        loss = C.c_double()
+        self._check(lib().am_learned_train(self.h, epochs, batch, lr, int(normalise), C.byref(loss)))
+        return loss.value
+
+    def learned_use(self, mode=1):
+        self._check(lib().am_learned_use(self.h, mode))
+
+    def learned_info(self):
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(lib().am_learned_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"n_params": a.value, "n_samples": b.value, "fallback_scenes": c.value}
+
+    def learned_weights(self, set_w=None, set_norm=None):
+        info = self.learned_info()
+        w = np.zeros(info["n_params"], np.float32)
+        nm = np.zeros(48, np.float32)
+        fp = C.POINTER(C.c_float)
+        sw = None if set_w is None else np.ascontiguousarray(set_w, np.float32)
+        sn = None if set_norm is None else np.ascontiguousarray(set_norm, np.float32)
+        self._check(lib().am_learned_weights(self.h, w.ctypes.data_as(fp),
+                                             None if sw is None else sw.ctypes.data_as(fp),
+                                             nm.ctypes.data_as(fp), None if sn is None else sn.ctypes.data_as(fp)))
+        return w, nm
+
+    def learned_grad(self, X, Y):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.ascontiguousarray(Y, np.float32)
+        g = np.zeros(self.learned_info()["n_params"], np.float32)
+        loss = np.zeros(1, np.float32)
+        fp = C.POINTER(C.c_float)
+        self._check(lib().am_learned_grad(self.h, X.ctypes.data_as(fp), Y.ctypes.data_as(fp), len(X),
+                                          g.ctypes.data_as(fp), loss.ctypes.data_as(fp)))
+        return float(loss[0]), g
+
+    def learned_infer(self, X, tensor_cores=True):
+        X = np.ascontiguousarray(X, np.float32)
+        out = np.zeros((len(X), 3), np.float32)
+        fp = C.POINTER(C.c_float)
+        self._check(lib().am_learned_infer(self.h, X.ctypes.data_as(fp), len(X), out.ctypes.data_as(fp),
+                                           int(tensor_cores)))
+        return out
 
 
 class System:

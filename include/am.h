@@ -242,6 +242,32 @@ int32_t am_set_batch(void* ctx, const am_scene* scenes, int32_t n_scenes);
 /* threads: 0 = autotune on the first step; residual_target <= 0 disables the test */
 int32_t am_set_batch_options(void* ctx, int32_t threads, double residual_target, int32_t check_every);
 int32_t am_get_batch_stats(void* ctx, am_batch_stats* out);
+/* per-scene figures of the last step (arrays of n_scenes; NULL skips one) */
+int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, int32_t* fell_back);
+
+/*
+ * Learned warm start for the batched solve (no reference counterpart).  An
+ * MLP 24 -> 64 -> 64 -> 3 (GELU) maps per-contact features to the converged
+ * multipliers; it is trained on the device by the library's own forward,
+ * backward and Adam kernels from (features, converged multiplier) pairs that
+ * the plain solver records, and evaluated with BF16 weights on the tensor
+ * cores.  Scenes that miss the residual target from the learned start are
+ * solved again from the plain previous-frame warm start.
+ */
+/* record (features, converged multipliers) of converged scenes during am_step */
+int32_t am_learned_collect(void* ctx, int32_t enable, int32_t capacity);
+/* mini-batch Adam over the recorded samples; normalise = 1 recomputes feature scaling */
+int32_t am_learned_train(void* ctx, int32_t epochs, int32_t batch, double lr, int32_t normalise, double* last_loss);
+/* 0: plain warm start; 1: learned start, BF16 tensor-core inference; 2: learned start, FP32 inference */
+int32_t am_learned_use(void* ctx, int32_t mode);
+/* get / set the FP32 parameters (n_params floats) and the feature scaling (48 floats); NULL skips */
+int32_t am_learned_weights(void* ctx, float* get, const float* set, float* norm_get, const float* norm_set);
+/* n_params, recorded samples, scenes that fell back to the plain start in the last step */
+int32_t am_learned_info(void* ctx, int32_t* n_params, int32_t* n_samples, int32_t* fallback_scenes);
+/* loss and gradient of the current parameters on n samples (X: n x 24, Y: n x 3, row-major) */
+int32_t am_learned_grad(void* ctx, const float* X, const float* Y, int32_t n, float* grad, float* loss);
+/* network outputs for n feature rows; tensor_cores = 1 uses the BF16 kernel */
+int32_t am_learned_infer(void* ctx, const float* X, int32_t n, float* out, int32_t tensor_cores);
 
 /* Top-level body list (RigidBodySystem.bodies, RigidBodySystem.java:31) with
  * collection membership (RigidCollection.bodies, RigidCollection.java:28):
