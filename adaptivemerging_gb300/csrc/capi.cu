@@ -266,6 +266,13 @@ int32_t am_learned_infer(void* ctx, const float* X, int32_t n, float* out, int32
     return c->learnedInfer(X, n, out, tensor_cores);
 }
 
+int32_t am_learned_infer_noalloc(void* ctx, const float* X, int32_t n, float* out, int32_t tensor_cores) {
+    if (!ctx || !X || n <= 0 || !out) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    return c->learnedInferNoAlloc(X, n, out, tensor_cores);
+}
+
 int32_t am_step(void* ctx, double dt) {
     if (!ctx) return AM_E_ARG;
     Ctx* c = (Ctx*)ctx;

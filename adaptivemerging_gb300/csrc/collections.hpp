@@ -367,6 +367,7 @@ struct Ctx {
     int learnedInfer(const float* X, int n, float* out, int tensorCores);
     int learnedWeights(float* w, const float* in, float* norm, const float* normIn);
     int learnedCollect(int enable, int capacity);
+    int learnedInferNoAlloc(const float* X, int n, float* out, int tensorCores);
     std::vector<void*> tmps;
     template <class T>
     int tmpAlloc(T** p, size_t n);

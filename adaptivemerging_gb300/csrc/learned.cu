@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "am_ctx.hpp"
@@ -615,6 +616,55 @@ int Ctx::tmpFree(int r) {
     for (void* q : tmps) cudaFree(q);
     tmps.clear();
     return r;
+}
+
+// ---------------------------------------------------------------------------
+// Inference without allocation.  The rows pass through one fixed device
+// scratch per device (AM_NOALLOC_MAX_ROWS rows of 24 input and 3 output
+// floats, 7.1 MB) instead of the per-call temporaries of learnedInfer.  The
+// scratch address is looked up once per device, on the first call made with
+// that device current.  No part of the scratch needs to start at zero: every
+// row a call reads was written by the same call's host-to-device copy.  Two
+// calls that overlap in time on one device (any thread, stream or context)
+// share the scratch and race.
+static const int NOALLOC_ROWS = AM_NOALLOC_MAX_ROWS;
+static const int NOALLOC_MAX_DEVICES = 64;
+static __device__ __align__(256) float g_noalloc_scratch[(size_t)NOALLOC_ROWS * (NIN + NOUT)];
+static float* g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mu;
+
+static float* noalloc_scratch() {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) return nullptr;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return nullptr;
+        g_noalloc_ptr[dev] = (float*)p;
+    }
+    return g_noalloc_ptr[dev];
+}
+
+// Same results as learnedInfer.  Status only (the context's error text is not
+// touched, so a rejected call allocates nothing either).
+int Ctx::learnedInferNoAlloc(const float* X, int n, float* out, int tensorCores) {
+    if (n > NOALLOC_ROWS) return AM_E_CAPACITY;
+    if (!lW || !lWb) return AM_E_STATE;   // weights are set up by am_learned_use / _weights / _train
+    float* base = noalloc_scratch();
+    if (!base) return AM_E_CUDA;
+    float* dX = base;
+    float* dO = base + (size_t)NOALLOC_ROWS * NIN;
+    if (cudaMemcpyAsync(dX, X, sizeof(float) * NIN * (size_t)n, cudaMemcpyHostToDevice, stream) != cudaSuccess)
+        return AM_E_CUDA;
+    k_pack_bf16<<<(NH * NH + 255) / 256, 256, 0, stream>>>(lW, lWb, lBias);
+    if (tensorCores) k_infer_bf16<<<(n + 63) / 64, 128, 0, stream>>>(dX, lNorm, lWb, lBias, n, dO);
+    else k_infer_f32<<<(n + 127) / 128, 128, 0, stream>>>(dX, lNorm, lW, n, dO);
+    AM_LAUNCHED(2);
+    if (cudaGetLastError() != cudaSuccess) return AM_E_CUDA;
+    if (cudaMemcpyAsync(out, dO, sizeof(float) * NOUT * (size_t)n, cudaMemcpyDeviceToHost, stream) != cudaSuccess)
+        return AM_E_CUDA;
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return AM_E_CUDA;
+    return AM_OK;
 }
 
 int learned_num_params() { return NPAR; }

@@ -21,7 +21,7 @@ EXPORTS = [
     "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
     "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats",
     "am_learned_collect", "am_learned_train", "am_learned_use", "am_learned_weights", "am_learned_info",
-    "am_learned_grad", "am_learned_infer",
+    "am_learned_grad", "am_learned_infer", "am_learned_infer_noalloc",
 ]
 
 _lib = None
@@ -72,6 +72,7 @@ def lib():
         L.am_learned_info.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.am_learned_grad.argtypes = [vp, fp, fp, C.c_int32, fp, fp]
         L.am_learned_infer.argtypes = [vp, fp, C.c_int32, fp, C.c_int32]
+        L.am_learned_infer_noalloc.argtypes = [vp, fp, C.c_int32, fp, C.c_int32]
         L.am_get_topology.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32,
                                       C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.am_reset_perf.argtypes = [vp]

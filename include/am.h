@@ -269,6 +269,27 @@ int32_t am_learned_grad(void* ctx, const float* X, const float* Y, int32_t n, fl
 /* network outputs for n feature rows; tensor_cores = 1 uses the BF16 kernel */
 int32_t am_learned_infer(void* ctx, const float* X, int32_t n, float* out, int32_t tensor_cores);
 
+/*
+ * am_learned_infer without allocation (no counterpart in the reference).
+ * Same arguments and results as am_learned_infer, but the rows pass through a
+ * fixed device scratch of AM_NOALLOC_MAX_ROWS rows (7.1 MB per device)
+ * instead of device temporaries allocated and freed by every call.  It is for
+ * hosts that must not allocate inside their step loop: a real-time JNI / FFM
+ * thread, where cudaMalloc / cudaFree can stall on device-wide
+ * synchronisation, and hosts that reserve the device memory for their own
+ * pool up front and leave the library none to take mid-run.
+ *   - needs the context's weights set up first (am_learned_use,
+ *     am_learned_weights or am_learned_train), else AM_E_STATE;
+ *   - n > AM_NOALLOC_MAX_ROWS returns AM_E_CAPACITY, n <= 0 AM_E_ARG;
+ *   - errors are reported by the status alone (am_last_error is not updated);
+ *   - the first call on a device, made with that device current, looks up
+ *     the scratch's address; make that first call before any stream capture;
+ *   - calls that overlap in time on one device share the scratch and race:
+ *     serialise them.
+ */
+#define AM_NOALLOC_MAX_ROWS 65536
+int32_t am_learned_infer_noalloc(void* ctx, const float* X, int32_t n, float* out, int32_t tensor_cores);
+
 /* Top-level body list (RigidBodySystem.bodies, RigidBodySystem.java:31) with
  * collection membership (RigidCollection.bodies, RigidCollection.java:28):
  * entry t spans items[item_off[t] .. item_off[t+1]); a free body is [id], a
