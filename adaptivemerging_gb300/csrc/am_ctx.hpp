@@ -121,6 +121,8 @@ struct DCount {
     double res_abs;  // residual
     double lam_max;
     int n_prev;      // contacts in the previous buffer
+    unsigned long long reschk[2];  // residual-target check of the coloured solve (double bits, by check parity)
+    unsigned long long lamchk[2];
 };
 
 // ---- kernels / launchers (defined in the .cu files) ----------------------
@@ -152,7 +154,7 @@ void colour_groups(const DBodies& B, const DContacts& C, DPairs& P, int npairs, 
 void launch_pgs_fast(const DBodies& B, DContacts& C, DPairs& P, const int* groupOrder, const int* colourOff,
                      int ncol, int nc, int iters, double omega, double comp, double tol, bool early, int fo,
                      double fv, double slide, double* Mj, double* invD, int mcap, DCount* dc, int gridBlocks,
-                     cudaStream_t s);
+                     cudaStream_t s, double resTol = 0.0, int check = 0);
 void launch_residual(const DBodies& B, DContacts& C, int nc, double comp, int frictionOv, double frictionVal,
                      DCount* dc, cudaStream_t s);
 void launch_bpc_keep(const DContacts& C, DPairs& P, int npairs, cudaStream_t s);

@@ -82,12 +82,20 @@ __global__ void k_batch_pack(DBodies B, DContacts C, int nc, const int* sceneOf,
     lid[c] = make_int2(s1 - base, s2 - base);
 }
 
-// colour the groups of one scene (one CTA per scene)
+// Colour the groups (body pairs) of one scene, one CTA per scene:
+// Jones-Plassmann rounds with first-fit colours.  Each round, an uncoloured
+// group whose priority is the largest among the uncoloured groups at both of
+// its (non-pinned) bodies takes the smallest colour not yet used at either
+// body.  Selected groups of one round share no body, so the per-body colour
+// masks need no atomics between them.  Priorities put groups with more
+// contacts first (they then sit in the low colours), ties broken by a hash
+// and made unique by the group index.
 __global__ void k_batch_colour(DBodies B, DContacts C, DPairs P, const int* pairOff, const int* sceneBodyOff,
                                int* colourOf, int* gOrder, int* colOff, int maxBodies, DCount* dc) {
-    extern __shared__ unsigned smemu[];
-    unsigned* bodyMax = smemu;                 // [maxBodies]
-    __shared__ int s_left, s_cnt[MAXCB + 1];
+    extern __shared__ unsigned long long smemq[];
+    unsigned long long* bodyMax = smemq;               // [maxBodies] largest uncoloured priority
+    unsigned long long* used = smemq + maxBodies;      // [maxBodies] colours taken at the body
+    __shared__ int s_left, s_full, s_cnt[MAXCB + 1];
     int s = blockIdx.x;
     int g0 = pairOff[s], g1 = pairOff[s + 1];
     int b0 = sceneBodyOff[s], nb = sceneBodyOff[s + 1] - b0;
@@ -95,19 +103,25 @@ __global__ void k_batch_colour(DBodies B, DContacts C, DPairs P, const int* pair
     if (nb > maxBodies) { if (t == 0) dc->error = AM_E_CAPACITY; return; }
     for (int g = g0 + t; g < g1; g += T) colourOf[g] = P.count[g] > 0 ? -1 : -2;
     for (int k = t; k <= MAXCB; k += T) s_cnt[k] = 0;
+    for (int b = t; b < nb; b += T) used[b] = 0ull;
+    if (t == 0) s_full = 0;
     __syncthreads();
-    int ncol = 0;
-    for (int round = 0; round < MAXCB; round++) {
-        for (int b = t; b < nb; b += T) bodyMax[b] = 0u;
+    auto prio = [&](int g) -> unsigned long long {
+        unsigned h = (unsigned)g * 2654435761u;
+        h ^= h >> 16;
+        unsigned long long cnt = (unsigned long long)min(P.count[g], 255);
+        return (cnt << 56) | ((unsigned long long)(h & 0xFFFFFFu) << 32) | (unsigned)(g - g0);
+    };
+    const int maxRounds = 1 << 16;
+    for (int round = 0; round < maxRounds; round++) {
+        for (int b = t; b < nb; b += T) bodyMax[b] = 0ull;
         if (t == 0) s_left = 0;
         __syncthreads();
         for (int g = g0 + t; g < g1; g += T) {
             if (colourOf[g] != -1) continue;
             int c = P.off[g];
             int s1 = C.sb1[c], s2 = C.sb2[c];
-            unsigned h = (unsigned)g * 2654435761u;
-            h ^= h >> 16;
-            unsigned pr = (h & 0xFFFF0000u) | (unsigned)((g - g0) & 0xFFFF) | 1u << 31;
+            unsigned long long pr = prio(g);
             if (!(B.flags[s1] & F_PINNED)) atomicMax(&bodyMax[s1 - b0], pr);
             if (!(B.flags[s2] & F_PINNED)) atomicMax(&bodyMax[s2 - b0], pr);
         }
@@ -116,22 +130,28 @@ __global__ void k_batch_colour(DBodies B, DContacts C, DPairs P, const int* pair
             if (colourOf[g] != -1) continue;
             int c = P.off[g];
             int s1 = C.sb1[c], s2 = C.sb2[c];
-            unsigned h = (unsigned)g * 2654435761u;
-            h ^= h >> 16;
-            unsigned pr = (h & 0xFFFF0000u) | (unsigned)((g - g0) & 0xFFFF) | 1u << 31;
-            bool ok = ((B.flags[s1] & F_PINNED) || bodyMax[s1 - b0] == pr) &&
-                      ((B.flags[s2] & F_PINNED) || bodyMax[s2 - b0] == pr);
-            if (ok) { colourOf[g] = round; atomicAdd(&s_cnt[round], 1); }
-            else atomicAdd(&s_left, 1);
+            bool p1 = B.flags[s1] & F_PINNED, p2 = B.flags[s2] & F_PINNED;
+            unsigned long long pr = prio(g);
+            bool ok = (p1 || bodyMax[s1 - b0] == pr) && (p2 || bodyMax[s2 - b0] == pr);
+            if (!ok) { atomicAdd(&s_left, 1); continue; }
+            unsigned long long m = (p1 ? 0ull : used[s1 - b0]) | (p2 ? 0ull : used[s2 - b0]);
+            if (m == ~0ull) { colourOf[g] = -2; s_full = 1; continue; }   // more than MAXCB colours needed
+            int col = __ffsll((long long)~m) - 1;
+            if (!p1) used[s1 - b0] |= 1ull << col;
+            if (!p2) used[s2 - b0] |= 1ull << col;
+            colourOf[g] = col;
+            atomicAdd(&s_cnt[col], 1);
         }
         __syncthreads();
         int left = s_left;
-        ncol = round + 1;
         __syncthreads();
         if (left == 0) break;
     }
+    __syncthreads();
     if (t == 0) {
-        if (s_left) dc->error = AM_E_CAPACITY;
+        if (s_left || s_full) dc->error = AM_E_CAPACITY;
+        int ncol = 0;
+        for (int k = 0; k < MAXCB; k++) if (s_cnt[k]) ncol = k + 1;
         int run = g0;
         for (int k = 0; k < ncol; k++) { int n = s_cnt[k]; s_cnt[k] = run; colOff[s * (MAXCB + 1) + k] = run; run += n; }
         for (int k = ncol; k <= MAXCB; k++) colOff[s * (MAXCB + 1) + k] = run;
@@ -144,6 +164,24 @@ __global__ void k_batch_colour(DBodies B, DContacts C, DPairs P, const int* pair
 }
 
 __device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ void prefetch_l1(const float* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+// J . dv of one row over the group's two bodies (record layout: a.v a.w b.v b.w
+// in j0..j2), as two independent half sums
+__device__ __forceinline__ float group_jdv(const float* a, const float* b, float4 j0, float4 j1, float4 j2) {
+    float sa = j0.x * a[0] + j0.y * a[1] + j0.z * a[2] + j0.w * a[3] + j1.x * a[4] + j1.y * a[5];
+    float sb = j1.z * b[0] + j1.w * b[1] + j2.x * b[2] + j2.y * b[3] + j2.z * b[4] + j2.w * b[5];
+    return sa + sb;
+}
+
+// delta-v += (minv J.v, jinv J.w) * d for both bodies (i0, i1 hold jinv J.w)
+__device__ __forceinline__ void group_update(float* a, float* b, float la, float lb, float d, float4 j0, float4 j1,
+                                             float4 j2, float4 i0, float4 i1) {
+    a[0] += la * j0.x; a[1] += la * j0.y; a[2] += la * j0.z;
+    a[3] += d * i0.x; a[4] += d * i0.y; a[5] += d * i0.z;
+    b[0] += lb * j1.z; b[1] += lb * j1.w; b[2] += lb * j2.x;
+    b[3] += d * i0.w; b[4] += d * i1.x; b[5] += d * i1.y;
+}
 
 // one CTA per scene; dynamic smem: dv[6 * maxBodies] + minv[maxBodies]
 __global__ void k_batch_sweep(DBodies B, DContacts C, DPairs P, const int* pairOff, const int* sceneBodyOff,
@@ -158,7 +196,9 @@ __global__ void k_batch_sweep(DBodies B, DContacts C, DPairs P, const int* pairO
     __shared__ float s_res, s_lam;
     __shared__ int s_stop;
     int t = threadIdx.x, T = blockDim.x;
-    for (int b = t; b < nb; b += T) mv[b] = (float)B.minv[b0 + b];
+    // pinned bodies get 0 here, the same test the colouring uses to let groups
+    // of one colour share them
+    for (int b = t; b < nb; b += T) mv[b] = (B.flags[b0 + b] & F_PINNED) ? 0.f : (float)B.minv[b0 + b];
     const int* co = colOff + s * (MAXCB + 1);
     int ncol = 0;
     while (ncol < MAXCB && co[ncol + 1] > co[ncol]) ncol++;
@@ -180,27 +220,29 @@ __global__ void k_batch_sweep(DBodies B, DContacts C, DPairs P, const int* pairO
         for (int b = t; b < nb; b += T)
             for (int k = 0; k < 6; k++) dv[6 * b + k] = 0.f;
         __syncthreads();
-        // confidentWarmStart
+        // confidentWarmStart.  Every contact of a group acts on the same two
+        // bodies, so their delta-v stays in registers for the whole group.
         for (int col = 0; col < ncol; col++) {
             for (int k = co[col] + t; k < co[col + 1]; k += T) {
                 int g = gOrder[k];
-                for (int c = P.off[g]; c < P.off[g] + P.count[g]; c++) {
-                    int2 id = lid[c];
+                int c0 = P.off[g], c1 = c0 + P.count[g];
+                int2 id = lid[c0];
+                float a[6], b[6];
+                for (int q = 0; q < 6; q++) { a[q] = dv[6 * id.x + q]; b[q] = dv[6 * id.y + q]; }
+                float ma = mv[id.x], mb = mv[id.y];
+                for (int c = c0; c < c1; c++) {
                     const float* R = rec + (size_t)REC * c;
-                    float* da = dv + 6 * id.x;
-                    float* db = dv + 6 * id.y;
-                    float ma = mv[id.x], mb = mv[id.y];
+#pragma unroll
                     for (int q = 0; q < 3; q++) {
                         float l = lamf[3 * c + q];
                         float4 j0 = ld4(R + 20 * q), j1 = ld4(R + 20 * q + 4), j2 = ld4(R + 20 * q + 8);
                         float4 i0 = ld4(R + 20 * q + 12), i1 = ld4(R + 20 * q + 16);
-                        float la = ma * l, lb = mb * l;
-                        da[0] += la * j0.x; da[1] += la * j0.y; da[2] += la * j0.z;
-                        da[3] += l * i0.x; da[4] += l * i0.y; da[5] += l * i0.z;
-                        db[0] += lb * j1.z; db[1] += lb * j1.w; db[2] += lb * j2.x;
-                        db[3] += l * i0.w; db[4] += l * i1.x; db[5] += l * i1.y;
+                        group_update(a, b, ma * l, mb * l, l, j0, j1, j2, i0, i1);
                     }
                 }
+                // pinned bodies (minv = 0) never change and may be shared within a colour
+                if (ma != 0.f) for (int q = 0; q < 6; q++) dv[6 * id.x + q] = a[q];
+                if (mb != 0.f) for (int q = 0; q < 6; q++) dv[6 * id.y + q] = b[q];
             }
             __syncthreads();
         }
@@ -210,37 +252,47 @@ __global__ void k_batch_sweep(DBodies B, DContacts C, DPairs P, const int* pairO
             for (int col = 0; col < ncol; col++) {
                 for (int k = co[col] + t; k < co[col + 1]; k += T) {
                     int g = gOrder[k];
-                    for (int c = P.off[g]; c < P.off[g] + P.count[g]; c++) {
-                        int2 id = lid[c];
+                    int c0 = P.off[g], c1 = c0 + P.count[g];
+                    int2 id = lid[c0];
+                    float a[6], b[6];
+                    for (int q = 0; q < 6; q++) { a[q] = dv[6 * id.x + q]; b[q] = dv[6 * id.y + q]; }
+                    float ma = mv[id.x], mb = mv[id.y];
+                    for (int c = c0; c < c1; c++) {
                         const float* R = rec + (size_t)REC * c;
-                        float* da = dv + 6 * id.x;
-                        float* db = dv + 6 * id.y;
-                        float ma = mv[id.x], mb = mv[id.y];
                         float4 tail = ld4(R + 60);
-                        float l0 = lamf[3 * c];
-                        float lam[3];
+                        float lam[3] = {lamf[3 * c], lamf[3 * c + 1], lamf[3 * c + 2]};
+                        float l0 = lam[0];
+#pragma unroll
                         for (int q = 0; q < 3; q++) {
                             float4 j0 = ld4(R + 20 * q), j1 = ld4(R + 20 * q + 4), j2 = ld4(R + 20 * q + 8);
                             float4 i0 = ld4(R + 20 * q + 12), i1 = ld4(R + 20 * q + 16);
-                            float jd = j0.x * da[0] + j0.y * da[1] + j0.z * da[2] + j0.w * da[3] + j1.x * da[4] +
-                                       j1.y * da[5] + j1.z * db[0] + j1.w * db[1] + j2.x * db[2] + j2.y * db[3] +
-                                       j2.z * db[4] + j2.w * db[5];
+                            float jd = group_jdv(a, b, j0, j1, j2);
                             float D = q == 0 ? tail.x : (q == 1 ? tail.y : tail.z);
-                            float l = lamf[3 * c + q];
+                            float l = lam[q];
                             float nl = (D * l - omega * (i1.z + jd)) * i1.w;
                             if (q == 0) nl = fmaxf(nl, 0.f);
                             else { float lim = tail.w * l0; nl = fminf(fmaxf(nl, -lim), lim); }
                             float d = nl - l;
                             if (q == 0) l0 = nl;
                             lam[q] = nl;
-                            float la = ma * d, lb = mb * d;
-                            da[0] += la * j0.x; da[1] += la * j0.y; da[2] += la * j0.z;
-                            da[3] += d * i0.x; da[4] += d * i0.y; da[5] += d * i0.z;
-                            db[0] += lb * j1.z; db[1] += lb * j1.w; db[2] += lb * j2.x;
-                            db[3] += d * i0.w; db[4] += d * i1.x; db[5] += d * i1.y;
+                            group_update(a, b, ma * d, mb * d, d, j0, j1, j2, i0, i1);
                         }
                         lamf[3 * c] = lam[0]; lamf[3 * c + 1] = lam[1]; lamf[3 * c + 2] = lam[2];
-                        (void)last;
+                    }
+                    if (ma != 0.f) for (int q = 0; q < 6; q++) dv[6 * id.x + q] = a[q];
+                    if (mb != 0.f) for (int q = 0; q < 6; q++) dv[6 * id.y + q] = b[q];
+                }
+                // while the colour drains, pull this thread's first group of the
+                // next colour (or of colour 0 for the next sweep) into L1
+                {
+                    int nc2 = col + 1 < ncol ? col + 1 : 0;
+                    int k2 = co[nc2] + t;
+                    if (k2 < co[nc2 + 1]) {
+                        int g2 = gOrder[k2];
+                        const float* R2 = rec + (size_t)REC * P.off[g2];
+                        int lines = 2 * P.count[g2];
+                        for (int q = 0; q < lines; q++) prefetch_l1(R2 + 32 * q);
+                        prefetch_l1(lamf + 3 * P.off[g2]);
                     }
                 }
                 __syncthreads();
@@ -338,7 +390,7 @@ int Ctx::batchSolve(double dt) {
     k_scene_ranges<<<(np + 1 + 255) / 256, 256, 0, stream>>>(PR, np, sceneOfDev, S, bPairOff);
     k_batch_pack<<<(nc + 127) / 128, 128, 0, stream>>>(B, C[cur], nc, sceneOfDev, sceneBodyOffDev, comp,
                                                      P.friction_override, P.friction, bRec, bLid, bLam);
-    size_t csm = sizeof(unsigned) * (size_t)maxSceneBodies;
+    size_t csm = 2 * sizeof(unsigned long long) * (size_t)maxSceneBodies;
     k_batch_colour<<<S, 256, csm, stream>>>(B, C[cur], PR, bPairOff, sceneBodyOffDev, bColour, bOrder, bColOff,
                                             maxSceneBodies, dc);
     size_t ssm = sizeof(float) * 7 * (size_t)maxSceneBodies;
@@ -374,6 +426,21 @@ __global__ void k_scene_cs(DPairs P, int npairs, int nc, const int* pairOff, con
     int a = pairOff[s] < npairs ? P.off[pairOff[s]] : nc;
     int b = pairOff[s + 1] < npairs ? P.off[pairOff[s + 1]] : nc;
     out[s] = (long long)(b - a) * sweeps[s];
+}
+
+// colours per scene of the last colouring (colours are contiguous from 0)
+int Ctx::batchColours(int* out) {
+    std::vector<int> co((size_t)nScenes * (MAXCB + 1));
+    cudaMemcpyAsync(co.data(), bColOff, sizeof(int) * co.size(), cudaMemcpyDeviceToHost, stream);
+    int r = syncErr();
+    if (r) return r;
+    for (int s = 0; s < nScenes; s++) {
+        const int* c = co.data() + (size_t)s * (MAXCB + 1);
+        int n = 0;
+        while (n < MAXCB && c[n + 1] > c[n]) n++;
+        out[s] = n;
+    }
+    return AM_OK;
 }
 
 int Ctx::batchStats() {
@@ -466,6 +533,9 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     cudaMemcpyAsync(topEnd, tEnd.data(), sizeof(int) * all.n_bodies, cudaMemcpyHostToDevice, stream);
     size_t ssm = sizeof(float) * 7 * (size_t)maxSceneBodies;
     if (ssm > 48 * 1024) cudaFuncSetAttribute(batch_sweep_kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm);
+    size_t csm = 2 * sizeof(unsigned long long) * (size_t)maxSceneBodies;
+    if (csm > 48 * 1024)
+        cudaFuncSetAttribute((const void*)k_batch_colour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm);
     return syncErr();
 }
 

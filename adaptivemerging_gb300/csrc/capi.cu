@@ -197,7 +197,15 @@ int32_t am_get_batch_stats(void* ctx, am_batch_stats* o) {
     return AM_OK;
 }
 
-int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, int32_t* fell_back) {
+int32_t am_set_residual_target(void* ctx, double residual_target, int32_t check_every) {
+    if (!ctx || check_every < 0 || !(residual_target >= 0)) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    c->solveTol = residual_target;
+    c->solveCheck = check_every;
+    return AM_OK;
+}
+
+int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, int32_t* fell_back, int32_t* colours) {
     if (!ctx) return AM_E_ARG;
     Ctx* c = (Ctx*)ctx;
     if (!c->nScenes || !c->bSweeps) return AM_E_STATE;
@@ -205,6 +213,7 @@ int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, in
     if (sweeps) cudaMemcpyAsync(sweeps, c->bSweeps, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream);
     if (residual) cudaMemcpyAsync(residual, c->bRes, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
     if (fell_back) cudaMemcpyAsync(fell_back, c->bFall, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream);
+    if (colours) return c->batchColours(colours);
     return c->syncErr();
 }
 
@@ -233,6 +242,12 @@ int32_t am_learned_use(void* ctx, int32_t mode) {
     if (r) return r;
     if (mode && (r = c->learnedPackInference())) return r;
     c->lUse = mode;
+    return AM_OK;
+}
+
+int32_t am_learned_scope(void* ctx, int32_t scope) {
+    if (!ctx || scope < 0 || scope > 1) return AM_E_ARG;
+    ((Ctx*)ctx)->lScope = scope;
     return AM_OK;
 }
 

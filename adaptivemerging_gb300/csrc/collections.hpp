@@ -245,6 +245,8 @@ struct Ctx {
     int* bSweeps = nullptr;
     float* bRes = nullptr;
     int batchThreads = 0;        // 0: autotune on the first solve
+    double solveTol = 0.0;       // coloured single-scene solve: relative residual target (0: off)
+    int solveCheck = 0;
     double batchTol = 1e-6;      // relative natural-map residual target
     int batchCheck = 10;         // sweeps between residual checks
     long long batchSweepsTotal = 0;
@@ -261,6 +263,7 @@ struct Ctx {
     int *lKeep = nullptr, *lPos = nullptr, *lIdx = nullptr;
     int lFeatCap = 0, lDcap = 0, lDn = 0, lTrainCap = 0, lIdxCap = 0;
     int lCollect = 0, lUse = 0;   // lUse: 0 off, 1 BF16 tensor cores, 2 FP32
+    int lScope = 0;               // 0: fresh contacts take the learned start, 1: all contacts
     long long lAdamT = 0;
     int lFallbackScenes = 0;      // scenes re-solved from the plain warm start, last step
     float* bLamL = nullptr;       // learned start, packed like bLam
@@ -355,6 +358,7 @@ struct Ctx {
     int batchSolve(double dt);
     int batchStats();
     int batchAutotune(double dt);
+    int batchColours(int* out);
     int learnedInit();
     int ensureFeat(int nc);
     int learnedFeatures(double dt);

@@ -7,18 +7,19 @@
 //                   solver setup (free contact velocity b, penetration / dt,
 //                   normal, previous-frame impulse * D, persistence, mu,
 //                   log-D ratios, mass split, contacts in the pair, ...);
-//   * k_labels    : lambda * D of the converged solve (recorded for fresh
-//                   contacts of scenes that reached the residual target);
+//   * k_labels    : (lambda - lambda_warm) * D of the converged solve, the
+//                   change from the previous-frame start (recorded for the
+//                   contacts in scope of scenes that reached the target);
 //   * training    : FP32 forward (k_fwd), backward with per-block weight-
 //                   gradient reduction (k_bwd), Adam (k_adam), MSE loss;
 //   * inference   : BF16 weights on the tensor cores (mma.sync m16n8k16,
 //                   FP32 accumulate); the 16 x 8 accumulator tiles of one
 //                   layer are re-packed in registers as the A operand of the
 //                   next, so activations never leave the warp;
-//   * the prediction is projected (lambda_n >= 0, |lambda_t| <= mu lambda_n)
-//                   and becomes the start of fresh contacts, whose plain
-//                   start is zero; persisting contacts keep the previous-frame
-//                   impulse.
+//   * lambda_warm + prediction / D, projected (lambda_n >= 0,
+//                   |lambda_t| <= mu lambda_n), becomes the start of the
+//                   contacts in scope: fresh contacts only (scope 0, whose
+//                   plain start is zero) or all contacts (scope 1).
 // Features are standardised with the training set's mean and deviation.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -85,18 +86,24 @@ __global__ void k_features(DBodies B, DContacts C, DPairs P, int nc, float dt, i
     for (int k = 0; k < NIN; k++) X[(size_t)c * NIN + k] = f[k];
 }
 
+// label: the converged impulse's change from the previous-frame start, in
+// velocity units ((lambda - lambda_warm) * D); for a fresh contact the start
+// is zero and the label is lambda * D
 __global__ void k_labels(DContacts C, int nc, float* Y) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
     int cap = C.cap;
-    for (int r = 0; r < 3; r++) Y[(size_t)c * NOUT + r] = (float)(C.lam[r * cap + c] * C.bD[(3 + r) * cap + c]);
+    for (int r = 0; r < 3; r++)
+        Y[(size_t)c * NOUT + r] = (float)((C.lam[r * cap + c] - C.lamw[r * cap + c]) * C.bD[(3 + r) * cap + c]);
 }
 
-// keep flag: a fresh contact whose scene reached the residual target
-__global__ void k_keep_converged(DContacts C, int nc, const int* sceneOf, const float* sceneRes, float tol, int* keep) {
+// keep flag: a contact in scope (fresh ones, or all) whose scene reached the
+// residual target
+__global__ void k_keep_converged(DContacts C, int nc, const int* sceneOf, const float* sceneRes, float tol, int all,
+                                 int* keep) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
-    keep[c] = (C.fresh[c] && sceneRes[sceneOf[C.b1[c]]] <= tol) ? 1 : 0;
+    keep[c] = ((all || C.fresh[c]) && sceneRes[sceneOf[C.b1[c]]] <= tol) ? 1 : 0;
 }
 
 __global__ void k_append(const float* X, const float* Y, const int* keep, const int* pos, int nc, float* DX,
@@ -364,22 +371,22 @@ __global__ void k_pack_bf16(const float* W, __nv_bfloat16* Wb, float* bias) {
     if (k < 8) bias[2 * NH + k] = k < NOUT ? W[OB3 + k] : 0.f;
 }
 
-// predicted lambda = y / D, projected on the friction cone, packed (3 floats
-// per contact) as the batched solver's learned start.  Only fresh contacts
-// (no previous-frame impulse to carry over) take the prediction; a persisting
-// contact keeps its previous-frame impulse, already the converged value of the
-// last step.
-__global__ void k_apply_prediction(DBodies B, DContacts C, int nc, const float* Yp, int fo, float fv,
+// learned start = previous-frame start + y / D, projected on the friction
+// cone, packed (3 floats per contact) as the batched solver's start.  With
+// scope 0 only fresh contacts (no previous-frame impulse) take it; the others
+// keep the plain start, already the converged impulse of the last step.
+__global__ void k_apply_prediction(DBodies B, DContacts C, int nc, const float* Yp, int fo, float fv, int all,
                                    const float* lamPlain, float* lamL) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
-    if (!C.fresh[c]) {
+    if (!all && !C.fresh[c]) {
         for (int r = 0; r < 3; r++) lamL[3 * c + r] = lamPlain[3 * c + r];
         return;
     }
     int cap = C.cap;
     double l[3];
-    for (int r = 0; r < 3; r++) l[r] = (double)Yp[(size_t)c * NOUT + r] / C.bD[(3 + r) * cap + c];
+    for (int r = 0; r < 3; r++)
+        l[r] = C.lamw[r * cap + c] + (double)Yp[(size_t)c * NOUT + r] / C.bD[(3 + r) * cap + c];
     double mu;
     if (fo) mu = fv;
     else {
@@ -442,7 +449,8 @@ int Ctx::learnedRecord() {
     int nc = nContacts;
     if (!lCollect || nc <= 0) return AM_OK;
     k_labels<<<(nc + 127) / 128, 128, 0, stream>>>(C[cur], nc, lY);
-    k_keep_converged<<<(nc + 127) / 128, 128, 0, stream>>>(C[cur], nc, sceneOfDev, bRes, (float)batchTol, lKeep);
+    k_keep_converged<<<(nc + 127) / 128, 128, 0, stream>>>(C[cur], nc, sceneOfDev, bRes, (float)batchTol, lScope,
+                                                           lKeep);
     AM_LAUNCHED(2);
     int* total = &dc->need_contacts;   // scratch counter
     launch_scan(lKeep, lPos, nc, SC, total, stream);
@@ -465,7 +473,7 @@ int Ctx::learnedPredict(bool tensorCores) {
         k_infer_f32<<<(nc + 127) / 128, 128, 0, stream>>>(lX, lNorm, lW, nc, lY);
     }
     k_apply_prediction<<<(nc + 127) / 128, 128, 0, stream>>>(B, C[cur], nc, lY, P.friction_override,
-                                                             (float)P.friction, bLam, bLamL);
+                                                             (float)P.friction, lScope, bLam, bLamL);
     AM_LAUNCHED(2);
     return AM_OK;
 }

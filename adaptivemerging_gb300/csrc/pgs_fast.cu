@@ -88,7 +88,8 @@ __device__ __forceinline__ double mu_fast(const DBodies& B, const DContacts& C, 
 __global__ void __launch_bounds__(128) k_pgs_fast(DBodies B, DContacts C, DPairs P, const int* groupOrder,
                                                    const int* colourOff, int ncol, int iters, double omega,
                                                    double tol, int early, int fo, double fv, double slide,
-                                                   const double* Mj, const double* invD, int mcap, DCount* dc) {
+                                                   const double* Mj, const double* invD, int mcap, DCount* dc,
+                                                   double comp, double resTol, int check) {
     const int nblocks = gridDim.x;
     const int lane = threadIdx.x & 15;
     const int half = (threadIdx.x >> 4) & 1;
@@ -184,6 +185,45 @@ __global__ void __launch_bounds__(128) k_pgs_fast(DBodies B, DContacts C, DPairs
         done = it + 1;
         if (blockIdx.x == 0 && threadIdx.x == 0) dc->maxchg[par ^ 1] = 0ull;
         if (early && change < tol) break;
+        if (check > 0 && resTol > 0 && (done % check == 0 || done == iters)) {
+            // relative natural-map residual max|l - proj(l - w / (D + c))| / max(1, max|l|),
+            // w = b + J dv + c l, over all contacts at the current state
+            const int rp = (done / check) & 1;
+            double rm = 0, lm = 0;
+            for (int k = hw; k < colourOff[ncol]; k += nhw) {
+                int g = groupOrder[k];
+                int c0 = P.off[g], n = P.count[g];
+                int body = act ? (side == 0 ? C.sb1[c0] : C.sb2[c0]) : 0;
+                double dv = act ? __ldcg(B.dv + 6 * body + comp6) : 0.0;
+                for (int c = c0; c < c0 + n; c++) {
+                    double l0 = C.lam[c];
+                    double lim = mu_fast(B, C, c, fo, fv) * l0;
+                    for (int r = 0; r < 3; r++) {
+                        double j = act ? C.J[(12 * r + lane) * ccap + c] : 0.0;
+                        double jd = hw_sum(j * dv, mask);
+                        double l = C.lam[r * ccap + c];
+                        double w = C.bD[r * ccap + c] + jd + comp * l;
+                        double z = l - w * invD[r * mcap + c];
+                        z = r == 0 ? fmax(z, 0.0) : fmin(fmax(z, -lim), lim);
+                        rm = fmax(rm, fabs(l - z));
+                        lm = fmax(lm, fabs(l));
+                    }
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                rm = fmax(rm, __shfl_xor_sync(0xffffffffu, rm, o));
+                lm = fmax(lm, __shfl_xor_sync(0xffffffffu, lm, o));
+            }
+            if ((threadIdx.x & 31) == 0) {
+                if (rm > 0) atomicMax(&dc->reschk[rp], (unsigned long long)__double_as_longlong(rm));
+                if (lm > 0) atomicMax(&dc->lamchk[rp], (unsigned long long)__double_as_longlong(lm));
+            }
+            if (!grid_barrier_f(dc, nblocks)) return;
+            double res = __longlong_as_double((long long)*(volatile unsigned long long*)&dc->reschk[rp]);
+            double lmax = __longlong_as_double((long long)*(volatile unsigned long long*)&dc->lamchk[rp]);
+            if (blockIdx.x == 0 && threadIdx.x == 0) { dc->reschk[rp ^ 1] = 0ull; dc->lamchk[rp ^ 1] = 0ull; }
+            if (res / fmax(1.0, lmax) <= resTol) break;
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         dc->sweeps = done;
@@ -196,16 +236,17 @@ const void* pgs_fast_kernel() { return (const void*)k_pgs_fast; }
 void launch_pgs_fast(const DBodies& B, DContacts& C, DPairs& P, const int* groupOrder, const int* colourOff,
                      int ncol, int nc, int iters, double omega, double comp, double tol, bool early, int fo,
                      double fv, double slide, double* Mj, double* invD, int mcap, DCount* dc, int gridBlocks,
-                     cudaStream_t s) {
+                     cudaStream_t s, double resTol, int check) {
     if (ncol <= 0 || nc <= 0) return;
     k_fast_prep<<<(nc + 127) / 128, 128, 0, s>>>(B, C, nc, comp, Mj, invD, mcap);
     AM_LAUNCHED(1);
     cudaMemsetAsync(&dc->maxchg, 0, sizeof(unsigned long long) * 2, s);
     cudaMemsetAsync(&dc->bar_count, 0, sizeof(int) * 2, s);
+    cudaMemsetAsync(&dc->reschk, 0, sizeof(unsigned long long) * 4, s);
     int earlyI = early ? 1 : 0;
     DBodies Bc = B;
     void* args[] = {&Bc, &C, &P, (void*)&groupOrder, (void*)&colourOff, &ncol, &iters, &omega, &tol, &earlyI,
-                    &fo, &fv, &slide, (void*)&Mj, (void*)&invD, &mcap, &dc};
+                    &fo, &fv, &slide, (void*)&Mj, (void*)&invD, &mcap, &dc, &comp, &resTol, &check};
     cudaLaunchCooperativeKernel((void*)k_pgs_fast, dim3(gridBlocks), dim3(128), args, 0, s);
     AM_LAUNCHED(1);
 }

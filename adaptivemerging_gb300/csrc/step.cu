@@ -642,7 +642,8 @@ int Ctx::runPGS(int nc, const int* order, int iters, bool inColl, double dt, boo
         int blocks = std::min(coopBlocks, std::max(1, (nPairs + 7) / 8));
         if (timed) cudaEventRecord(evA, stream);   // time the sweep (prep + persistent kernel)
         launch_pgs_fast(B, c, PR, groupOrder, colourOff, ncol, nc, iters, P.omega, comp, P.tolerance, !inColl,
-                        P.friction_override, P.friction, P.sliding_threshold, Mj, invD, mjCap, dc, blocks, stream);
+                        P.friction_override, P.friction, P.sliding_threshold, Mj, invD, mjCap, dc, blocks, stream,
+                        inColl ? 0.0 : solveTol, inColl ? 0 : solveCheck);
     }
     if (timed) { cudaEventRecord(evB, stream); pgsPending = true; }
     return AM_OK;

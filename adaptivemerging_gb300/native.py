@@ -19,8 +19,8 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libam.so")
 EXPORTS = [
     "am_params_default", "am_create", "am_destroy", "am_last_error", "am_set_params", "am_set_scene",
     "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
-    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats",
-    "am_learned_collect", "am_learned_train", "am_learned_use", "am_learned_weights", "am_learned_info",
+    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats", "am_set_residual_target",
+    "am_learned_collect", "am_learned_train", "am_learned_use", "am_learned_scope", "am_learned_weights", "am_learned_info",
     "am_learned_grad", "am_learned_infer", "am_learned_infer_noalloc",
 ]
 
@@ -64,10 +64,12 @@ def lib():
         L.am_get_batch_stats.argtypes = [vp, C.POINTER(abi.am_batch_stats)]
         fp = C.POINTER(C.c_float)
         ip = C.POINTER(C.c_int32)
-        L.am_get_batch_scene_stats.argtypes = [vp, ip, fp, ip]
+        L.am_get_batch_scene_stats.argtypes = [vp, ip, fp, ip, ip]
+        L.am_set_residual_target.argtypes = [vp, C.c_double, C.c_int32]
         L.am_learned_collect.argtypes = [vp, C.c_int32, C.c_int32]
         L.am_learned_train.argtypes = [vp, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_double)]
         L.am_learned_use.argtypes = [vp, C.c_int32]
+        L.am_learned_scope.argtypes = [vp, C.c_int32]
         L.am_learned_weights.argtypes = [vp, fp, fp, fp, fp]
         L.am_learned_info.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.am_learned_grad.argtypes = [vp, fp, fp, C.c_int32, fp, fp]
@@ -113,10 +115,11 @@ class BatchSystem:
         sw = np.zeros(n, np.int32)
         rs = np.zeros(n, np.float32)
         fb = np.zeros(n, np.int32)
-        self._check(lib().am_get_batch_scene_stats(self.h, sw.ctypes.data_as(C.POINTER(C.c_int32)),
-                                                   rs.ctypes.data_as(C.POINTER(C.c_float)),
-                                                   fb.ctypes.data_as(C.POINTER(C.c_int32))))
-        return {"sweeps": sw, "residual": rs, "fell_back": fb}
+        nc = np.zeros(n, np.int32)
+        ip = C.POINTER(C.c_int32)
+        self._check(lib().am_get_batch_scene_stats(self.h, sw.ctypes.data_as(ip), rs.ctypes.data_as(C.POINTER(C.c_float)),
+                                                   fb.ctypes.data_as(ip), nc.ctypes.data_as(ip)))
+        return {"sweeps": sw, "residual": rs, "fell_back": fb, "colours": nc}
 
     # learned warm start
     def learned_collect(self, enable=True, capacity=2_000_000):
@@ -129,6 +132,9 @@ class BatchSystem:
 
     def learned_use(self, mode=1):
         self._check(lib().am_learned_use(self.h, mode))
+
+    def learned_scope(self, all_contacts=False):
+        self._check(lib().am_learned_scope(self.h, int(all_contacts)))
 
     def learned_info(self):
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
@@ -237,6 +243,9 @@ class System:
     def set_params(self, params):
         self.params = params
         self._check(lib().am_set_params(self.h, C.byref(params)))
+
+    def set_residual_target(self, target, check_every=10):
+        self._check(lib().am_set_residual_target(self.h, target, check_every))
 
     def num_contacts(self):
         n = C.c_int32()

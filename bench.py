@@ -8,12 +8,14 @@ A step is one RigidBodySystem.advanceTime of every scene of the workload:
 collision detection, contact setup, warm start, the projected Gauss-Seidel
 solve, integration and sleeping.  The default workload is the batched one
 (512 independent bins, FP32 solve, each scene iterated until its relative LCP
-residual <= 1e-6 or the iteration cap); `value` is simulated scene-steps per
+residual <= 1e-6, cap 5000 sweeps); `value` is simulated scene-steps per
 second with the state resident in HBM (device time of K steps measured with
 CUDA events on the library's stream); `e2e` runs the same steps through the C
 ABI with the body state pushed from and read back into pinned host buffers
-every step.  `--impl reference` times the CPU restatement of the reference
-path (the oracle) on the same workload.  Scenes are independent, so several
+every step.  `plain_gpu_pgs` times the FP64 drop-in stepping a sample of the
+same scenes one at a time to the same residual.  `--impl reference` times the
+CPU restatement of the reference path (the oracle) on the same workload, over
+all host cores.  Scenes are independent, so several
 GPUs each run their own batch ("weak" scaling, no collective): value = all
 ranks' scene-steps / max time.
 """
@@ -39,6 +41,10 @@ FP64_BYTES_PER_CONTACT_SWEEP = 736   # J 288 + b,D 48 + lambda r/w 48 + dv of 2 
 FP32_BYTES_PER_CONTACT_SWEEP = 368   # the same quantities in FP32
 BATCH_SCENES = 512
 BATCH_SAMPLE_STRIDE = 16             # CPU baseline: every 16th scene, scaled by 16
+REFERENCE_SAMPLE_STRIDE = 4          # reference arm: every 4th scene, all host cores
+PLAIN_SAMPLE_STRIDE = 32             # plain GPU PGS arm: every 32nd scene, one scene at a time
+SWEEP_CAP = 5000                     # sweep cap of the residual-targeted solves
+RESIDUAL_TARGET = 1e-6
 
 
 def workload(name):
@@ -46,12 +52,13 @@ def workload(name):
     if name == "batch":
         sc = scenes.batch_scenes(BATCH_SCENES, seed=3)
         P = abi.default_params(gravity_amount=9.81, friction_override=0, restitution_override=1,
-                               restitution=0.0, iterations=500, enable_merging=0)
+                               restitution=0.0, iterations=SWEEP_CAP, enable_merging=0)
         return sc, P, 0.005, {
             "workload": "512 independent bins, body counts log-uniform 20..2000, boxes U(0.1,1.0) m and "
                         "spheres U(0.05,0.5) m, density U(500,2000), per-scene mu U(0.3,0.8), 4 pinned walls + plane",
             "scenes": BATCH_SCENES, "bodies": int(sum(x.n for x in sc)), "dt": 0.005,
-            "pgs": "FP32, one CTA per scene, stop at relative residual <= 1e-6 (checked every 10 sweeps), cap 500",
+            "pgs": f"FP32, one CTA per scene, previous-frame warm start, each scene swept until its relative "
+                   f"LCP residual <= {RESIDUAL_TARGET:g} (checked every 10 sweeps, cap {SWEEP_CAP})",
             "merging": "off", "precision": "fp32 solve, fp64 collision/contact setup/integration"}
     if name in ("wall", "wall_nomerge"):
         merging = name == "wall"
@@ -162,25 +169,39 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def oracle_batch_sample(sc_list, P, dt, warmup, steps):
-    """Oracle on every BATCH_SAMPLE_STRIDE-th scene from the initial state:
-    `warmup` untimed steps, then `steps` timed steps.  Returns scene-steps/s
-    of the full batch estimated from the sample (the scenes are i.i.d.)."""
+def _oracle_scene_time(job):
+    """One scene on the oracle: `warmup` untimed steps, then the seconds of
+    `steps` timed steps (runs in a worker process)."""
+    scene, P, dt, warmup, steps = job
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_binding import Oracle
+    o = Oracle(scene, P)
+    o.step(dt, warmup)
+    t0 = time.perf_counter()
+    o.step(dt, steps)
+    return time.perf_counter() - t0
+
+
+def oracle_batch_sample(sc_list, P, dt, warmup, steps, stride=BATCH_SAMPLE_STRIDE, workers=1):
+    """Oracle on every `stride`-th scene from the initial state: `warmup`
+    untimed steps, then `steps` timed steps, the scenes spread over `workers`
+    processes.  Returns scene-steps/s of `workers` cores (sum of the scenes'
+    timed steps / sum of their timed seconds x workers)."""
     P.solver_order = abi.AM_ORDER_REFERENCE
     P.iterations = 100            # the reference algorithm: 100 PGS iterations, early exit on tolerance
-    sample = sc_list[::BATCH_SAMPLE_STRIDE]
-    t = 0.0
-    for s in sample:
-        o = Oracle(s, P)
-        o.step(dt, warmup)
-        t0 = time.perf_counter()
-        o.step(dt, steps)
-        t += time.perf_counter() - t0
-    return steps * len(sample) / t, (f"{len(sample)} of {len(sc_list)} scenes (every {BATCH_SAMPLE_STRIDE}th), "
-                                     f"{steps} timed steps after {warmup} from the initial state, "
-                                     f"{t:.1f} s single thread; reference algorithm (100 iterations, early exit)")
+    sample = sc_list[::stride]
+    jobs = [(s, P, dt, warmup, steps) for s in sample]
+    if workers > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(workers) as pool:
+            ts = pool.map(_oracle_scene_time, jobs, chunksize=1)
+    else:
+        ts = [_oracle_scene_time(j) for j in jobs]
+    t = sum(ts)
+    return workers * steps * len(sample) / t, (
+        f"{len(sample)} of {len(sc_list)} scenes (every {stride}th), {steps} timed steps after {warmup} from the "
+        f"initial state, {t:.1f} s of scene time on {workers} concurrent worker process(es); reference algorithm "
+        f"(100 iterations, early exit on max |delta lambda| < 1e-5)")
 
 
 def cpu_baseline(name, max_seconds=15.0, max_steps=400, warmup=20, steps=10):
@@ -215,8 +236,11 @@ def run_reference(args):
     from oracle_binding import Oracle
     P.solver_order = abi.AM_ORDER_REFERENCE
     unit = "steps/s"
+    cores = 1
     if args.workload == "batch":
-        v, desc = oracle_batch_sample(sc, P, dt, args.warmup, args.steps)
+        cores = max(1, len(os.sched_getaffinity(0)))
+        v, desc = oracle_batch_sample(sc, P, dt, args.warmup, args.steps, stride=REFERENCE_SAMPLE_STRIDE,
+                                      workers=cores)
         el = args.steps * BATCH_SCENES / v
         unit = "scene-steps/s"
     else:
@@ -231,9 +255,90 @@ def run_reference(args):
            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
            "config": cfg,
-           "cpu_baseline": {"value": v, "unit": unit, "cores": 1, "kind": "port", "sample": desc},
+           "cpu_baseline": {"value": v, "unit": unit, "cores": cores, "kind": "port", "sample": desc},
            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
+
+
+def plain_gpu_pgs(sc_list, dt, warmup, steps, flush):
+    """The plain GPU PGS: the FP64 drop-in, one scene per context and launch
+    sequence (coloured full solve, stop at the same relative residual), on
+    every PLAIN_SAMPLE_STRIDE-th scene.  CUDA-event time per scene-step."""
+    import torch
+    from adaptivemerging_gb300 import native
+    P = abi.default_params(gravity_amount=9.81, friction_override=0, restitution_override=1, restitution=0.0,
+                           iterations=SWEEP_CAP, tolerance=0.0, enable_merging=0,
+                           solver_order=abi.AM_ORDER_COLOURED)
+    sample = sc_list[::PLAIN_SAMPLE_STRIDE]
+    tot_ms, n, conv, sweeps = 0.0, 0, 0, []
+    for s in sample:
+        g = native.System(s, P)
+        g.set_residual_target(RESIDUAL_TARGET, 10)
+        stream = torch.cuda.ExternalStream(g.stream_handle())
+        for _ in range(warmup):
+            g.step(dt)
+        for _ in range(steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.step(dt)
+            e1.record(stream)
+            e1.synchronize()
+            tot_ms += e0.elapsed_time(e1)
+            st = g.stats()
+            conv += int(st.residual_rel <= RESIDUAL_TARGET)
+            sweeps.append(st.sweeps)
+            n += 1
+        g.close()
+    return {"value": 1e3 * n / tot_ms, "unit": "scene-steps/s",
+            "sample": f"{len(sample)} of {len(sc_list)} scenes (every {PLAIN_SAMPLE_STRIDE}th) stepped one at a "
+                      f"time, {steps} timed steps each after {warmup}, FP64 coloured PGS to relative residual <= "
+                      f"{RESIDUAL_TARGET:g} (cap {SWEEP_CAP})",
+            "frac_scene_steps_residual_le_1e-6": conv / max(1, n), "pgs_sweeps_mean": float(np.mean(sweeps))}
+
+
+def learned_protocol(sc_list, P, dt, collect_steps=100, compare_steps=30, stride=4):
+    """Learned warm start against the plain previous-frame start: two copies
+    of every `stride`-th scene step in lockstep; the first records (features,
+    converged impulse) pairs and trains the network on the device, the
+    second then takes the learned start.  Contact-sweeps of the two over the
+    next `compare_steps` steps, same residual target."""
+    from adaptivemerging_gb300 import native
+    sample = sc_list[::stride]
+    a = native.BatchSystem(sample, P, threads=0, residual_target=RESIDUAL_TARGET, check_every=10)
+    b = native.BatchSystem(sample, P, threads=0, residual_target=RESIDUAL_TARGET, check_every=10)
+    a.learned_collect(True, 2_000_000)
+    for _ in range(collect_steps):
+        a.step(dt)
+        b.step(dt)
+    n = a.learned_info()["n_samples"]
+    t0 = time.perf_counter()
+    loss = a.learned_train(epochs=1, batch=min(4096, max(64, n // 8)), lr=1e-3, normalise=True)
+    loss = a.learned_train(epochs=20, batch=min(4096, max(64, n // 8)), lr=1e-3, normalise=False)
+    train_s = time.perf_counter() - t0
+    w, nm = a.learned_weights()
+    b.learned_weights(set_w=w, set_norm=nm)
+    b.learned_use(1)
+    a.learned_collect(False)
+    cs = [0, 0]
+    conv = [0, 0]
+    falls = 0
+    for _ in range(compare_steps):
+        for k, g in enumerate((a, b)):
+            g.step(dt)
+            st = g.batch_stats()
+            cs[k] += st.contact_sweeps
+            conv[k] += st.converged
+        falls += b.learned_info()["fallback_scenes"]
+    return {"scenes": len(sample), "samples": n, "train_seconds": train_s, "train_loss": loss,
+            "contact_sweeps_plain": cs[0], "contact_sweeps_learned": cs[1],
+            "sweeps_saved_frac": 1.0 - cs[1] / max(1, cs[0]),
+            "converged_scene_steps_plain": conv[0], "converged_scene_steps_learned": conv[1],
+            "fallback_scene_steps": falls, "scene_steps": compare_steps * len(sample),
+            "protocol": f"{collect_steps} recording steps, 21 epochs of Adam on the device, then {compare_steps} "
+                        f"steps in lockstep; learned start for fresh contacts, BF16 tensor-core inference"}
 
 
 def run_ours(args):
@@ -346,6 +451,13 @@ def run_ours(args):
                         "bytes_per_contact_sweep": bpcs,
                         "pgs_ms_per_launch": pgs_ms / pgs_l if pgs_l else None},
            "clocks": clk}
+    if batch and not args.no_plain:
+        sysm.close()
+        pl = plain_gpu_pgs(sc, dt, args.warmup, min(args.steps, 10), flush)
+        pl["batched_over_plain"] = value / pl["value"]
+        out["plain_gpu_pgs"] = pl
+    if batch and args.learned:
+        out["learned_warm_start"] = learned_protocol(sc, P, dt)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.workload, warmup=args.warmup, steps=min(args.steps, 10))
     print(json.dumps(out))
@@ -359,6 +471,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain GPU PGS comparison arm")
+    ap.add_argument("--learned", action="store_true", help="also run the learned warm-start protocol")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -242,8 +242,14 @@ int32_t am_set_batch(void* ctx, const am_scene* scenes, int32_t n_scenes);
 /* threads: 0 = autotune on the first step; residual_target <= 0 disables the test */
 int32_t am_set_batch_options(void* ctx, int32_t threads, double residual_target, int32_t check_every);
 int32_t am_get_batch_stats(void* ctx, am_batch_stats* out);
-/* per-scene figures of the last step (arrays of n_scenes; NULL skips one) */
-int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, int32_t* fell_back);
+/* coloured full solve of a single scene (AM_ORDER_COLOURED): stop once the
+ * relative natural-map residual is <= residual_target, tested every
+ * check_every sweeps (0 disables; the reference's max-change tolerance still
+ * applies).  No reference counterpart: PGS.java stops on max |delta lambda| only. */
+int32_t am_set_residual_target(void* ctx, double residual_target, int32_t check_every);
+/* per-scene figures of the last step (arrays of n_scenes; NULL skips one):
+ * sweeps, relative residual, learned start fell back, colours of the contact groups */
+int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, int32_t* fell_back, int32_t* colours);
 
 /*
  * Learned warm start for the batched solve (no reference counterpart).  An
@@ -260,6 +266,8 @@ int32_t am_learned_collect(void* ctx, int32_t enable, int32_t capacity);
 int32_t am_learned_train(void* ctx, int32_t epochs, int32_t batch, double lr, int32_t normalise, double* last_loss);
 /* 0: plain warm start; 1: learned start, BF16 tensor-core inference; 2: learned start, FP32 inference */
 int32_t am_learned_use(void* ctx, int32_t mode);
+/* which contacts are recorded and take the learned start: 0 fresh contacts (default), 1 all contacts */
+int32_t am_learned_scope(void* ctx, int32_t scope);
 /* get / set the FP32 parameters (n_params floats) and the feature scaling (48 floats); NULL skips */
 int32_t am_learned_weights(void* ctx, float* get, const float* set, float* norm_get, const float* norm_set);
 /* n_params, recorded samples, scenes that fell back to the plain start in the last step */

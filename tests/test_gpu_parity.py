@@ -114,3 +114,29 @@ def test_coloured_converged(gpu_lib, name):
     print(f"{name}: contacts {lo.shape[0]} rel err {err:.2e} sweeps {st.sweeps} residual_rel {st.residual_rel:.2e}")
     assert err <= 1e-6, err
     assert st.residual_rel <= 1e-6
+
+
+def test_coloured_residual_target_stops_at_target(gpu_lib):
+    """am_set_residual_target: the coloured FP64 solve stops as soon as the
+    relative natural-map residual is <= the target (the reference's
+    max-change tolerance switched off), well before the sweep cap, and the
+    multipliers agree with the oracle run to a fixed point."""
+    from adaptivemerging_gb300 import native
+    sc = SCENES["pile_box_sphere"]()
+    P = params(iterations=100)
+    g = native.System(sc, P)
+    o = Oracle(sc, P)
+    g.step(DT, 90)
+    o.step(DT, 90)
+    g.set_params(params(iterations=60000, tolerance=0.0, solver_order=abi.AM_ORDER_COLOURED))
+    g.set_residual_target(1e-7, 10)
+    o.set_params(params(iterations=60000, tolerance=1e-13))
+    g.step(DT)
+    o.step(DT)
+    st = g.stats()
+    lg, lo = g.contacts()["lambda"], o.contacts()["lambda"]
+    assert lg.shape == lo.shape and lo.size > 0
+    err = float(np.abs(lg - lo).max()) / max(1.0, float(np.abs(lo).max()))
+    print(f"residual target 1e-7: sweeps {st.sweeps} residual_rel {st.residual_rel:.2e} rel err {err:.2e}")
+    assert st.residual_rel <= 1e-7 and st.sweeps % 10 == 0 and st.sweeps < 60000
+    assert err <= 1e-5
