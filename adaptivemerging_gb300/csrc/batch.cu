@@ -1,26 +1,32 @@
-// batch.cu -- many independent scenes solved by one persistent launch.
+// batch.cu -- many independent scenes solved by one launch.
 //
 // The scenes' bodies are concatenated (scene s owns body slots
 // [sceneBodyOff[s], sceneBodyOff[s+1])); the collision pipeline runs on the
 // whole batch with the broad phase restricted to pairs inside one scene, so
 // every scene's contacts and body-pair groups are contiguous runs.  The solve
 // then runs one CTA per scene:
-//   * the scene's body delta-v lives in shared memory (FP32) for the whole
-//     solve, so no delta-v traffic reaches HBM;
-//   * the scene's body-pair groups are coloured inside the CTA (independent
-//     set rounds over scene-local body indices);
+//   * the scene's body-pair groups are coloured inside the CTA (first-fit
+//     Jones-Plassmann over scene-local bodies; 3-4 colours for a bin);
 //   * every contact is packed into a 64-float record (J, jinv J.w for both
-//     bodies, b, D, 1/(D + c), mu, local body ids) read with 128-bit loads;
-//   * each sweep walks the colours with __syncthreads between them; every
-//     `check` sweeps the CTA evaluates the natural-map residual of its scene
-//     and stops when it is below the target (or at the iteration cap);
+//     bodies, b, D, 1/(D + c), mu), stored in colour order ("slots"), so a
+//     colour's records form one contiguous run;
+//   * the scene's delta-v lives in shared memory (FP32) for the whole solve;
+//     the records and multipliers of a scene that fits the staging buffer
+//     are loaded into shared memory once and stay there; a larger scene is
+//     walked in chunks (whole groups of one colour) that all threads copy
+//     into shared memory with coalesced 128-bit loads before processing;
+//   * a thread owns one group (body pair) at a time and keeps the two
+//     bodies' delta-v in registers across the group's contacts;
+//   * every `check` sweeps the CTA evaluates the natural-map residual of its
+//     scene and stops when it is below the target (or at the sweep cap);
 //   * multipliers go back to the FP64 contact arrays and delta-v to the FP64
 //     body arrays for integration.
 // This is the FP32 path of the batched workload (the single-scene drop-in
-// stays FP64); threads per CTA are chosen by the autotuner in Ctx.
+// stays FP64).  CTA size and staging capacity are chosen by the autotuner.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <numeric>
 #include <vector>
 
 #include "am_ctx.hpp"
@@ -30,15 +36,17 @@
 namespace am {
 using namespace amd;
 
-static const int REC = 64;      // floats per packed contact record
+static const int REC = 64;      // floats per packed contact record (global)
+static const int RECS = 68;     // shared-memory stride of a staged record (pads banks)
 static const int MAXCB = 64;    // colours per scene
+static const int MAXCH = 1024;  // staging chunks per scene
 
 // Packed record (floats): row r = 0..2 occupies [20r, 20r + 20):
 //   [20r .. 20r+11] J (a.v, a.w, b.v, b.w), [20r+12 .. 20r+14] jinv_a a.w,
 //   [20r+15 .. 20r+17] jinv_b b.w, [20r+18] b, [20r+19] 1/(D + c);
-// [60 .. 62] D of the three rows, [63] mu.  Scene-local body ids live in a
-// separate int2 array, the multipliers in a separate float array (the only
-// per-sweep writes).
+// [60 .. 62] D of the three rows, [63] mu.  The multipliers live in a
+// separate array in the same slot order, 4 floats per slot (the fourth is
+// padding, so a slot is one 16-byte copy); they are the only per-sweep writes.
 
 __global__ void k_scene_ranges(const DPairs P, int npairs, const int* sceneOf, int nScenes, int* pairOff) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -48,11 +56,12 @@ __global__ void k_scene_ranges(const DPairs P, int npairs, const int* sceneOf, i
     for (int s = sq + 1; s <= sp; s++) pairOff[s] = p;
 }
 
-__global__ void k_batch_pack(DBodies B, DContacts C, int nc, const int* sceneOf, const int* sceneBodyOff,
-                             double comp, int fo, double fv, float* rec, int2* lid, float* lamf) {
+__global__ void k_batch_pack(DBodies B, DContacts C, int nc, const int* slotOf, double comp, int fo, double fv,
+                             float* rec, float* lamf) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
     int cap = C.cap;
+    int sl = slotOf[c];
     float r[REC];
     for (int q = 0; q < 3; q++) {
         for (int k = 0; k < 12; k++) r[20 * q + k] = (float)C.J[(12 * q + k) * cap + c];
@@ -64,8 +73,9 @@ __global__ void k_batch_pack(DBodies B, DContacts C, int nc, const int* sceneOf,
         r[20 * q + 18] = (float)C.bD[q * cap + c];
         r[20 * q + 19] = (float)(1.0 / (D + comp));
         r[60 + q] = (float)D;
-        lamf[3 * c + q] = (float)C.lam[q * cap + c];
+        lamf[4 * sl + q] = (float)C.lam[q * cap + c];
     }
+    lamf[4 * sl + 3] = 0.f;
     double mu;
     if (fo) mu = fv;
     else {
@@ -75,11 +85,8 @@ __global__ void k_batch_pack(DBodies B, DContacts C, int nc, const int* sceneOf,
         else mu = (f1 + f2) / 2.;
     }
     r[63] = (float)mu;
-    float4* dst = reinterpret_cast<float4*>(rec + (size_t)REC * c);
+    float4* dst = reinterpret_cast<float4*>(rec + (size_t)REC * sl);
     for (int k = 0; k < REC / 4; k++) dst[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
-    int s1 = C.sb1[c], s2 = C.sb2[c];
-    int base = sceneBodyOff[sceneOf[s1]];
-    lid[c] = make_int2(s1 - base, s2 - base);
 }
 
 // Colour the groups (body pairs) of one scene, one CTA per scene:
@@ -163,8 +170,98 @@ __global__ void k_batch_colour(DBodies B, DContacts C, DPairs P, const int* pair
     }
 }
 
+__device__ __forceinline__ int scene_colours(const int* co) {
+    int n = 0;
+    while (n < MAXCB && co[n + 1] > co[n]) n++;
+    return n;
+}
+
+// Slots of one scene (one CTA per scene): the groups in colour order get
+// consecutive slot runs (an exclusive scan of their contact counts); the
+// scene is cut into chunks of whole groups of one colour whose records fit
+// `cap` slots.  A chunk head entry carries bit 30 when it starts a colour.
+__global__ void k_batch_slots(DContacts C, DPairs P, const int* pairOff, const int* gOrder, const int* colOff,
+                              const int* sceneBodyOff, int nc, int npairs, int cap, int2* gInfo, int2* glid,
+                              int* slotOf, int* contactOf, int* chunkK, int* nChunks, DCount* dc) {
+    __shared__ int s_carry, s_maxcnt, s_warp[32], s_colch[MAXCB + 1];
+    const unsigned FULL = 0xffffffffu;
+    int s = blockIdx.x, t = threadIdx.x, T = blockDim.x;
+    int lane = t & 31, w = t >> 5, nw = T >> 5;
+    int g0 = pairOff[s];
+    const int* co = colOff + s * (MAXCB + 1);
+    int ncol = scene_colours(co);
+    int kEnd = co[ncol];
+    int slot0 = g0 < npairs ? P.off[g0] : nc;
+    int b0 = sceneBodyOff[s];
+    if (t == 0) { s_carry = 0; s_maxcnt = 0; }
+    __syncthreads();
+    for (int base = g0; base < kEnd; base += T) {
+        int k = base + t;
+        int cnt = 0, g = 0;
+        if (k < kEnd) { g = gOrder[k]; cnt = P.count[g]; }
+        int x = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(FULL, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_warp[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int v = lane < nw ? s_warp[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(FULL, v, o);
+                if (lane >= o) v += y;
+            }
+            if (lane < nw) s_warp[lane] = v;
+        }
+        __syncthreads();
+        int excl = s_carry + (w ? s_warp[w - 1] : 0) + x - cnt;
+        if (k < kEnd) {
+            int sl = slot0 + excl;
+            int c0 = P.off[g];
+            gInfo[k] = make_int2(sl, cnt);
+            glid[k] = make_int2(C.sb1[c0] - b0, C.sb2[c0] - b0);
+            for (int j = 0; j < cnt; j++) { slotOf[c0 + j] = sl + j; contactOf[sl + j] = c0 + j; }
+            atomicMax(&s_maxcnt, cnt);
+        }
+        __syncthreads();
+        if (t == 0) s_carry += s_warp[nw - 1];
+        __syncthreads();
+    }
+    int maxc = s_maxcnt;
+    int win = cap - maxc;
+    if (win < maxc || win <= 0) {   // a group larger than half the staging buffer
+        if (t == 0) { dc->error = AM_E_CAPACITY; nChunks[s] = 0; }
+        return;
+    }
+    for (int col = t; col < ncol; col += T) {
+        int st = gInfo[co[col]].x;
+        s_colch[col] = (gInfo[co[col + 1] - 1].x - st) / win + 1;
+    }
+    __syncthreads();
+    if (t == 0) {
+        int run = 0;
+        for (int col = 0; col < ncol; col++) { int n = s_colch[col]; s_colch[col] = run; run += n; }
+        s_colch[ncol] = run;
+        if (run > MAXCH) { dc->error = AM_E_CAPACITY; run = 0; }
+        nChunks[s] = run;
+        chunkK[s * (MAXCH + 1) + run] = kEnd | (1 << 30);
+    }
+    __syncthreads();
+    if (s_colch[ncol] > MAXCH) return;
+    for (int k = g0 + t; k < kEnd; k += T) {
+        int col = 0;
+        while (co[col + 1] <= k) col++;
+        int st = gInfo[co[col]].x;
+        int j = (gInfo[k].x - st) / win;
+        bool chead = k == co[col];
+        if (chead || (gInfo[k - 1].x - st) / win != j)
+            chunkK[s * (MAXCH + 1) + s_colch[col] + j] = k | (chead ? (1 << 30) : 0);
+    }
+}
+
 __device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
-__device__ __forceinline__ void prefetch_l1(const float* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ float4 sld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 
 // J . dv of one row over the group's two bodies (record layout: a.v a.w b.v b.w
 // in j0..j2), as two independent half sums
@@ -183,149 +280,262 @@ __device__ __forceinline__ void group_update(float* a, float* b, float la, float
     b[3] += d * i0.w; b[4] += d * i1.x; b[5] += d * i1.y;
 }
 
-// one CTA per scene; dynamic smem: dv[6 * maxBodies] + minv[maxBodies]
-__global__ void k_batch_sweep(DBodies B, DContacts C, DPairs P, const int* pairOff, const int* sceneBodyOff,
-                              const int* gOrder, const int* colOff, const float* rec, const int2* lid, float* lamf,
-                              int iters, float omega, float comp, float tolRel, int check, float slide,
-                              int* sceneSweeps, float* sceneRes, DCount* dc, const float* lamAlt, int* sceneFall) {
+// shared-memory layout of the sweep kernel (floats).  The staging arrays
+// hold two buffers of `cap` slots each (double buffering of chunks); a
+// resident scene uses both as one buffer of 2 cap slots.
+struct SweepSmem {
+    int dv, mv, rec, lam, gi, gl, total;
+    __host__ __device__ SweepSmem(int nbMax, int cap) {
+        dv = 0;
+        mv = 6 * nbMax;
+        rec = (7 * nbMax + 3) & ~3;
+        lam = rec + 2 * cap * RECS;
+        gi = lam + 8 * cap;
+        gl = gi + 4 * cap;
+        total = gl + 4 * cap;
+    }
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+enum { OP_WARM = 0, OP_SWEEP = 1, OP_RES = 2, OP_FINAL = 3 };
+
+__global__ void __launch_bounds__(512) k_batch_sweep(
+    DBodies B, DContacts C, const int* sceneBodyOff, const int* sceneOrder, const int2* gInfo, const int2* glid,
+    const int* chunkK, const int* nChunks, const int* contactOf, const float* __restrict__ rec, float* lamS, int cap,
+    int nbMax, int iters, float omega, float comp, float tolRel, int check, float slide, int* sceneSweeps,
+    float* sceneRes, const float* lamAlt, int* sceneFall, int writeBack) {
     extern __shared__ float sm[];
-    int s = blockIdx.x;
-    int b0 = sceneBodyOff[s], nb = sceneBodyOff[s + 1] - b0;
-    float* dv = sm;                 // [6 nb]
-    float* mv = sm + 6 * nb;        // [nb]
+    const SweepSmem L(nbMax, cap);
+    float* dv = sm + L.dv;
+    float* mv = sm + L.mv;
+    float* srec = sm + L.rec;
+    float* slam = sm + L.lam;
+    int2* sgi = reinterpret_cast<int2*>(sm + L.gi);
+    int2* sgl = reinterpret_cast<int2*>(sm + L.gl);
     __shared__ float s_res, s_lam;
     __shared__ int s_stop;
-    int t = threadIdx.x, T = blockDim.x;
+    const int s = sceneOrder ? sceneOrder[blockIdx.x] : blockIdx.x;
+    const int t = threadIdx.x, T = blockDim.x;
+    const int b0 = sceneBodyOff[s], nb = sceneBodyOff[s + 1] - b0;
+    const int* ck = chunkK + s * (MAXCH + 1);
+    const int nch = nChunks[s];
+    const int HEAD = 1 << 30, KMASK = HEAD - 1;
     // pinned bodies get 0 here, the same test the colouring uses to let groups
-    // of one colour share them
-    for (int b = t; b < nb; b += T) mv[b] = (B.flags[b0 + b] & F_PINNED) ? 0.f : (float)B.minv[b0 + b];
-    const int* co = colOff + s * (MAXCB + 1);
-    int ncol = 0;
-    while (ncol < MAXCB && co[ncol + 1] > co[ncol]) ncol++;
+    // of one colour share them; their delta-v is never written
+    for (int b = t; b < nb; b += T) {
+        mv[b] = (B.flags[b0 + b] & F_PINNED) ? 0.f : (float)B.minv[b0 + b];
+        for (int k = 0; k < 6; k++) dv[6 * b + k] = 0.f;
+    }
+    if (nch == 0) {
+        if (!writeBack) return;
+        __syncthreads();
+        for (int b = t; b < nb; b += T)
+            for (int k = 0; k < 6; k++) B.dv[6 * (b0 + b) + k] = 0.0;
+        if (t == 0) { sceneSweeps[s] = 0; sceneRes[s] = 0.f; if (sceneFall) sceneFall[s] = 0; }
+        return;
+    }
+    const int kS0 = ck[0] & KMASK, kS1 = ck[nch] & KMASK;
+    const int slotS0 = gInfo[kS0].x;
+    const int2 lastG = gInfo[kS1 - 1];
+    const int nslots = lastG.x + lastG.y - slotS0;
+    const bool resident = nslots <= 2 * cap;
+
+    // issue the asynchronous copy of groups [k0, k1) (and their slots) into
+    // staging buffer `buf` (one commit group per call)
+    auto stage = [&](int buf, int k0, int k1) {
+        int s0 = gInfo[k0].x;
+        int2 e = gInfo[k1 - 1];
+        int nsl = e.x + e.y - s0;
+        float* R = srec + buf * cap * RECS;
+        float* Lm = slam + buf * cap * 4;
+        for (int i = t; i < nsl * 16; i += T) {
+            int sl = i >> 4, q = i & 15;
+            cp_async16(R + sl * RECS + 4 * q, rec + (size_t)(s0 + sl) * REC + 4 * q);
+        }
+        for (int i = t; i < nsl; i += T) cp_async16(Lm + 4 * i, lamS + 4 * ((size_t)s0 + i));
+        for (int i = t; i < k1 - k0; i += T) {
+            cp_async8(sgi + buf * cap + i, gInfo + k0 + i);
+            cp_async8(sgl + buf * cap + i, glid + k0 + i);
+        }
+        cp_async_commit();
+    };
+    // multipliers of a staged chunk back to global memory
+    auto unstage = [&](int buf, int k0, int k1) {
+        int s0 = gInfo[k0].x;
+        int2 e = gInfo[k1 - 1];
+        int nsl = e.x + e.y - s0;
+        const float* Lm = slam + buf * cap * 4;
+        for (int i = t; i < nsl; i += T)
+            *reinterpret_cast<float4*>(lamS + 4 * ((size_t)s0 + i)) = *reinterpret_cast<const float4*>(Lm + 4 * i);
+    };
+
+    float rmax = 0.f, lmax = 0.f;
+    // one group: its two bodies' delta-v in registers across its contacts;
+    // sl0 is the group's first slot in the staging buffer, slA in the scene
+    auto group = [&](int op, int sl0, int slA, int cnt, int2 id) {
+        float a[6], b[6];
+        for (int q = 0; q < 6; q++) { a[q] = dv[6 * id.x + q]; b[q] = dv[6 * id.y + q]; }
+        float ma = mv[id.x], mb = mv[id.y];
+        for (int j = 0; j < cnt; j++) {
+            const float* R = srec + (sl0 + j) * RECS;
+            float* lp = slam + 4 * (sl0 + j);
+            float4 tail = sld4(R + 60);
+            float lam[3] = {lp[0], lp[1], lp[2]};
+            if (op == OP_WARM) {   // PGS.confidentWarmStart
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
+                    float4 i0 = sld4(R + 20 * q + 12), i1 = sld4(R + 20 * q + 16);
+                    group_update(a, b, ma * lam[q], mb * lam[q], lam[q], j0, j1, j2, i0, i1);
+                }
+            } else if (op == OP_SWEEP) {
+                float l0 = lam[0];
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
+                    float4 i0 = sld4(R + 20 * q + 12), i1 = sld4(R + 20 * q + 16);
+                    float jd = group_jdv(a, b, j0, j1, j2);
+                    float D = q == 0 ? tail.x : (q == 1 ? tail.y : tail.z);
+                    float nl = (D * lam[q] - omega * (i1.z + jd)) * i1.w;
+                    if (q == 0) nl = fmaxf(nl, 0.f);
+                    else { float lim = tail.w * l0; nl = fminf(fmaxf(nl, -lim), lim); }
+                    float d = nl - lam[q];
+                    if (q == 0) l0 = nl;
+                    lam[q] = nl;
+                    group_update(a, b, ma * d, mb * d, d, j0, j1, j2, i0, i1);
+                }
+                lp[0] = lam[0]; lp[1] = lam[1]; lp[2] = lam[2];
+            } else if (op == OP_RES) {
+                // natural-map residual at the current state
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
+                    float4 i1 = sld4(R + 20 * q + 16);
+                    float w = i1.z + group_jdv(a, b, j0, j1, j2) + comp * lam[q];
+                    float z = lam[q] - w * i1.w;
+                    if (q == 0) z = fmaxf(z, 0.f);
+                    else { float lim = tail.w * lam[0]; z = fminf(fmaxf(z, -lim), lim); }
+                    rmax = fmaxf(rmax, fabsf(lam[q] - z));
+                    lmax = fmaxf(lmax, fabsf(lam[q]));
+                }
+            } else {
+                // contact state after the final sweep (Contact.updateContactState)
+                float wt[2];
+#pragma unroll
+                for (int q = 1; q < 3; q++) {
+                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
+                    float4 i1 = sld4(R + 20 * q + 16);
+                    wt[q - 1] = i1.z + group_jdv(a, b, j0, j1, j2);
+                }
+                int c = contactOf[slA + j];
+                int st;
+                if (fabsf(lam[0]) <= 1e-14f) st = AM_STATE_BROKEN;
+                else if (fabsf(wt[0]) > slide || fabsf(wt[1]) > slide) st = AM_STATE_ONEDGE;
+                else st = AM_STATE_CLEAR;
+                C.state[c] = st;
+                for (int q = 0; q < 3; q++) C.lam[q * C.cap + c] = (double)lam[q];
+            }
+        }
+        if (op == OP_WARM || op == OP_SWEEP) {
+            if (ma != 0.f) for (int q = 0; q < 6; q++) dv[6 * id.x + q] = a[q];
+            if (mb != 0.f) for (int q = 0; q < 6; q++) dv[6 * id.y + q] = b[q];
+        }
+    };
+    // one pass of `op` over the scene, colour by colour.  Resident: the whole
+    // scene sits in the buffers and the chunks of one colour run together.
+    // Otherwise chunks stream through the two buffers: chunk i + 1 is copied
+    // in while chunk i is processed, and (sweeps only) a chunk's multipliers
+    // go back to global memory after it.
+    auto pass = [&](int op) {
+        if (resident) {
+            int i = 0;
+            while (i < nch) {
+                int k0 = ck[i] & KMASK;
+                int i2 = i + 1;
+                while (i2 < nch && !(ck[i2] & HEAD)) i2++;
+                int k1 = ck[i2] & KMASK;
+                for (int k = k0 + t; k < k1; k += T) {
+                    int2 gi = sgi[k - kS0];
+                    group(op, gi.x - slotS0, gi.x, gi.y, sgl[k - kS0]);
+                }
+                __syncthreads();
+                i = i2;
+            }
+            return;
+        }
+        stage(0, ck[0] & KMASK, ck[1] & KMASK);
+        for (int i = 0; i < nch; i++) {
+            int buf = i & 1;
+            int k0 = ck[i] & KMASK, k1 = ck[i + 1] & KMASK;
+            if (i + 1 < nch) {
+                stage(buf ^ 1, k1, ck[i + 2] & KMASK);
+                cp_async_wait_one();
+            } else {
+                cp_async_wait_all();
+            }
+            __syncthreads();
+            const int2* gi0 = sgi + buf * cap;
+            const int2* gl0 = sgl + buf * cap;
+            int ss = gi0[0].x;
+            for (int k = k0 + t; k < k1; k += T) {
+                int2 gi = gi0[k - k0];
+                group(op, buf * cap + gi.x - ss, gi.x, gi.y, gl0[k - k0]);
+            }
+            __syncthreads();
+            if (op == OP_SWEEP) {
+                unstage(buf, k0, k1);
+                __syncthreads();
+            }
+        }
+    };
+
+    if (resident) {
+        stage(0, kS0, kS1);
+        cp_async_wait_all();
+    }
+    __syncthreads();
     int total = 0;
     float res = 0.f;
-    // attempt 0 starts from lamf; with lamAlt given, a scene that misses the
+    // attempt 0 starts from lamS; with lamAlt given, a scene that misses the
     // residual target starts again from lamAlt (the learned start's fallback)
     const int attempts = (lamAlt && check > 0 && tolRel > 0.f) ? 2 : 1;
     for (int attempt = 0; attempt < attempts; attempt++) {
         if (attempt == 1) {
             if (res <= tolRel) break;   // uniform: res comes from shared memory
-            for (int g = pairOff[s] + t; g < pairOff[s + 1]; g += T)
-                for (int c = P.off[g]; c < P.off[g] + P.count[g]; c++)
-                    for (int q = 0; q < 3; q++) lamf[3 * c + q] = lamAlt[3 * c + q];
+            if (resident)
+                for (int i = t; i < nslots * 4; i += T) slam[i] = lamAlt[(size_t)slotS0 * 4 + i];
+            else
+                for (int i = t; i < nslots * 4; i += T) lamS[(size_t)slotS0 * 4 + i] = lamAlt[(size_t)slotS0 * 4 + i];
+            for (int b = t; b < nb; b += T)
+                for (int k = 0; k < 6; k++) dv[6 * b + k] = 0.f;
             if (t == 0 && sceneFall) sceneFall[s] = 1;
+            __syncthreads();
         } else if (t == 0 && sceneFall) {
             sceneFall[s] = 0;
         }
-        for (int b = t; b < nb; b += T)
-            for (int k = 0; k < 6; k++) dv[6 * b + k] = 0.f;
-        __syncthreads();
-        // confidentWarmStart.  Every contact of a group acts on the same two
-        // bodies, so their delta-v stays in registers for the whole group.
-        for (int col = 0; col < ncol; col++) {
-            for (int k = co[col] + t; k < co[col + 1]; k += T) {
-                int g = gOrder[k];
-                int c0 = P.off[g], c1 = c0 + P.count[g];
-                int2 id = lid[c0];
-                float a[6], b[6];
-                for (int q = 0; q < 6; q++) { a[q] = dv[6 * id.x + q]; b[q] = dv[6 * id.y + q]; }
-                float ma = mv[id.x], mb = mv[id.y];
-                for (int c = c0; c < c1; c++) {
-                    const float* R = rec + (size_t)REC * c;
-#pragma unroll
-                    for (int q = 0; q < 3; q++) {
-                        float l = lamf[3 * c + q];
-                        float4 j0 = ld4(R + 20 * q), j1 = ld4(R + 20 * q + 4), j2 = ld4(R + 20 * q + 8);
-                        float4 i0 = ld4(R + 20 * q + 12), i1 = ld4(R + 20 * q + 16);
-                        group_update(a, b, ma * l, mb * l, l, j0, j1, j2, i0, i1);
-                    }
-                }
-                // pinned bodies (minv = 0) never change and may be shared within a colour
-                if (ma != 0.f) for (int q = 0; q < 6; q++) dv[6 * id.x + q] = a[q];
-                if (mb != 0.f) for (int q = 0; q < 6; q++) dv[6 * id.y + q] = b[q];
-            }
-            __syncthreads();
-        }
+        pass(OP_WARM);
         int done = 0;
         for (int it = 0; it < iters; it++) {
-            bool last = (it == iters - 1);
-            for (int col = 0; col < ncol; col++) {
-                for (int k = co[col] + t; k < co[col + 1]; k += T) {
-                    int g = gOrder[k];
-                    int c0 = P.off[g], c1 = c0 + P.count[g];
-                    int2 id = lid[c0];
-                    float a[6], b[6];
-                    for (int q = 0; q < 6; q++) { a[q] = dv[6 * id.x + q]; b[q] = dv[6 * id.y + q]; }
-                    float ma = mv[id.x], mb = mv[id.y];
-                    for (int c = c0; c < c1; c++) {
-                        const float* R = rec + (size_t)REC * c;
-                        float4 tail = ld4(R + 60);
-                        float lam[3] = {lamf[3 * c], lamf[3 * c + 1], lamf[3 * c + 2]};
-                        float l0 = lam[0];
-#pragma unroll
-                        for (int q = 0; q < 3; q++) {
-                            float4 j0 = ld4(R + 20 * q), j1 = ld4(R + 20 * q + 4), j2 = ld4(R + 20 * q + 8);
-                            float4 i0 = ld4(R + 20 * q + 12), i1 = ld4(R + 20 * q + 16);
-                            float jd = group_jdv(a, b, j0, j1, j2);
-                            float D = q == 0 ? tail.x : (q == 1 ? tail.y : tail.z);
-                            float l = lam[q];
-                            float nl = (D * l - omega * (i1.z + jd)) * i1.w;
-                            if (q == 0) nl = fmaxf(nl, 0.f);
-                            else { float lim = tail.w * l0; nl = fminf(fmaxf(nl, -lim), lim); }
-                            float d = nl - l;
-                            if (q == 0) l0 = nl;
-                            lam[q] = nl;
-                            group_update(a, b, ma * d, mb * d, d, j0, j1, j2, i0, i1);
-                        }
-                        lamf[3 * c] = lam[0]; lamf[3 * c + 1] = lam[1]; lamf[3 * c + 2] = lam[2];
-                    }
-                    if (ma != 0.f) for (int q = 0; q < 6; q++) dv[6 * id.x + q] = a[q];
-                    if (mb != 0.f) for (int q = 0; q < 6; q++) dv[6 * id.y + q] = b[q];
-                }
-                // while the colour drains, pull this thread's first group of the
-                // next colour (or of colour 0 for the next sweep) into L1
-                {
-                    int nc2 = col + 1 < ncol ? col + 1 : 0;
-                    int k2 = co[nc2] + t;
-                    if (k2 < co[nc2 + 1]) {
-                        int g2 = gOrder[k2];
-                        const float* R2 = rec + (size_t)REC * P.off[g2];
-                        int lines = 2 * P.count[g2];
-                        for (int q = 0; q < lines; q++) prefetch_l1(R2 + 32 * q);
-                        prefetch_l1(lamf + 3 * P.off[g2]);
-                    }
-                }
-                __syncthreads();
-            }
+            pass(OP_SWEEP);
             done = it + 1;
             if (check > 0 && (done % check == 0 || done == iters)) {
-                // natural-map residual of the scene at the current state
                 if (t == 0) { s_res = 0.f; s_lam = 0.f; }
+                rmax = 0.f;
+                lmax = 0.f;
                 __syncthreads();
-                float rmax = 0.f, lmax = 0.f;
-                for (int g = pairOff[s] + t; g < pairOff[s + 1]; g += T)
-                    for (int c = P.off[g]; c < P.off[g] + P.count[g]; c++) {
-                        int2 id = lid[c];
-                        const float* R = rec + (size_t)REC * c;
-                        const float* da = dv + 6 * id.x;
-                        const float* db = dv + 6 * id.y;
-                        float4 tail = ld4(R + 60);
-                        float l0 = lamf[3 * c];
-                        for (int q = 0; q < 3; q++) {
-                            float4 j0 = ld4(R + 20 * q), j1 = ld4(R + 20 * q + 4), j2 = ld4(R + 20 * q + 8);
-                            float4 i1 = ld4(R + 20 * q + 16);
-                            float jd = j0.x * da[0] + j0.y * da[1] + j0.z * da[2] + j0.w * da[3] + j1.x * da[4] +
-                                       j1.y * da[5] + j1.z * db[0] + j1.w * db[1] + j2.x * db[2] + j2.y * db[3] +
-                                       j2.z * db[4] + j2.w * db[5];
-                            float l = lamf[3 * c + q];
-                            float w = i1.z + jd + comp * l;
-                            float z = l - w * i1.w;
-                            if (q == 0) z = fmaxf(z, 0.f);
-                            else { float lim = tail.w * l0; z = fminf(fmaxf(z, -lim), lim); }
-                            rmax = fmaxf(rmax, fabsf(l - z));
-                            lmax = fmaxf(lmax, fabsf(l));
-                        }
-                    }
+                pass(OP_RES);
                 atomicMax(reinterpret_cast<int*>(&s_res), __float_as_int(rmax));
                 atomicMax(reinterpret_cast<int*>(&s_lam), __float_as_int(lmax));
                 __syncthreads();
@@ -337,30 +547,8 @@ __global__ void k_batch_sweep(DBodies B, DContacts C, DPairs P, const int* pairO
         }
         total += done;
     }
-    // contact state after the final sweep (Contact.updateContactState)
-    for (int g = pairOff[s] + t; g < pairOff[s + 1]; g += T)
-        for (int c = P.off[g]; c < P.off[g] + P.count[g]; c++) {
-            int2 id = lid[c];
-            const float* R = rec + (size_t)REC * c;
-            const float* da = dv + 6 * id.x;
-            const float* db = dv + 6 * id.y;
-            float w[2];
-            for (int q = 1; q < 3; q++) {
-                float4 j0 = ld4(R + 20 * q), j1 = ld4(R + 20 * q + 4), j2 = ld4(R + 20 * q + 8);
-                float4 i1 = ld4(R + 20 * q + 16);
-                w[q - 1] = i1.z + j0.x * da[0] + j0.y * da[1] + j0.z * da[2] + j0.w * da[3] + j1.x * da[4] +
-                           j1.y * da[5] + j1.z * db[0] + j1.w * db[1] + j2.x * db[2] + j2.y * db[3] +
-                           j2.z * db[4] + j2.w * db[5];
-            }
-            int cap = C.cap;
-            float l0 = lamf[3 * c];
-            int st;
-            if (fabsf(l0) <= 1e-14f) st = AM_STATE_BROKEN;
-            else if (fabsf(w[0]) > slide || fabsf(w[1]) > slide) st = AM_STATE_ONEDGE;
-            else st = AM_STATE_CLEAR;
-            C.state[c] = st;
-            for (int q = 0; q < 3; q++) C.lam[q * cap + c] = (double)lamf[3 * c + q];
-        }
+    if (!writeBack) return;   // autotuner trial: results are discarded
+    pass(OP_FINAL);
     for (int b = t; b < nb; b += T)
         for (int k = 0; k < 6; k++) B.dv[6 * (b0 + b) + k] = (double)dv[6 * b + k];
     if (t == 0) { sceneSweeps[s] = total; sceneRes[s] = res; }
@@ -368,33 +556,64 @@ __global__ void k_batch_sweep(DBodies B, DContacts C, DPairs P, const int* pairO
 
 const void* batch_sweep_kernel() { return (const void*)k_batch_sweep; }
 
+size_t batch_sweep_smem(int nbMax, int cap) { return sizeof(float) * (size_t)SweepSmem(nbMax, cap).total; }
+
+int Ctx::batchLaunchSweep(int threads, int cap, int iters, float tol, int check, float* lamStart, const float* lamAlt,
+                          int* fall, int writeBack) {
+    double comp = P.enable_compliance ? P.compliance : 0.;
+    size_t ssm = batch_sweep_smem(maxSceneBodies, cap);
+    k_batch_sweep<<<nScenes, threads, ssm, stream>>>(
+        B, C[cur], sceneBodyOffDev, bSceneOrder, bGInfo, bLid, bChunkK, bNChunks, bContactOf, bRec, lamStart, cap,
+        maxSceneBodies, iters, (float)P.omega, (float)comp, tol, check, (float)P.sliding_threshold, bSweeps, bRes,
+        lamAlt, fall, writeBack);
+    AM_LAUNCHED(1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { err = std::string("sweep launch: ") + cudaGetErrorString(e); return AM_E_CUDA; }
+    return AM_OK;
+}
+
+// slots and chunks for staging capacity `cap`, then the packed records
+int Ctx::batchLayout(int cap) {
+    double comp = P.enable_compliance ? P.compliance : 0.;
+    int nc = nContacts;
+    k_batch_slots<<<nScenes, 256, 0, stream>>>(C[cur], PR, bPairOff, bOrder, bColOff, sceneBodyOffDev, nc, nPairs, cap,
+                                               bGInfo, bLid, bSlotOf, bContactOf, bChunkK, bNChunks, dc);
+    k_batch_pack<<<(nc + 127) / 128, 128, 0, stream>>>(B, C[cur], nc, bSlotOf, comp, P.friction_override, P.friction,
+                                                     bRec, bLam);
+    AM_LAUNCHED(2);
+    return AM_OK;
+}
+
 int Ctx::batchSolve(double dt) {
     int r;
     int nc = nContacts, np = nPairs, S = nScenes;
     if (nc <= 0) return AM_OK;
-    double comp = P.enable_compliance ? P.compliance : 0.;
     launch_solve_prep(B, C[cur], nc, dt, P.feedback_stiffness, false, P.restitution_override, P.restitution,
                       P.warm_start ? 1 : 0, stream);
     if (nc > bRecCap) {
         int cap = std::max(nc + nc / 2, 4096);
-        if (alloc(&bRec, (size_t)REC * cap) || alloc(&bLid, cap) || alloc(&bLam, 3 * (size_t)cap) ||
-            alloc(&bLamL, 3 * (size_t)cap))
+        if (alloc(&bRec, (size_t)REC * cap) || alloc(&bLam, 4 * (size_t)cap) || alloc(&bLamL, 4 * (size_t)cap) ||
+            alloc(&bSlotOf, cap) || alloc(&bContactOf, cap))
             return AM_E_CUDA;
         bRecCap = cap;
     }
     if (np > bPairCap) {
         int cap = std::max(np + np / 2, 4096);
-        if (alloc(&bColour, cap) || alloc(&bOrder, cap)) return AM_E_CUDA;
+        if (alloc(&bColour, cap) || alloc(&bOrder, cap) || alloc(&bLid, cap) || alloc(&bGInfo, cap)) return AM_E_CUDA;
         bPairCap = cap;
     }
     k_scene_ranges<<<(np + 1 + 255) / 256, 256, 0, stream>>>(PR, np, sceneOfDev, S, bPairOff);
-    k_batch_pack<<<(nc + 127) / 128, 128, 0, stream>>>(B, C[cur], nc, sceneOfDev, sceneBodyOffDev, comp,
-                                                     P.friction_override, P.friction, bRec, bLid, bLam);
     size_t csm = 2 * sizeof(unsigned long long) * (size_t)maxSceneBodies;
     k_batch_colour<<<S, 256, csm, stream>>>(B, C[cur], PR, bPairOff, sceneBodyOffDev, bColour, bOrder, bColOff,
                                             maxSceneBodies, dc);
-    size_t ssm = sizeof(float) * 7 * (size_t)maxSceneBodies;
-    int threads = batchThreads > 0 ? batchThreads : 128;
+    AM_LAUNCHED(2);
+    // tune on the first solve and again whenever the contact count has grown
+    // by half since the last tuning (piles forming change the best shape)
+    if ((batchThreads == 0 || batchCap == 0 || 2 * (long long)nc > 3 * (long long)batchTunedContacts) &&
+        (r = batchAutotune(dt)))
+        return r;
+    int threads = batchThreads, cap = batchCap;
+    if ((r = batchLayout(cap))) return r;
     if (evA) cudaEventRecord(evA, stream);
     if (lUse || lCollect) {
         if ((r = learnedFeatures(dt))) return r;
@@ -408,11 +627,8 @@ int Ctx::batchSolve(double dt) {
         lamStart = bLamL;
         lamAlt = bLam;
     }
-    k_batch_sweep<<<S, threads, ssm, stream>>>(B, C[cur], PR, bPairOff, sceneBodyOffDev, bOrder, bColOff, bRec,
-                                               bLid, lamStart, P.iterations, (float)P.omega, (float)comp,
-                                               (float)batchTol, batchCheck, (float)P.sliding_threshold,
-                                               bSweeps, bRes, dc, lamAlt, bFall);
-    AM_LAUNCHED(4);
+    if ((r = batchLaunchSweep(threads, cap, P.iterations, (float)batchTol, batchCheck, lamStart, lamAlt, bFall, 1)))
+        return r;
     if (evB) { cudaEventRecord(evB, stream); pgsPending = true; }
     if (lCollect && (r = learnedRecord())) return r;
     return AM_OK;
@@ -459,8 +675,10 @@ int Ctx::batchStats() {
     long long tot = 0;
     int mx = 0;
     float rmax = 0.f;
-    int conv = 0, fall = 0;
+    int conv = 0, fall = 0, resid = 0;
     for (int s = 0; s < nScenes; s++) {
+        long long ncs = sw[s] > 0 ? cs[s] / sw[s] : 0;
+        resid += (ncs > 0 && ncs <= 2 * batchCap) ? 1 : 0;
         tot += sw[s];
         mx = std::max(mx, sw[s]);
         rmax = std::max(rmax, rs[s]);
@@ -468,9 +686,18 @@ int Ctx::batchStats() {
         fall += fl[s];
     }
     lFallbackScenes = lUse ? fall : 0;
+    batchResident = resid;
     batchSweepsTotal = tot;
     batchContactSweepsLast = 0;
     for (long long v : cs) batchContactSweepsLast += v;
+    // launch order of the next solve: costliest scenes (contacts x sweeps of
+    // this step) first, so the long ones start in the first wave
+    std::vector<int> order(nScenes);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cs[a] > cs[b]; });
+    cudaMemcpyAsync(bSceneOrderBuf, order.data(), sizeof(int) * nScenes, cudaMemcpyHostToDevice, stream);
+    if ((r = syncErr())) return r;
+    bSceneOrder = bSceneOrderBuf;
     stats.sweeps = mx;
     stats.residual_rel = rmax;
     batchConverged = conv;
@@ -531,51 +758,75 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     cudaMemcpyAsync(sceneOfDev, sOf.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(sceneBodyOffDev, bodyOff.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(topEnd, tEnd.data(), sizeof(int) * all.n_bodies, cudaMemcpyHostToDevice, stream);
-    size_t ssm = sizeof(float) * 7 * (size_t)maxSceneBodies;
-    if (ssm > 48 * 1024) cudaFuncSetAttribute(batch_sweep_kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm);
+    if (alloc(&bChunkK, (size_t)n * (MAXCH + 1)) || alloc(&bNChunks, n) || alloc(&bSceneOrderBuf, n)) return AM_E_CUDA;
+    bSceneOrder = nullptr;
+    // dynamic shared memory the sweep may take: the opt-in limit less its static part
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, batch_sweep_kernel()) != cudaSuccess) { err = "sweep kernel attributes"; return AM_E_CUDA; }
+    batchSmemLimit = (size_t)optin > fa.sharedSizeBytes ? optin - fa.sharedSizeBytes : 0;
+    if (cudaFuncSetAttribute(batch_sweep_kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batchSmemLimit) !=
+        cudaSuccess) {
+        err = "sweep kernel shared-memory limit";
+        return AM_E_CUDA;
+    }
     size_t csm = 2 * sizeof(unsigned long long) * (size_t)maxSceneBodies;
-    if (csm > 48 * 1024)
-        cudaFuncSetAttribute((const void*)k_batch_colour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm);
+    if (csm > 48 * 1024 &&
+        cudaFuncSetAttribute((const void*)k_batch_colour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm) !=
+            cudaSuccess) {
+        err = "a scene has too many bodies for the batched colouring's shared memory";
+        return AM_E_CAPACITY;
+    }
     return syncErr();
 }
 
-// Picks the CTA size of the scene solve: every candidate runs a few sweeps
-// from the same packed state (multipliers restored between candidates) and
-// the fastest per sweep wins.
+// Picks the CTA size and staging capacity of the scene solve: every
+// candidate lays out the records for its capacity and runs a few sweeps from
+// the same packed state (multipliers restored between candidates); the
+// fastest wins.
 int Ctx::batchAutotune(double dt) {
     (void)dt;
-    const int cand[4] = {64, 128, 256, 512};
-    double comp = P.enable_compliance ? P.compliance : 0.;
+    const int fixedThreads = batchThreadsUser;   // a CTA size given by the caller is kept
+    std::vector<int> thr = fixedThreads > 0 ? std::vector<int>{fixedThreads} : std::vector<int>{128, 256, 512};
+    std::vector<int> caps;
+    for (int c : {64, 128, 192, 256})
+        if (batch_sweep_smem(maxSceneBodies, c) <= batchSmemLimit) caps.push_back(c);
+    if (caps.empty()) {
+        err = "a scene has too many bodies for the batched solve's shared memory";
+        return AM_E_CAPACITY;
+    }
     int nc = nContacts;
-    float* save = nullptr;
-    if (alloc(&save, 3 * (size_t)nc)) return AM_E_CUDA;
-    cudaMemcpyAsync(save, bLam, sizeof(float) * 3 * nc, cudaMemcpyDeviceToDevice, stream);
+    float* save = bLamL;   // the learned start is written only after tuning
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    size_t ssm = sizeof(float) * 7 * (size_t)maxSceneBodies;
     float best = 1e30f;
-    int bestT = 128;
+    int bestT = 256, bestC = caps[0];
     tuneMs.clear();
-    for (int k = 0; k < 4; k++) {
-        int T = cand[k];
-        cudaMemcpyAsync(bLam, save, sizeof(float) * 3 * nc, cudaMemcpyDeviceToDevice, stream);
-        cudaEventRecord(e0, stream);
-        k_batch_sweep<<<nScenes, T, ssm, stream>>>(B, C[cur], PR, bPairOff, sceneBodyOffDev, bOrder, bColOff, bRec,
-                                                   bLid, bLam, 8, (float)P.omega, (float)comp, 0.f, 0,
-                                                   (float)P.sliding_threshold, bSweeps, bRes, dc, nullptr, nullptr);
-        cudaEventRecord(e1, stream);
-        AM_LAUNCHED(1);
-        cudaEventSynchronize(e1);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        tuneMs.push_back(ms);
-        if (ms < best) { best = ms; bestT = T; }
+    for (int cap : caps) {
+        batchLayout(cap);
+        cudaMemcpyAsync(save, bLam, sizeof(float) * 4 * nc, cudaMemcpyDeviceToDevice, stream);
+        for (int T : thr) {
+            cudaMemcpyAsync(bLam, save, sizeof(float) * 4 * nc, cudaMemcpyDeviceToDevice, stream);
+            cudaEventRecord(e0, stream);
+            int r = batchLaunchSweep(T, cap, 8, 0.f, 0, bLam, nullptr, nullptr, 0);
+            if (r) return r;
+            cudaEventRecord(e1, stream);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            tuneMs.push_back(ms);
+            if (ms < best) { best = ms; bestT = T; bestC = cap; }
+        }
+        cudaMemcpyAsync(bLam, save, sizeof(float) * 4 * nc, cudaMemcpyDeviceToDevice, stream);
     }
-    cudaMemcpyAsync(bLam, save, sizeof(float) * 3 * nc, cudaMemcpyDeviceToDevice, stream);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     batchThreads = bestT;
+    batchCap = bestC;
+    batchTunedContacts = nc;
     return syncErr();
 }
 
@@ -587,18 +838,6 @@ int Ctx::stepBatch(double dt) {
     if ((r = warmStart())) return r;
     if ((r = wake())) return r;
     if (!evA) { cudaEventCreate(&evA); cudaEventCreate(&evB); }
-    if (batchThreads == 0 && nContacts > 0) {
-        // pack once to tune on real data, then solve with the chosen size
-        int keep = batchThreads;
-        batchThreads = 128;
-        if ((r = batchSolve(dt))) return r;
-        if ((r = syncErr())) return r;
-        pgsPending = false;
-        batchThreads = keep;
-        // restore the warm-start multipliers the solve consumed and retune
-        if ((r = batchAutotune(dt))) return r;
-        cudaMemsetAsync(B.dv, 0, sizeof(double) * 6 * host.cap, stream);
-    }
     if ((r = batchSolve(dt))) return r;
     if ((r = finishStep(dt))) return r;
     if ((r = readCounts())) return r;

@@ -177,8 +177,9 @@ int32_t am_set_batch(void* ctx, const am_scene* scenes, int32_t n) {
 int32_t am_set_batch_options(void* ctx, int32_t threads, double residual_target, int32_t check_every) {
     if (!ctx) return AM_E_ARG;
     Ctx* c = (Ctx*)ctx;
-    if (threads != 0 && (threads < 32 || threads > 1024 || threads % 32)) { c->err = "threads"; return AM_E_ARG; }
+    if (threads != 0 && (threads < 32 || threads > 512 || threads % 32)) { c->err = "threads"; return AM_E_ARG; }
     c->batchThreads = threads;
+    c->batchThreadsUser = threads;
     c->batchTol = residual_target;
     c->batchCheck = check_every < 0 ? 0 : check_every;
     return AM_OK;
@@ -191,6 +192,8 @@ int32_t am_get_batch_stats(void* ctx, am_batch_stats* o) {
     o->converged = c->batchConverged;
     o->sweeps_max = c->stats.sweeps;
     o->threads = c->batchThreads;
+    o->stage_slots = c->batchCap;
+    o->resident_scenes = c->batchResident;
     o->sweeps_sum = c->batchSweepsTotal;
     o->contact_sweeps = c->batchContactSweepsLast;
     o->residual_max = c->stats.residual_rel;

@@ -235,7 +235,17 @@ struct Ctx {
     int* topEnd = nullptr;
     int* bPairOff = nullptr;
     float* bRec = nullptr;
-    int2* bLid = nullptr;
+    int2* bLid = nullptr;        // per group (colour order): scene-local body ids
+    int2* bGInfo = nullptr;      // per group (colour order): first slot, contacts
+    int* bSlotOf = nullptr;      // contact -> slot (records are stored in colour order)
+    int* bContactOf = nullptr;   // slot -> contact
+    int* bChunkK = nullptr;      // per scene: chunk heads (group positions), MAXCH + 1 each
+    int* bNChunks = nullptr;
+    int* bSceneOrder = nullptr;  // CTA -> scene, costliest scenes first (null: identity)
+    int* bSceneOrderBuf = nullptr;
+    int batchCap = 0;            // records staged per chunk (0: autotune)
+    int batchResident = 0;       // scenes solved with all records in shared memory, last step
+    size_t batchSmemLimit = 0;   // dynamic shared memory the sweep kernel may use
     float* bLam = nullptr;
     int bRecCap = 0;
     int* bColour = nullptr;
@@ -244,7 +254,9 @@ struct Ctx {
     int* bColOff = nullptr;
     int* bSweeps = nullptr;
     float* bRes = nullptr;
-    int batchThreads = 0;        // 0: autotune on the first solve
+    int batchThreads = 0;        // threads per scene CTA in use (0: not tuned yet)
+    int batchThreadsUser = 0;    // CTA size fixed by the caller (0: autotuned)
+    int batchTunedContacts = 0;  // contacts at the last tuning
     double solveTol = 0.0;       // coloured single-scene solve: relative residual target (0: off)
     int solveCheck = 0;
     double batchTol = 1e-6;      // relative natural-map residual target
@@ -359,6 +371,9 @@ struct Ctx {
     int batchStats();
     int batchAutotune(double dt);
     int batchColours(int* out);
+    int batchLayout(int cap);
+    int batchLaunchSweep(int threads, int cap, int iters, float tol, int check, float* lamStart, const float* lamAlt,
+                         int* fall, int writeBack);
     int learnedInit();
     int ensureFeat(int nc);
     int learnedFeatures(double dt);

@@ -372,15 +372,16 @@ __global__ void k_pack_bf16(const float* W, __nv_bfloat16* Wb, float* bias) {
 }
 
 // learned start = previous-frame start + y / D, projected on the friction
-// cone, packed (3 floats per contact) as the batched solver's start.  With
+// cone, packed (4 floats per contact, slot order) as the batched solver's start.  With
 // scope 0 only fresh contacts (no previous-frame impulse) take it; the others
 // keep the plain start, already the converged impulse of the last step.
 __global__ void k_apply_prediction(DBodies B, DContacts C, int nc, const float* Yp, int fo, float fv, int all,
-                                   const float* lamPlain, float* lamL) {
+                                   const int* slotOf, const float* lamPlain, float* lamL) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
+    int sl = slotOf[c];
     if (!all && !C.fresh[c]) {
-        for (int r = 0; r < 3; r++) lamL[3 * c + r] = lamPlain[3 * c + r];
+        for (int r = 0; r < 4; r++) lamL[4 * sl + r] = lamPlain[4 * sl + r];
         return;
     }
     int cap = C.cap;
@@ -398,7 +399,8 @@ __global__ void k_apply_prediction(DBodies B, DContacts C, int nc, const float* 
     l[0] = l[0] > 0 ? l[0] : 0.0;
     double lim = mu * l[0];
     for (int r = 1; r < 3; r++) l[r] = fmin(fmax(l[r], -lim), lim);
-    for (int r = 0; r < 3; r++) lamL[3 * c + r] = (float)l[r];
+    for (int r = 0; r < 3; r++) lamL[4 * sl + r] = (float)l[r];
+    lamL[4 * sl + 3] = 0.f;
 }
 
 // ---------------------------------------------------------------------------
@@ -473,7 +475,7 @@ int Ctx::learnedPredict(bool tensorCores) {
         k_infer_f32<<<(nc + 127) / 128, 128, 0, stream>>>(lX, lNorm, lW, nc, lY);
     }
     k_apply_prediction<<<(nc + 127) / 128, 128, 0, stream>>>(B, C[cur], nc, lY, P.friction_override,
-                                                             (float)P.friction, lScope, bLam, bLamL);
+                                                             (float)P.friction, lScope, bSlotOf, bLam, bLamL);
     AM_LAUNCHED(2);
     return AM_OK;
 }

@@ -375,6 +375,17 @@ int Ctx::setScene(const am_scene& s) {
     topEnd = nullptr;
     bRecCap = bPairCap = 0;
     batchThreads = 0;
+    batchThreadsUser = 0;
+    batchTunedContacts = 0;
+    batchCap = 0;
+    bSceneOrder = nullptr;
+    // device buffers of the learned start went with release()
+    lW = lG = lM = lV = lNorm = lBias = lLoss = nullptr;
+    lWb = nullptr;
+    lX = lY = lDX = lDY = lZ1 = lZ2 = lYh = nullptr;
+    lKeep = lPos = lIdx = nullptr;
+    lFeatCap = lDcap = lDn = lTrainCap = lIdxCap = 0;
+    lCollect = lUse = 0;
     if (s.n_bodies <= 0) { err = "empty scene"; return AM_E_ARG; }
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaMalloc((void**)&dc, sizeof(DCount)));
@@ -508,6 +519,9 @@ int Ctx::uploadTopology() {
 
 int Ctx::syncErr() {
     cudaError_t e = cudaStreamSynchronize(stream);
+    // a launch refused for its configuration is not sticky and leaves the
+    // stream clean; it shows only in the last-error slot
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) { err = std::string("CUDA: ") + cudaGetErrorString(e); return AM_E_CUDA; }
     return AM_OK;
 }

@@ -435,7 +435,10 @@ def run_ours(args):
                 "timed_window": f"steps {args.warmup + 1}..{args.warmup + args.steps} from the initial state"})
     if batch:
         cfg["frac_scene_steps_residual_le_1e-6"] = float(np.mean(conv))
-        cfg["cta_threads"] = int(sysm.batch_stats().threads)
+        bst = sysm.batch_stats()
+        cfg["cta_threads"] = int(bst.threads)
+        cfg["stage_slots"] = int(bst.stage_slots)
+        cfg["resident_scenes_last_step"] = int(bst.resident_scenes)
     else:
         cfg["frac_steps_residual_le_1e-6"] = float(np.mean(np.array(res) <= 1e-6))
     unit = "scene-steps/s" if batch else "steps/s"

@@ -234,6 +234,8 @@ typedef struct am_batch_stats {
     int32_t converged;       /* scenes that reached the residual target        */
     int32_t sweeps_max;      /* largest sweep count of the last step           */
     int32_t threads;         /* threads per scene CTA (autotuned when 0 given) */
+    int32_t stage_slots;     /* contact records per shared-memory staging buffer (autotuned) */
+    int32_t resident_scenes; /* scenes whose records stayed in shared memory, last step */
     int64_t sweeps_sum;      /* sum of the scenes' sweep counts, last step     */
     int64_t contact_sweeps;  /* sum of contacts x sweeps, last step            */
     double  residual_max;    /* worst scene residual, last step                */
