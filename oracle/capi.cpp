@@ -18,6 +18,11 @@ void or_destroy(void* h) { delete (World*)h; }
 
 void or_set_params(void* h, const am_params* p) { ((World*)h)->P = *p; }
 
+void or_set_residual_target(void* h, double target, int check) {
+    ((World*)h)->resTarget = target;
+    ((World*)h)->resCheck = check;
+}
+
 void or_step(void* h, double dt) { ((World*)h)->step(dt); }
 
 void or_run(void* h, double dt, int n) {

@@ -938,8 +938,39 @@ void World::pgs(std::vector<Contact*>& list, double dt, bool inColl, int iters, 
         done++;
         change = mx;
         if (early && mx < P.tolerance) break;
+        if (!inColl && resTarget > 0 && resCheck > 0 && (done % resCheck == 0 || iter == 0) &&
+            relResidual(list, comp) <= resTarget)
+            break;
     }
     if (!inColl) { stats.sweeps = done; stats.last_change = change; }
+}
+
+// max_i |l_i - proj(l_i - w_i / (D_ii + c))| / max(1, max |l|) with
+// w = b + J dv + c l: the natural-map residual of the full solve's LCP
+double World::relResidual(std::vector<Contact*>& list, double comp) {
+    double rmax = 0, lmax = 0;
+    for (Contact* c : list) {
+        double mu;
+        if (P.friction_override) mu = P.friction;
+        else {
+            double f1 = c->body1->friction, f2 = c->body2->friction;
+            if (f1 < 0.2 || f2 < 0.2) mu = jmin(f1, f2);
+            else if (f1 > 1. || f2 > 1.) mu = jmax(f1, f2);
+            else mu = (f1 + f2) / 2.;
+        }
+        const double l[3] = {c->l0, c->l1, c->l2};
+        const double b[3] = {c->bn, c->bt1, c->bt2};
+        const double D[3] = {c->D00, c->D11, c->D22};
+        for (int i = 0; i < 3; i++) {
+            double w = b[i] + getJdv(c, false, i) + comp * l[i];
+            double z = l[i] - w / (D[i] + comp);
+            if (i == 0) z = std::max(z, 0.0);
+            else z = std::min(std::max(z, -mu * l[0]), mu * l[0]);
+            rmax = std::max(rmax, std::fabs(l[i] - z));
+            lmax = std::max(lmax, std::fabs(l[i]));
+        }
+    }
+    return rmax / std::max(1.0, lmax);
 }
 
 // CollisionProcessor.solveLCP (CollisionProcessor.java:108-137)

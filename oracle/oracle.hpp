@@ -139,6 +139,11 @@ struct Stats {
 
 struct World {
     am_params P;
+    // Stop of the full solve at a relative natural-map residual (not part of
+    // the reference, which stops on max |delta lambda| only): checked every
+    // resCheck sweeps when resTarget > 0.
+    double resTarget = 0;
+    int resCheck = 0;
     std::deque<Body> store;            // stable storage; scene bodies first
     std::vector<Body*> bodies;         // RigidBodySystem.bodies (top level)
     std::vector<Node> nodes;
@@ -193,6 +198,7 @@ struct World {
     void boxTree(int node, Body* box, Body* tree);
     void treeTree(int n1, int n2, Body* b1, Body* b2);
     void pgs(std::vector<Contact*>& list, double dt, bool inColl, int iters, double fb, double comp, bool early);
+    double relResidual(std::vector<Contact*>& list, double comp);
     void updateBPCsForContact(Contact* c);
     void removeEmptyBodyPairContacts();
     void getOrganizedContacts(std::vector<Contact*>& out);

@@ -34,6 +34,7 @@ def lib():
             getattr(L, f).argtypes = [C.c_void_p]
         L.or_step.argtypes = [C.c_void_p, C.c_double]
         L.or_set_params.argtypes = [C.c_void_p, C.POINTER(abi.am_params)]
+        L.or_set_residual_target.argtypes = [C.c_void_p, C.c_double, C.c_int]
         L.or_solve.argtypes = [C.c_void_p, C.c_double]
         L.or_run.argtypes = [C.c_void_p, C.c_double, C.c_int]
         L.or_num_contacts.argtypes = [C.c_void_p]
@@ -74,6 +75,9 @@ class Oracle:
     def set_params(self, params):
         self.params = params
         lib().or_set_params(self.h, C.byref(params))
+
+    def set_residual_target(self, target, check=10):
+        lib().or_set_residual_target(self.h, target, check)
 
     def step(self, dt, n=1):
         lib().or_run(self.h, dt, n)

@@ -159,6 +159,27 @@ def test_determinism_and_pgs_fixed_point():
     assert (np.abs(ca["lambda"][:, 1]) <= mu * ca["lambda"][:, 0] + 1e-12).all()
 
 
+def test_residual_target_stop():
+    """The oracle's residual-target stop (used for the equal-residual CPU
+    baseline) ends the solve on a check sweep once the relative natural-map
+    residual is below the target, at the same fixed point as a long solve."""
+    sc = scenes.random_pile(24, seed=5, kinds=("box", "sphere"))
+    base = params(iterations=100)
+    a, b = Oracle(sc, base), Oracle(sc, base)
+    a.step(0.005, 60)
+    b.step(0.005, 60)
+    a.set_params(params(iterations=20000, tolerance=0.0))
+    a.set_residual_target(1e-9, 10)
+    b.set_params(params(iterations=20000, tolerance=1e-15))
+    a.step(0.005)
+    b.step(0.005)
+    sw = a.counters()["sweeps"]
+    assert 0 < sw < 20000 and sw % 10 == 0
+    la, lb = a.contacts()["lambda"], b.contacts()["lambda"]
+    assert la.shape == lb.shape and la.size
+    assert np.abs(la - lb).max() <= 1e-6 * max(1.0, np.abs(lb).max())
+
+
 def _digest(o):
     c = o.contacts()
     b = o.bodies()
