@@ -61,6 +61,7 @@ struct DBodies {
     int* hist_n;     // number of valid entries
     int* hist_h;     // ring head
     double* B2C;     // 12: R(9) t(3) body-to-collection
+    float4* bc;      // broad-phase prefilter: bounding centre and radius in FP32 (w < 0: no prefilter)
 };
 static const int HIST = 16;
 

@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     DBodies B, DContacts C, const int* sceneBodyOff, const int* sceneOrder, const int2* gInfo, const int2* glid,
     const int* chunkK, const int* nChunks, const int* contactOf, const float* __restrict__ rec, float* lamS, int cap,
     int nbMax, int iters, float omega, float comp, float tolRel, int check, float slide, int* sceneSweeps,
-    float* sceneRes, const float* lamAlt, int* sceneFall, int writeBack) {
+    float* sceneRes, const float* lamAlt, int* sceneFall, int writeBack, int inner) {
     extern __shared__ float sm[];
     const SweepSmem L(nbMax, cap);
     float* dv = sm + L.dv;
@@ -388,7 +388,11 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         float a[6], b[6];
         for (int q = 0; q < 6; q++) { a[q] = dv[6 * id.x + q]; b[q] = dv[6 * id.y + q]; }
         float ma = mv[id.x], mb = mv[id.y];
-        for (int j = 0; j < cnt; j++) {
+        // sweeps may pass over a group's contacts `inner` times: Gauss-Seidel
+        // on the body pair's own block before the sweep moves on
+        const int reps = op == OP_SWEEP ? inner : 1;
+        for (int jj = 0; jj < reps * cnt; jj++) {
+            const int j = jj % cnt;
             const float* R = srec + (sl0 + j) * RECS;
             float* lp = slam + 4 * (sl0 + j);
             float4 tail = sld4(R + 60);
@@ -565,7 +569,7 @@ int Ctx::batchLaunchSweep(int threads, int cap, int iters, float tol, int check,
     k_batch_sweep<<<nScenes, threads, ssm, stream>>>(
         B, C[cur], sceneBodyOffDev, bSceneOrder, bGInfo, bLid, bChunkK, bNChunks, bContactOf, bRec, lamStart, cap,
         maxSceneBodies, iters, (float)P.omega, (float)comp, tol, check, (float)P.sliding_threshold, bSweeps, bRes,
-        lamAlt, fall, writeBack);
+        lamAlt, fall, writeBack, batchInner);
     AM_LAUNCHED(1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { err = std::string("sweep launch: ") + cudaGetErrorString(e); return AM_E_CUDA; }

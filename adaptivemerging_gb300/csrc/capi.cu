@@ -11,26 +11,34 @@ using am::Ctx;
 
 namespace am {
 
+// Body state straight into the caller's arrays (the device arrays hold the
+// scene's bodies first, in the same interleaving); the flags go through a
+// pinned staging buffer for the sleeping bit.  Pinned caller memory gives
+// full-speed copies.
 int Ctx::getBodies(am_body_state* o) {
-    int n = nScene, cap = host.cap;
-    std::vector<double> x(3 * cap), R(9 * cap), v(3 * cap), w(3 * cap);
-    std::vector<int> fl(cap), par(cap);
-    cudaMemcpyAsync(x.data(), B.x, sizeof(double) * 3 * cap, cudaMemcpyDeviceToHost, stream);
-    cudaMemcpyAsync(R.data(), B.R, sizeof(double) * 9 * cap, cudaMemcpyDeviceToHost, stream);
-    cudaMemcpyAsync(v.data(), B.v, sizeof(double) * 3 * cap, cudaMemcpyDeviceToHost, stream);
-    cudaMemcpyAsync(w.data(), B.w, sizeof(double) * 3 * cap, cudaMemcpyDeviceToHost, stream);
-    cudaMemcpyAsync(fl.data(), B.flags, sizeof(int) * cap, cudaMemcpyDeviceToHost, stream);
-    cudaMemcpyAsync(par.data(), B.parent, sizeof(int) * cap, cudaMemcpyDeviceToHost, stream);
+    int n = nScene;
+    if (o->x) cudaMemcpyAsync(o->x, B.x, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, stream);
+    if (o->R) cudaMemcpyAsync(o->R, B.R, sizeof(double) * 9 * n, cudaMemcpyDeviceToHost, stream);
+    if (o->v) cudaMemcpyAsync(o->v, B.v, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, stream);
+    if (o->omega) cudaMemcpyAsync(o->omega, B.w, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, stream);
+    if (o->parent) cudaMemcpyAsync(o->parent, B.parent, sizeof(int) * n, cudaMemcpyDeviceToHost, stream);
+    if (o->sleeping) {
+        if (n > flagStageCap) {
+            if (flagStage) cudaFreeHost(flagStage);
+            flagStage = nullptr;
+            flagStageCap = 0;
+            if (cudaMallocHost((void**)&flagStage, sizeof(int) * n) != cudaSuccess) {
+                err = "cudaMallocHost failed";
+                return AM_E_CUDA;
+            }
+            flagStageCap = n;
+        }
+        cudaMemcpyAsync(flagStage, B.flags, sizeof(int) * n, cudaMemcpyDeviceToHost, stream);
+    }
     int r = syncErr();
     if (r) return r;
-    for (int i = 0; i < n; i++) {
-        if (o->x) std::memcpy(o->x + 3 * i, &x[3 * i], sizeof(double) * 3);
-        if (o->R) std::memcpy(o->R + 9 * i, &R[9 * i], sizeof(double) * 9);
-        if (o->v) std::memcpy(o->v + 3 * i, &v[3 * i], sizeof(double) * 3);
-        if (o->omega) std::memcpy(o->omega + 3 * i, &w[3 * i], sizeof(double) * 3);
-        if (o->sleeping) o->sleeping[i] = (fl[i] & F_SLEEPING) ? 1 : 0;
-        if (o->parent) o->parent[i] = par[i];
-    }
+    if (o->sleeping)
+        for (int i = 0; i < n; i++) o->sleeping[i] = (flagStage[i] & F_SLEEPING) ? 1 : 0;
     return AM_OK;
 }
 
@@ -197,6 +205,12 @@ int32_t am_get_batch_stats(void* ctx, am_batch_stats* o) {
     o->sweeps_sum = c->batchSweepsTotal;
     o->contact_sweeps = c->batchContactSweepsLast;
     o->residual_max = c->stats.residual_rel;
+    return AM_OK;
+}
+
+int32_t am_set_batch_local_sweeps(void* ctx, int32_t passes) {
+    if (!ctx || passes < 1 || passes > 64) return AM_E_ARG;
+    ((Ctx*)ctx)->batchInner = passes;
     return AM_OK;
 }
 

@@ -246,6 +246,7 @@ struct Ctx {
     int batchCap = 0;            // records staged per chunk (0: autotune)
     int batchResident = 0;       // scenes solved with all records in shared memory, last step
     size_t batchSmemLimit = 0;   // dynamic shared memory the sweep kernel may use
+    int batchInner = 1;          // passes over a body pair's contacts per sweep
     float* bLam = nullptr;
     int bRecCap = 0;
     int* bColour = nullptr;
@@ -388,6 +389,8 @@ struct Ctx {
     int learnedCollect(int enable, int capacity);
     int learnedInferNoAlloc(const float* X, int n, float* out, int tensorCores);
     std::vector<void*> tmps;
+    int* flagStage = nullptr;    // pinned host staging of body flags (getBodies)
+    int flagStageCap = 0;
     template <class T>
     int tmpAlloc(T** p, size_t n);
     int tmpFree(int r);

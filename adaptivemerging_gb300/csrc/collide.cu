@@ -147,6 +147,42 @@ __device__ bool pair_may_touch(const DBodies& B, const DNodes& N, int a, int b) 
     return dist2(ldv(N.cW + 3 * r1), ldv(N.cW + 3 * r2)) < rr * rr;
 }
 
+// Bounding centre and radius of every top-level body in FP32 for a
+// conservative prefilter: boxes use (x, radius) of BoxBox / BoxSphere's
+// quick exit, sphere trees their root node (cW, r); planes and collections
+// get w = -1 and always take the exact test.
+__global__ void k_broad_pack(DBodies B, DNodes N, const int* top, int ntop) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntop) return;
+    int a = top[i];
+    int t = B.type[a];
+    float4 c = make_float4(0.f, 0.f, 0.f, -1.f);
+    if (!(B.flags[a] & F_COLLECTION) && t != AM_PLANE) {
+        if (t == AM_BOX) {
+            v3 x = bodyX(B, a);
+            c = make_float4((float)x.x, (float)x.y, (float)x.z, (float)B.radius[a]);
+        } else {
+            int r0 = B.root[a];
+            v3 x = ldv(N.cW + 3 * r0);
+            c = make_float4((float)x.x, (float)x.y, (float)x.z, (float)N.r[r0]);
+        }
+    }
+    B.bc[a] = c;
+}
+
+// True only when the FP32 distance proves the centres farther apart than the
+// sum of the radii, i.e. when the exact FP64 quick exit would reject the pair
+// too.  The margin, 1e-5 of the radii plus 1e-6 of the coordinates' size,
+// covers the FP32 rounding of the centres, the differences and the sums
+// (each below 2^-22 relative).
+__device__ __forceinline__ bool far_apart32(float4 a, float4 b) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    float d2 = dx * dx + dy * dy + dz * dz;
+    float size = 1.f + fabsf(a.x) + fabsf(a.y) + fabsf(a.z) + fabsf(b.x) + fabsf(b.y) + fabsf(b.z);
+    float T = (a.w + b.w) * 1.00001f + 1e-6f * size;
+    return d2 > T * T;
+}
+
 // one warp per row i of the top-level list; ballot + popc keeps row-major order
 template <bool WRITE>
 __global__ void k_broad_rows(DBodies B, DNodes N, const int* top, int ntop, int* rowCount, const int* rowOff,
@@ -158,10 +194,17 @@ __global__ void k_broad_rows(DBodies B, DNodes N, const int* top, int ntop, int*
     int a = top[i];
     int run = WRITE ? rowOff[i] : 0;
     int end = topEnd ? topEnd[i] : ntop;   // batched scenes: pairs stay inside one scene
+    const float4 ca = B.bc[a];
     for (int j0 = i + 1; j0 < end; j0 += 32) {
         int j = j0 + lane;
         bool hit = false;
-        if (j < end) hit = pair_may_touch(B, N, a, top[j]);
+        if (j < end) {
+            int b = top[j];
+            float4 cb = B.bc[b];
+            // the prefilter only removes pairs the exact test rejects as well
+            bool far = ca.w >= 0.f && cb.w >= 0.f && far_apart32(ca, cb);
+            hit = !far && pair_may_touch(B, N, a, b);
+        }
         unsigned m = __ballot_sync(0xffffffffu, hit);
         if (WRITE && hit) {
             int pos = run + __popc(m & ((1u << lane) - 1u));
@@ -179,6 +222,8 @@ int launch_broadphase(const DBodies& B, const DNodes& N, const int* top, int nto
         cudaMemsetAsync(&dc->n_cand, 0, sizeof(int), s);
         return 0;
     }
+    k_broad_pack<<<(ntop + 127) / 128, 128, 0, s>>>(B, N, top, ntop);
+    AM_LAUNCHED(1);
     int warps = ntop - 1;
     int blocks = (warps * 32 + 255) / 256;
     k_broad_rows<false><<<blocks, 256, 0, s>>>(B, N, top, ntop, rowCount, nullptr, nullptr, nullptr, 0, topEnd);

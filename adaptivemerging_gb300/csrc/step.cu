@@ -304,6 +304,9 @@ void Ctx::release() {
     dc = nullptr;
     if (hc) cudaFreeHost(hc);
     hc = nullptr;
+    if (flagStage) cudaFreeHost(flagStage);
+    flagStage = nullptr;
+    flagStageCap = 0;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
 }
@@ -409,6 +412,7 @@ int Ctx::setScene(const am_scene& s) {
     r |= alloc(&B.radius, cap); r |= alloc(&B.friction, cap); r |= alloc(&B.restitution, cap);
     r |= alloc(&B.plane, 4 * cap); r |= alloc(&B.pp, 3 * cap); r |= alloc(&B.bbB, 24 * cap);
     r |= alloc(&B.hist, HIST * cap); r |= alloc(&B.hist_n, cap); r |= alloc(&B.hist_h, cap);
+    r |= alloc(&B.bc, cap);
     r |= alloc(&B.B2C, 12 * cap);
     r |= alloc(&top, cap); r |= alloc(&subOff, cap + 1); r |= alloc(&subIds, cap);
     r |= alloc(&rowCount, cap + 1); r |= alloc(&rowOff, cap + 1); r |= alloc(&wakeFlag, cap); r |= alloc(&extFlag, cap);

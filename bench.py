@@ -360,8 +360,23 @@ def run_ours(args):
         n_units = 1
     stream = torch.cuda.ExternalStream(sysm.stream_handle())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    # host-owned body state in pinned memory: every timed step pushes it to the
+    # device, steps, and reads it back (the end-to-end figure); the device
+    # time of the step alone is the `value` figure, on the same steps
+    n = sysm.n
+    pin = {k: torch.zeros(m * n, dtype=torch.float64, pin_memory=True) for k, m in
+           (("x", 3), ("R", 9), ("v", 3), ("omega", 3))}
+    pin_i = {k: torch.zeros(n, dtype=torch.int32, pin_memory=True) for k in ("sleeping", "parent")}
+    st_s = abi.am_body_state()
+    for k, t in pin.items():
+        setattr(st_s, k, C.cast(t.data_ptr(), C.POINTER(C.c_double)))
+    for k, t in pin_i.items():
+        setattr(st_s, k, C.cast(t.data_ptr(), C.POINTER(C.c_int32)))
+    h2d = sum(t.numel() * 8 for t in pin.values())
+    d2h = h2d + sum(t.numel() * 4 for t in pin_i.values())
     for _ in range(args.warmup):
         sysm.step(dt)
+    sysm.get_bodies_struct(st_s)
     sysm.reset_perf()
     p0 = sysm.perf()
     barrier(ws)
@@ -369,6 +384,8 @@ def run_ours(args):
     clocks = ClockSampler(local)
     clocks.start()
     total_ms = 0.0
+    e2e_s = 0.0
+    split = [0.0, 0.0]
     sweeps, contacts, res = [], [], []
     conv = []
     for _ in range(args.steps):
@@ -376,11 +393,20 @@ def run_ours(args):
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        ta = time.perf_counter()
+        sysm.put_bodies_struct(st_s)         # H2D of the host-owned state
+        tb = time.perf_counter()
         e0.record(stream)
         sysm.step(dt)
         e1.record(stream)
+        tc = time.perf_counter()
+        sysm.get_bodies_struct(st_s)         # D2H of the new state
+        td = time.perf_counter()
         e1.synchronize()
         total_ms += e0.elapsed_time(e1)
+        e2e_s += td - ta
+        split[0] += tb - ta
+        split[1] += td - tc
         st = sysm.stats()
         contacts.append(st.n_contacts)
         if batch:
@@ -395,27 +421,7 @@ def run_ours(args):
     p1 = sysm.perf()
     t_max = max_over_ranks(ws, total_ms / 1e3, "cuda")
     value = ws * args.steps * n_units / t_max
-
-    # end to end through the C ABI: host-owned state pushed and read back every step
-    n = sysm.n
-    pin = {k: torch.zeros(m * n, dtype=torch.float64, pin_memory=True) for k, m in
-           (("x", 3), ("R", 9), ("v", 3), ("omega", 3))}
-    pin_i = {k: torch.zeros(n, dtype=torch.int32, pin_memory=True) for k in ("sleeping", "parent")}
-    st_s = abi.am_body_state()
-    for k, t in pin.items():
-        setattr(st_s, k, C.cast(t.data_ptr(), C.POINTER(C.c_double)))
-    for k, t in pin_i.items():
-        setattr(st_s, k, C.cast(t.data_ptr(), C.POINTER(C.c_int32)))
-    sysm.get_bodies_struct(st_s)
-    h2d = sum(t.numel() * 8 for t in pin.values())
-    d2h = h2d + sum(t.numel() * 4 for t in pin_i.values())
-    barrier(ws)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        sysm.put_bodies_struct(st_s)
-        sysm.step(dt)
-        sysm.get_bodies_struct(st_s)
-    e2e_t = max_over_ranks(ws, time.perf_counter() - t0, "cuda")
+    e2e_t = max_over_ranks(ws, e2e_s, "cuda")
     e2e = ws * args.steps * n_units / e2e_t
 
     pgs_l = p1.pgs_launches - p0.pgs_launches
@@ -449,7 +455,9 @@ def run_ours(args):
            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if batch else "f64", "data": "synthetic",
            "config": cfg,
-           "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                   "ms_per_step_put_get": [1e3 * x / args.steps for x in split],
+                   "note": "same steps as value; wall time of push + step + read back"},
            "gpu_launches": int(p1.launches - p0.launches),
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak if peak else None, "traffic": traffic,

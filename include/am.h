@@ -244,6 +244,9 @@ int32_t am_set_batch(void* ctx, const am_scene* scenes, int32_t n_scenes);
 /* threads: 0 = autotune on the first step; residual_target <= 0 disables the test */
 int32_t am_set_batch_options(void* ctx, int32_t threads, double residual_target, int32_t check_every);
 int32_t am_get_batch_stats(void* ctx, am_batch_stats* out);
+/* passes of each sweep over one body pair's contacts (1 = plain PGS; more is
+ * block Gauss-Seidel on the pair, same fixed point).  No reference counterpart. */
+int32_t am_set_batch_local_sweeps(void* ctx, int32_t passes);
 /* coloured full solve of a single scene (AM_ORDER_COLOURED): stop once the
  * relative natural-map residual is <= residual_target, tested every
  * check_every sweeps (0 disables; the reference's max-change tolerance still
