@@ -116,7 +116,7 @@ class am_perf(C.Structure):
 
 class am_batch_stats(C.Structure):
     _fields_ = [("n_scenes", _i32), ("converged", _i32), ("sweeps_max", _i32), ("threads", _i32),
-                ("stage_slots", _i32), ("resident_scenes", _i32),
+                ("stage_slots", _i32), ("resident_scenes", _i32), ("cluster_scenes", _i32), ("cluster_size", _i32),
                 ("sweeps_sum", C.c_int64), ("contact_sweeps", C.c_int64), ("residual_max", _f64)]
 
 

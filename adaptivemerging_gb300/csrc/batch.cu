@@ -182,7 +182,8 @@ __device__ __forceinline__ int scene_colours(const int* co) {
 // `cap` slots.  A chunk head entry carries bit 30 when it starts a colour.
 __global__ void k_batch_slots(DContacts C, DPairs P, const int* pairOff, const int* gOrder, const int* colOff,
                               const int* sceneBodyOff, int nc, int npairs, int cap, int2* gInfo, int2* glid,
-                              int* slotOf, int* contactOf, int* chunkK, int* nChunks, DCount* dc) {
+                              int* slotOf, int* contactOf, int* chunkK, int* nChunks, int2* sceneSize,
+                              DCount* dc) {
     __shared__ int s_carry, s_maxcnt, s_warp[32], s_colch[MAXCB + 1];
     const unsigned FULL = 0xffffffffu;
     int s = blockIdx.x, t = threadIdx.x, T = blockDim.x;
@@ -229,6 +230,9 @@ __global__ void k_batch_slots(DContacts C, DPairs P, const int* pairOff, const i
         __syncthreads();
     }
     int maxc = s_maxcnt;
+    // slots of the scene, and the most a split of every colour into equal
+    // slot windows can add to one part (one group per colour)
+    if (t == 0) sceneSize[s] = make_int2(s_carry, ncol * maxc);
     int win = cap - maxc;
     if (win < maxc || win <= 0) {   // a group larger than half the staging buffer
         if (t == 0) { dc->error = AM_E_CAPACITY; nChunks[s] = 0; }
@@ -558,16 +562,300 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     if (t == 0) { sceneSweeps[s] = total; sceneRes[s] = res; }
 }
 
+// ---------------------------------------------------------------------------
+// Scenes too large for one CTA's shared memory: a thread-block cluster of K
+// CTAs (on K SMs) holds one scene.  Every colour's slot range is split into
+// K equal windows; CTA `rank` keeps the groups that start in its window, so
+// the scene's records stay resident across the cluster for the whole solve.
+// Body delta-v is distributed: body b lives in the shared memory of CTA
+// b % K (slot b / K) and is read and written through distributed shared
+// memory.  A cluster barrier separates colours; residual checks reduce into
+// CTA 0.  Every CTA runs the same colour and sweep loops and takes the stop
+// decision from the same reduced value, so all of them reach every barrier.
+__device__ __forceinline__ unsigned cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ unsigned dsm_map(const void* p, unsigned rank) {
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_addr(p)), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ float2 dsm_ld2(unsigned a) {
+    float2 v;
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ void dsm_st2(unsigned a, float x, float y) {
+    asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(x), "f"(y) : "memory");
+}
+__device__ __forceinline__ int dsm_ld_s32(unsigned a) {
+    int v;
+    asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ void dsm_st_s32(unsigned a, int v) {
+    asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void dsm_max_s32(unsigned a, int v) {
+    asm volatile("red.shared::cluster.max.s32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+
+struct ClusterSmem {
+    int dv, mv, rec, lam, gi, gl, total;
+    __host__ __device__ ClusterSmem(int nbMax, int K, int cap) {
+        int own = (nbMax + K - 1) / K;
+        dv = 0;
+        mv = 6 * own;
+        rec = (6 * own + nbMax + 3) & ~3;
+        lam = rec + cap * RECS;
+        gi = lam + 4 * cap;
+        gl = gi + 2 * cap;
+        total = gl + 2 * cap;
+    }
+};
+
+__global__ void __launch_bounds__(256) k_batch_sweep_cluster(
+    DBodies B, DContacts C, const int* sceneBodyOff, const int* bigScenes, const int* colOff, const int2* gInfo,
+    const int2* glid, const int* contactOf, const float* __restrict__ rec, const float* lamS, int cap, int nbMax,
+    int K, int iters, float omega, float comp, float tolRel, int check, float slide, int* sceneSweeps,
+    float* sceneRes, int inner, int writeBack) {
+    extern __shared__ float sm[];
+    const ClusterSmem L(nbMax, K, cap);
+    float* dvOwn = sm + L.dv;
+    float* mv = sm + L.mv;
+    float* srec = sm + L.rec;
+    float* slam = sm + L.lam;
+    int2* sgi = reinterpret_cast<int2*>(sm + L.gi);
+    int2* sgl = reinterpret_cast<int2*>(sm + L.gl);
+    __shared__ int s_lo[MAXCB], s_hi[MAXCB], s_gs[MAXCB], s_kb[MAXCB + 1], s_sb[MAXCB + 1];
+    __shared__ int s_ok, s_any;          // capacity flags (s_any lives on CTA 0)
+    __shared__ int s_resC, s_lamC;       // cluster-wide maxima (CTA 0), float bits
+    __shared__ int s_res, s_lam;         // CTA-local maxima, float bits
+    const unsigned rank = cluster_rank();
+    const int s = bigScenes[blockIdx.x / K];
+    const int t = threadIdx.x, T = blockDim.x;
+    const int b0 = sceneBodyOff[s], nb = sceneBodyOff[s + 1] - b0;
+    const int own = (nb + K - 1) / K;
+    const int* co = colOff + s * (MAXCB + 1);
+    const int ncol = scene_colours(co);
+    for (int b = t; b < nb; b += T) mv[b] = (B.flags[b0 + b] & F_PINNED) ? 0.f : (float)B.minv[b0 + b];
+    for (int i = t; i < 6 * own; i += T) dvOwn[i] = 0.f;
+    // this CTA's part of every colour: groups starting in window `rank`
+    for (int col = t; col < ncol; col += T) {
+        int k0 = co[col], k1 = co[col + 1];
+        int2 e = gInfo[k1 - 1];
+        int st = gInfo[k0].x, span = e.x + e.y - st;
+        int w0 = st + (int)((long long)span * rank / K), w1 = st + (int)((long long)span * (rank + 1) / K);
+        // first group starting at or after w0 (w1): binary search over the
+        // colour's ascending group start slots
+        int lo = k0, z = k1;
+        while (lo < z) { int m = (lo + z) >> 1; if (gInfo[m].x < w0) lo = m + 1; else z = m; }
+        int hi = k1;
+        if (rank + 1 < (unsigned)K) {
+            int a = lo;
+            z = k1;
+            while (a < z) { int m = (a + z) >> 1; if (gInfo[m].x < w1) a = m + 1; else z = m; }
+            hi = a;
+        }
+        s_lo[col] = lo;
+        s_hi[col] = hi;
+        s_gs[col] = hi > lo ? gInfo[lo].x : 0;
+    }
+    if (t == 0) { s_any = 1; s_resC = 0; s_lamC = 0; }
+    __syncthreads();
+    if (t == 0) {
+        int kb = 0, sb = 0;
+        for (int col = 0; col < ncol; col++) {
+            s_kb[col] = kb;
+            s_sb[col] = sb;
+            int lo = s_lo[col], hi = s_hi[col];
+            kb += hi - lo;
+            if (hi > lo) { int2 e = gInfo[hi - 1]; sb += e.x + e.y - gInfo[lo].x; }
+        }
+        s_kb[ncol] = kb;
+        s_sb[ncol] = sb;
+        s_ok = (sb <= cap && kb <= cap) ? 1 : 0;
+    }
+    cluster_sync_all();
+    // every CTA learns whether all parts fit; if one does not, all return here
+    if (t == 0 && !s_ok) dsm_st_s32(dsm_map(&s_any, 0), 0);
+    cluster_sync_all();
+    int okAll = dsm_ld_s32(dsm_map(&s_any, 0));
+    cluster_sync_all();
+    if (!okAll) {
+        if (rank == 0 && t == 0) { sceneSweeps[s] = -1; sceneRes[s] = 1e30f; }
+        return;
+    }
+    // stage this CTA's parts of all colours
+    for (int col = 0; col < ncol; col++) {
+        int lo = s_lo[col], hi = s_hi[col];
+        if (hi <= lo) continue;
+        int gs0 = gInfo[lo].x;
+        int2 e = gInfo[hi - 1];
+        int nsl = e.x + e.y - gs0;
+        float* R = srec + s_sb[col] * RECS;
+        float* Lm = slam + 4 * s_sb[col];
+        for (int i = t; i < nsl * 16; i += T) {
+            int sl = i >> 4, q = i & 15;
+            cp_async16(R + sl * RECS + 4 * q, rec + (size_t)(gs0 + sl) * REC + 4 * q);
+        }
+        for (int i = t; i < nsl; i += T) cp_async16(Lm + 4 * i, lamS + 4 * ((size_t)gs0 + i));
+        for (int i = t; i < hi - lo; i += T) {
+            cp_async8(sgi + s_kb[col] + i, gInfo + lo + i);
+            cp_async8(sgl + s_kb[col] + i, glid + lo + i);
+        }
+    }
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+
+    float rmax = 0.f, lmax = 0.f;
+    auto group = [&](int op, int col, int kk) {
+        int2 gi = sgi[kk];
+        int2 id = sgl[kk];
+        int sl0 = s_sb[col] + (gi.x - s_gs[col]);
+        unsigned pa = dsm_map(dvOwn + 6 * (id.x / K), id.x % K);
+        unsigned pb = dsm_map(dvOwn + 6 * (id.y / K), id.y % K);
+        float a[6], b[6];
+        for (int q = 0; q < 3; q++) {
+            float2 u = dsm_ld2(pa + 8 * q), v = dsm_ld2(pb + 8 * q);
+            a[2 * q] = u.x; a[2 * q + 1] = u.y; b[2 * q] = v.x; b[2 * q + 1] = v.y;
+        }
+        float ma = mv[id.x], mb = mv[id.y];
+        const int cnt = gi.y;
+        const int reps = op == OP_SWEEP ? inner : 1;
+        for (int jj = 0; jj < reps * cnt; jj++) {
+            const int j = jj % cnt;
+            const float* R = srec + (sl0 + j) * RECS;
+            float* lp = slam + 4 * (sl0 + j);
+            float4 tail = sld4(R + 60);
+            float lam[3] = {lp[0], lp[1], lp[2]};
+            if (op == OP_WARM) {
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
+                    float4 i0 = sld4(R + 20 * q + 12), i1 = sld4(R + 20 * q + 16);
+                    group_update(a, b, ma * lam[q], mb * lam[q], lam[q], j0, j1, j2, i0, i1);
+                }
+            } else if (op == OP_SWEEP) {
+                float l0 = lam[0];
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
+                    float4 i0 = sld4(R + 20 * q + 12), i1 = sld4(R + 20 * q + 16);
+                    float jd = group_jdv(a, b, j0, j1, j2);
+                    float D = q == 0 ? tail.x : (q == 1 ? tail.y : tail.z);
+                    float nl = (D * lam[q] - omega * (i1.z + jd)) * i1.w;
+                    if (q == 0) nl = fmaxf(nl, 0.f);
+                    else { float lim = tail.w * l0; nl = fminf(fmaxf(nl, -lim), lim); }
+                    float d = nl - lam[q];
+                    if (q == 0) l0 = nl;
+                    lam[q] = nl;
+                    group_update(a, b, ma * d, mb * d, d, j0, j1, j2, i0, i1);
+                }
+                lp[0] = lam[0]; lp[1] = lam[1]; lp[2] = lam[2];
+            } else if (op == OP_RES) {
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
+                    float4 i1 = sld4(R + 20 * q + 16);
+                    float w = i1.z + group_jdv(a, b, j0, j1, j2) + comp * lam[q];
+                    float z = lam[q] - w * i1.w;
+                    if (q == 0) z = fmaxf(z, 0.f);
+                    else { float lim = tail.w * lam[0]; z = fminf(fmaxf(z, -lim), lim); }
+                    rmax = fmaxf(rmax, fabsf(lam[q] - z));
+                    lmax = fmaxf(lmax, fabsf(lam[q]));
+                }
+            } else {
+                float wt[2];
+#pragma unroll
+                for (int q = 1; q < 3; q++) {
+                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
+                    float4 i1 = sld4(R + 20 * q + 16);
+                    wt[q - 1] = i1.z + group_jdv(a, b, j0, j1, j2);
+                }
+                int c = contactOf[gi.x + j];
+                int st;
+                if (fabsf(lam[0]) <= 1e-14f) st = AM_STATE_BROKEN;
+                else if (fabsf(wt[0]) > slide || fabsf(wt[1]) > slide) st = AM_STATE_ONEDGE;
+                else st = AM_STATE_CLEAR;
+                C.state[c] = st;
+                for (int q = 0; q < 3; q++) C.lam[q * C.cap + c] = (double)lam[q];
+            }
+        }
+        if (op == OP_WARM || op == OP_SWEEP) {
+            if (ma != 0.f) for (int q = 0; q < 3; q++) dsm_st2(pa + 8 * q, a[2 * q], a[2 * q + 1]);
+            if (mb != 0.f) for (int q = 0; q < 3; q++) dsm_st2(pb + 8 * q, b[2 * q], b[2 * q + 1]);
+        }
+    };
+    // colours in order, a cluster barrier after each one that writes delta-v
+    auto pass = [&](int op) {
+        for (int col = 0; col < ncol; col++) {
+            for (int kk = s_kb[col] + t; kk < s_kb[col + 1]; kk += T) group(op, col, kk);
+            if (op == OP_WARM || op == OP_SWEEP) cluster_sync_all();
+        }
+    };
+
+    cluster_sync_all();   // zeroed delta-v of every CTA visible before any remote access
+    pass(OP_WARM);
+    int done = 0;
+    float res = 0.f;
+    for (int it = 0; it < iters; it++) {
+        pass(OP_SWEEP);
+        done = it + 1;
+        if (check > 0 && (done % check == 0 || done == iters)) {
+            if (t == 0) { s_res = 0; s_lam = 0; }
+            rmax = 0.f;
+            lmax = 0.f;
+            __syncthreads();
+            pass(OP_RES);
+            atomicMax(&s_res, __float_as_int(rmax));
+            atomicMax(&s_lam, __float_as_int(lmax));
+            __syncthreads();
+            if (t == 0) {
+                dsm_max_s32(dsm_map(&s_resC, 0), s_res);
+                dsm_max_s32(dsm_map(&s_lamC, 0), s_lam);
+            }
+            cluster_sync_all();
+            float rr = __int_as_float(dsm_ld_s32(dsm_map(&s_resC, 0)));
+            float ll = __int_as_float(dsm_ld_s32(dsm_map(&s_lamC, 0)));
+            res = rr / fmaxf(1.f, ll);
+            cluster_sync_all();   // everyone has read CTA 0's maxima
+            if (rank == 0 && t == 0) { s_resC = 0; s_lamC = 0; }
+            if (res <= tolRel) break;
+        }
+    }
+    if (writeBack) {   // an autotuner trial discards its results
+        pass(OP_FINAL);
+        // owners write their bodies' delta-v back
+        for (int i = t; i < own; i += T) {
+            int lb = i * K + (int)rank;
+            if (lb < nb)
+                for (int k = 0; k < 6; k++) B.dv[6 * (b0 + lb) + k] = (double)dvOwn[6 * i + k];
+        }
+        if (rank == 0 && t == 0) { sceneSweeps[s] = done; sceneRes[s] = res; }
+    }
+    cluster_sync_all();   // no CTA leaves while another may still read its shared memory
+}
+
+size_t batch_cluster_smem(int nbMax, int K, int cap) { return sizeof(float) * (size_t)ClusterSmem(nbMax, K, cap).total; }
+
 const void* batch_sweep_kernel() { return (const void*)k_batch_sweep; }
 
 size_t batch_sweep_smem(int nbMax, int cap) { return sizeof(float) * (size_t)SweepSmem(nbMax, cap).total; }
 
 int Ctx::batchLaunchSweep(int threads, int cap, int iters, float tol, int check, float* lamStart, const float* lamAlt,
-                          int* fall, int writeBack) {
+                          int* fall, int writeBack, int nGrid, const int* order) {
     double comp = P.enable_compliance ? P.compliance : 0.;
     size_t ssm = batch_sweep_smem(maxSceneBodies, cap);
-    k_batch_sweep<<<nScenes, threads, ssm, stream>>>(
-        B, C[cur], sceneBodyOffDev, bSceneOrder, bGInfo, bLid, bChunkK, bNChunks, bContactOf, bRec, lamStart, cap,
+    if (nGrid <= 0) return AM_OK;
+    k_batch_sweep<<<nGrid, threads, ssm, stream>>>(
+        B, C[cur], sceneBodyOffDev, order, bGInfo, bLid, bChunkK, bNChunks, bContactOf, bRec, lamStart, cap,
         maxSceneBodies, iters, (float)P.omega, (float)comp, tol, check, (float)P.sliding_threshold, bSweeps, bRes,
         lamAlt, fall, writeBack, batchInner);
     AM_LAUNCHED(1);
@@ -576,12 +864,126 @@ int Ctx::batchLaunchSweep(int threads, int cap, int iters, float tol, int check,
     return AM_OK;
 }
 
+// The split of the scenes for the sweep with staging capacity `cap`: a scene
+// whose records fit the one-CTA kernel's two buffers stays there; a larger one
+// goes to the cluster kernel with the smallest K in {2, 4, 8} whose CTAs can
+// hold it (its slots / K plus one group per colour within each CTA's
+// capacity), otherwise it streams through the one-CTA kernel.  Every list is
+// ordered costliest first (contacts x sweeps of the previous step) and they
+// are stored one after another: one-CTA scenes, then clusters of 2, 4 and 8.
+static const int CLUSTER_K[3] = {2, 4, 8};
+
+int Ctx::batchSplit(int cap, bool useCluster) {
+    int S = nScenes;
+    hSmall.clear();
+    for (auto& v : hBigK) v.clear();
+    if (useCluster) {
+        std::vector<int2> sz(S);
+        cudaMemcpyAsync(sz.data(), bSceneSize, sizeof(int2) * S, cudaMemcpyDeviceToHost, stream);
+        int r = syncErr();
+        if (r) return r;
+        for (int sc = 0; sc < S; sc++) {
+            int need = -1;
+            if (sz[sc].x > 2 * cap)
+                for (int q = 0; q < 3; q++) {
+                    int K = CLUSTER_K[q];
+                    if ((sz[sc].x + K - 1) / K + sz[sc].y <= clusterCap &&
+                        batch_cluster_smem(maxSceneBodies, K, clusterCap) <= batchSmemLimit) {
+                        need = q;
+                        break;
+                    }
+                }
+            if (need >= 0) hBigK[need].push_back(sc);
+            else hSmall.push_back(sc);
+        }
+    } else {
+        for (int sc = 0; sc < S; sc++) hSmall.push_back(sc);
+    }
+    auto byCost = [&](int a, int b) {
+        long long ca = (size_t)a < lastCost.size() ? lastCost[a] : 0, cb = (size_t)b < lastCost.size() ? lastCost[b] : 0;
+        return ca > cb;
+    };
+    std::vector<int> all;
+    std::stable_sort(hSmall.begin(), hSmall.end(), byCost);
+    all.insert(all.end(), hSmall.begin(), hSmall.end());
+    for (auto& v : hBigK) {
+        std::stable_sort(v.begin(), v.end(), byCost);
+        all.insert(all.end(), v.begin(), v.end());
+    }
+    cudaMemcpyAsync(bSceneOrderBuf, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice, stream);
+    return syncErr();
+}
+
+int Ctx::batchClusterScenes() const {
+    int n = 0;
+    for (auto& v : hBigK) n += (int)v.size();
+    return n;
+}
+
+int Ctx::batchClusterMaxK() const {
+    int k = 0;
+    for (int q = 0; q < 3; q++)
+        if (!hBigK[q].empty()) k = CLUSTER_K[q];
+    return k;
+}
+
+// one cluster launch per cluster size in use, each on its own stream
+int Ctx::batchLaunchClusters(int iters, float tol, int check, int writeBack) {
+    double comp = P.enable_compliance ? P.compliance : 0.;
+    const int* list = bSceneOrderBuf + hSmall.size();
+    for (int q = 0; q < 3; q++) {
+        int nBig = (int)hBigK[q].size();
+        if (nBig == 0) continue;
+        int K = CLUSTER_K[q];
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(nBig * K);
+        cfg.blockDim = dim3(256);
+        cfg.dynamicSmemBytes = batch_cluster_smem(maxSceneBodies, K, clusterCap);
+        cfg.stream = clusterStream[q];
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = K;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaError_t e = cudaLaunchKernelEx(&cfg, k_batch_sweep_cluster, B, C[cur], (const int*)sceneBodyOffDev, list,
+                                           (const int*)bColOff, (const int2*)bGInfo, (const int2*)bLid,
+                                           (const int*)bContactOf, (const float*)bRec, (const float*)bLam, clusterCap,
+                                           maxSceneBodies, K, iters, (float)P.omega, (float)comp, tol, check,
+                                           (float)P.sliding_threshold, bSweeps, bRes, batchInner, writeBack);
+        AM_LAUNCHED(1);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e != cudaSuccess) { err = std::string("cluster sweep launch: ") + cudaGetErrorString(e); return AM_E_CUDA; }
+        list += nBig;
+    }
+    return AM_OK;
+}
+
+// the one-CTA kernel on `stream` with the cluster launches forked beside it
+int Ctx::batchLaunchAll(int threads, int cap, int iters, float tol, int check, float* lamStart, int writeBack) {
+    int r;
+    cudaEventRecord(evFork, stream);
+    for (int q = 0; q < 3; q++)
+        if (!hBigK[q].empty()) cudaStreamWaitEvent(clusterStream[q], evFork, 0);
+    if ((r = batchLaunchClusters(iters, tol, check, writeBack))) return r;
+    if ((r = batchLaunchSweep(threads, cap, iters, tol, check, lamStart, nullptr, writeBack ? bFall : nullptr,
+                              writeBack, (int)hSmall.size(), bSceneOrderBuf)))
+        return r;
+    for (int q = 0; q < 3; q++)
+        if (!hBigK[q].empty()) {
+            cudaEventRecord(evJoin[q], clusterStream[q]);
+            cudaStreamWaitEvent(stream, evJoin[q], 0);
+        }
+    return AM_OK;
+}
+
 // slots and chunks for staging capacity `cap`, then the packed records
 int Ctx::batchLayout(int cap) {
     double comp = P.enable_compliance ? P.compliance : 0.;
     int nc = nContacts;
     k_batch_slots<<<nScenes, 256, 0, stream>>>(C[cur], PR, bPairOff, bOrder, bColOff, sceneBodyOffDev, nc, nPairs, cap,
-                                               bGInfo, bLid, bSlotOf, bContactOf, bChunkK, bNChunks, dc);
+                                               bGInfo, bLid, bSlotOf, bContactOf, bChunkK, bNChunks, bSceneSize, dc);
     k_batch_pack<<<(nc + 127) / 128, 128, 0, stream>>>(B, C[cur], nc, bSlotOf, comp, P.friction_override, P.friction,
                                                      bRec, bLam);
     AM_LAUNCHED(2);
@@ -618,6 +1020,8 @@ int Ctx::batchSolve(double dt) {
         return r;
     int threads = batchThreads, cap = batchCap;
     if ((r = batchLayout(cap))) return r;
+    if ((r = batchSplit(cap, !lUse && clusterEnabled))) return r;
+    bSceneOrder = bSceneOrderBuf;
     if (evA) cudaEventRecord(evA, stream);
     if (lUse || lCollect) {
         if ((r = learnedFeatures(dt))) return r;
@@ -631,8 +1035,16 @@ int Ctx::batchSolve(double dt) {
         lamStart = bLamL;
         lamAlt = bLam;
     }
-    if ((r = batchLaunchSweep(threads, cap, P.iterations, (float)batchTol, batchCheck, lamStart, lamAlt, bFall, 1)))
-        return r;
+    if (lUse) {
+        // the learned start and its in-kernel fallback run in the one-CTA kernel
+        if ((r = batchLaunchSweep(threads, cap, P.iterations, (float)batchTol, batchCheck, lamStart, lamAlt, bFall, 1,
+                                  S, bSceneOrder)))
+            return r;
+    } else {
+        // scenes too large for one CTA run as clusters on their own streams,
+        // concurrently with the one-CTA kernel
+        if ((r = batchLaunchAll(threads, cap, P.iterations, (float)batchTol, batchCheck, lamStart, 1))) return r;
+    }
     if (evB) { cudaEventRecord(evB, stream); pgsPending = true; }
     if (lCollect && (r = learnedRecord())) return r;
     return AM_OK;
@@ -680,9 +1092,11 @@ int Ctx::batchStats() {
     int mx = 0;
     float rmax = 0.f;
     int conv = 0, fall = 0, resid = 0;
-    for (int s = 0; s < nScenes; s++) {
+    for (int s : hSmall) {
         long long ncs = sw[s] > 0 ? cs[s] / sw[s] : 0;
         resid += (ncs > 0 && ncs <= 2 * batchCap) ? 1 : 0;
+    }
+    for (int s = 0; s < nScenes; s++) {
         tot += sw[s];
         mx = std::max(mx, sw[s]);
         rmax = std::max(rmax, rs[s]);
@@ -694,14 +1108,10 @@ int Ctx::batchStats() {
     batchSweepsTotal = tot;
     batchContactSweepsLast = 0;
     for (long long v : cs) batchContactSweepsLast += v;
-    // launch order of the next solve: costliest scenes (contacts x sweeps of
-    // this step) first, so the long ones start in the first wave
-    std::vector<int> order(nScenes);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cs[a] > cs[b]; });
-    cudaMemcpyAsync(bSceneOrderBuf, order.data(), sizeof(int) * nScenes, cudaMemcpyHostToDevice, stream);
-    if ((r = syncErr())) return r;
-    bSceneOrder = bSceneOrderBuf;
+    // cost of every scene (contacts x sweeps) orders the next solve's launches
+    lastCost = cs;
+    for (int sc = 0; sc < nScenes; sc++)
+        if (sw[sc] < 0) { err = "a scene did not fit its cluster"; return AM_E_CAPACITY; }
     stats.sweeps = mx;
     stats.residual_rel = rmax;
     batchConverged = conv;
@@ -762,8 +1172,19 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     cudaMemcpyAsync(sceneOfDev, sOf.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(sceneBodyOffDev, bodyOff.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(topEnd, tEnd.data(), sizeof(int) * all.n_bodies, cudaMemcpyHostToDevice, stream);
-    if (alloc(&bChunkK, (size_t)n * (MAXCH + 1)) || alloc(&bNChunks, n) || alloc(&bSceneOrderBuf, n)) return AM_E_CUDA;
+    if (alloc(&bChunkK, (size_t)n * (MAXCH + 1)) || alloc(&bNChunks, n) || alloc(&bSceneOrderBuf, n) ||
+        alloc(&bSceneSize, n))
+        return AM_E_CUDA;
     bSceneOrder = nullptr;
+    lastCost.clear();
+    for (int q = 0; q < 3; q++) {
+        if (!clusterStream[q] && cudaStreamCreateWithFlags(&clusterStream[q], cudaStreamNonBlocking) != cudaSuccess) {
+            err = "cluster stream";
+            return AM_E_CUDA;
+        }
+        if (!evJoin[q]) cudaEventCreateWithFlags(&evJoin[q], cudaEventDisableTiming);
+    }
+    if (!evFork) cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming);
     // dynamic shared memory the sweep may take: the opt-in limit less its static part
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
@@ -776,6 +1197,20 @@ int Ctx::setBatch(const am_scene* sc, int n) {
         err = "sweep kernel shared-memory limit";
         return AM_E_CUDA;
     }
+    // cluster kernel: the largest staging capacity (multiple of 32, at most
+    // 640 records) that fits for K = 2
+    cudaFuncAttributes fc;
+    clusterUsable = false;
+    if (cudaFuncGetAttributes(&fc, (const void*)k_batch_sweep_cluster) == cudaSuccess) {
+        size_t lim = (size_t)optin > fc.sharedSizeBytes ? optin - fc.sharedSizeBytes : 0;
+        clusterCap = 640;
+        while (clusterCap > 64 && batch_cluster_smem(maxSceneBodies, 2, clusterCap) > lim) clusterCap -= 32;
+        if (batch_cluster_smem(maxSceneBodies, 2, clusterCap) <= lim &&
+            cudaFuncSetAttribute((const void*)k_batch_sweep_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)lim) == cudaSuccess)
+            clusterUsable = true;
+    }
+    clusterEnabled = clusterAllowed && clusterUsable;
     size_t csm = 2 * sizeof(unsigned long long) * (size_t)maxSceneBodies;
     if (csm > 48 * 1024 &&
         cudaFuncSetAttribute((const void*)k_batch_colour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm) !=
@@ -796,12 +1231,16 @@ int Ctx::batchAutotune(double dt) {
     std::vector<int> thr = fixedThreads > 0 ? std::vector<int>{fixedThreads} : std::vector<int>{128, 256, 512};
     std::vector<int> caps;
     for (int c : {64, 128, 192, 256})
-        if (batch_sweep_smem(maxSceneBodies, c) <= batchSmemLimit) caps.push_back(c);
+        if (batch_sweep_smem(maxSceneBodies, c) <= batchSmemLimit && (!batchCapUser || c == batchCapUser))
+            caps.push_back(c);
+    if (batchCapUser && caps.empty() && batch_sweep_smem(maxSceneBodies, batchCapUser) <= batchSmemLimit)
+        caps.push_back(batchCapUser);
     if (caps.empty()) {
         err = "a scene has too many bodies for the batched solve's shared memory";
         return AM_E_CAPACITY;
     }
     int nc = nContacts;
+    int r0 = 0;
     float* save = bLamL;   // the learned start is written only after tuning
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -811,11 +1250,13 @@ int Ctx::batchAutotune(double dt) {
     tuneMs.clear();
     for (int cap : caps) {
         batchLayout(cap);
+        // time the one-CTA kernel on the scenes it would get with this capacity
+        if ((r0 = batchSplit(cap, clusterEnabled && !lUse))) return r0;
         cudaMemcpyAsync(save, bLam, sizeof(float) * 4 * nc, cudaMemcpyDeviceToDevice, stream);
         for (int T : thr) {
             cudaMemcpyAsync(bLam, save, sizeof(float) * 4 * nc, cudaMemcpyDeviceToDevice, stream);
             cudaEventRecord(e0, stream);
-            int r = batchLaunchSweep(T, cap, 8, 0.f, 0, bLam, nullptr, nullptr, 0);
+            int r = batchLaunchAll(T, cap, 8, 0.f, 0, bLam, 0);
             if (r) return r;
             cudaEventRecord(e1, stream);
             cudaEventSynchronize(e1);

@@ -202,6 +202,8 @@ int32_t am_get_batch_stats(void* ctx, am_batch_stats* o) {
     o->threads = c->batchThreads;
     o->stage_slots = c->batchCap;
     o->resident_scenes = c->batchResident;
+    o->cluster_scenes = c->batchClusterScenes();
+    o->cluster_size = c->batchClusterMaxK();
     o->sweeps_sum = c->batchSweepsTotal;
     o->contact_sweeps = c->batchContactSweepsLast;
     o->residual_max = c->stats.residual_rel;
@@ -211,6 +213,22 @@ int32_t am_get_batch_stats(void* ctx, am_batch_stats* o) {
 int32_t am_set_batch_local_sweeps(void* ctx, int32_t passes) {
     if (!ctx || passes < 1 || passes > 64) return AM_E_ARG;
     ((Ctx*)ctx)->batchInner = passes;
+    return AM_OK;
+}
+
+int32_t am_set_batch_clusters(void* ctx, int32_t enable) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    c->clusterAllowed = enable != 0;
+    c->clusterEnabled = c->clusterAllowed && c->clusterUsable;   // usable: checked when the batch was loaded
+    return AM_OK;
+}
+
+int32_t am_set_batch_stage(void* ctx, int32_t slots) {
+    if (!ctx || slots < 0 || (slots && (slots < 64 || slots % 32))) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    c->batchCapUser = slots;
+    c->batchCap = slots;
     return AM_OK;
 }
 

@@ -244,9 +244,18 @@ struct Ctx {
     int* bSceneOrder = nullptr;  // CTA -> scene, costliest scenes first (null: identity)
     int* bSceneOrderBuf = nullptr;
     int batchCap = 0;            // records staged per chunk (0: autotune)
+    int batchCapUser = 0;        // staging capacity fixed by the caller (0: autotuned)
     int batchResident = 0;       // scenes solved with all records in shared memory, last step
     size_t batchSmemLimit = 0;   // dynamic shared memory the sweep kernel may use
     int batchInner = 1;          // passes over a body pair's contacts per sweep
+    // scenes larger than one CTA's shared memory: thread-block clusters
+    int2* bSceneSize = nullptr;  // per scene: slots, one group per colour (split overhead)
+    std::vector<int> hSmall, hBigK[3];   // one-CTA scenes; clusters of 2, 4, 8 CTAs
+    std::vector<long long> lastCost;
+    int clusterCap = 0;
+    bool clusterEnabled = false, clusterAllowed = true, clusterUsable = false;
+    cudaStream_t clusterStream[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t evFork = nullptr, evJoin[3] = {nullptr, nullptr, nullptr};
     float* bLam = nullptr;
     int bRecCap = 0;
     int* bColour = nullptr;
@@ -374,7 +383,12 @@ struct Ctx {
     int batchColours(int* out);
     int batchLayout(int cap);
     int batchLaunchSweep(int threads, int cap, int iters, float tol, int check, float* lamStart, const float* lamAlt,
-                         int* fall, int writeBack);
+                         int* fall, int writeBack, int nGrid, const int* order);
+    int batchSplit(int cap, bool useCluster);
+    int batchLaunchClusters(int iters, float tol, int check, int writeBack);
+    int batchLaunchAll(int threads, int cap, int iters, float tol, int check, float* lamStart, int writeBack);
+    int batchClusterScenes() const;
+    int batchClusterMaxK() const;
     int learnedInit();
     int ensureFeat(int nc);
     int learnedFeatures(double dt);

@@ -309,6 +309,14 @@ void Ctx::release() {
     flagStageCap = 0;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
+    for (int q = 0; q < 3; q++) {
+        if (clusterStream[q]) { cudaStreamSynchronize(clusterStream[q]); cudaStreamDestroy(clusterStream[q]); }
+        clusterStream[q] = nullptr;
+        if (evJoin[q]) cudaEventDestroy(evJoin[q]);
+        evJoin[q] = nullptr;
+    }
+    if (evFork) cudaEventDestroy(evFork);
+    evFork = nullptr;
 }
 
 
@@ -381,6 +389,7 @@ int Ctx::setScene(const am_scene& s) {
     batchThreadsUser = 0;
     batchTunedContacts = 0;
     batchCap = 0;
+    batchCapUser = 0;
     bSceneOrder = nullptr;
     // device buffers of the learned start went with release()
     lW = lG = lM = lV = lNorm = lBias = lLoss = nullptr;

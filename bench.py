@@ -448,6 +448,8 @@ def run_ours(args):
         cfg["cta_threads"] = int(bst.threads)
         cfg["stage_slots"] = int(bst.stage_slots)
         cfg["resident_scenes_last_step"] = int(bst.resident_scenes)
+        cfg["cluster_scenes_last_step"] = int(bst.cluster_scenes)
+        cfg["cluster_size"] = int(bst.cluster_size)
     else:
         cfg["frac_steps_residual_le_1e-6"] = float(np.mean(np.array(res) <= 1e-6))
     unit = "scene-steps/s" if batch else "steps/s"

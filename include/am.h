@@ -236,6 +236,8 @@ typedef struct am_batch_stats {
     int32_t threads;         /* threads per scene CTA (autotuned when 0 given) */
     int32_t stage_slots;     /* contact records per shared-memory staging buffer (autotuned) */
     int32_t resident_scenes; /* scenes whose records stayed in shared memory, last step */
+    int32_t cluster_scenes;  /* scenes solved by a thread-block cluster, last step */
+    int32_t cluster_size;    /* CTAs in the largest cluster used, last step (0: none) */
     int64_t sweeps_sum;      /* sum of the scenes' sweep counts, last step     */
     int64_t contact_sweeps;  /* sum of contacts x sweeps, last step            */
     double  residual_max;    /* worst scene residual, last step                */
@@ -247,6 +249,12 @@ int32_t am_get_batch_stats(void* ctx, am_batch_stats* out);
 /* passes of each sweep over one body pair's contacts (1 = plain PGS; more is
  * block Gauss-Seidel on the pair, same fixed point).  No reference counterpart. */
 int32_t am_set_batch_local_sweeps(void* ctx, int32_t passes);
+/* 1 (default): scenes too large for one CTA's shared memory are solved by a
+ * thread-block cluster of 2-8 CTAs; 0: they stream through one CTA. */
+int32_t am_set_batch_clusters(void* ctx, int32_t enable);
+/* contact records per shared-memory staging buffer of the one-CTA kernel
+ * (a multiple of 32, at least 64; 0 = autotuned) */
+int32_t am_set_batch_stage(void* ctx, int32_t slots);
 /* coloured full solve of a single scene (AM_ORDER_COLOURED): stop once the
  * relative natural-map residual is <= residual_target, tested every
  * check_every sweeps (0 disables; the reference's max-change tolerance still

@@ -99,3 +99,32 @@ def test_batch_residual_target_stops_early(gpu_lib):
     st = g.batch_stats()
     assert st.n_scenes == len(sc) and st.threads in (64, 128, 256, 512)
     assert st.converged == len(sc) and st.sweeps_max < 2000 and st.residual_max <= 1e-5
+
+
+def test_cluster_path_converges_to_oracle(gpu_lib):
+    """A bin too large for one CTA's shared memory is solved by a thread-block
+    cluster; its converged multipliers match the FP64 oracle like the one-CTA
+    path's, and the streaming one-CTA path (clusters off) agrees."""
+    from adaptivemerging_gb300 import native
+    sc = [scenes.bin_scene(1400, 77, gap=-0.001), scenes.bin_scene(40, 78, gap=-0.001)]
+    P = params(friction_override=0, iterations=20000, tolerance=0.0)
+    g = native.BatchSystem(sc, P, threads=256, residual_target=0.0, check_every=0)
+    h = native.BatchSystem(sc, P, threads=256, residual_target=0.0, check_every=0)
+    h.set_clusters(False)
+    g.step(DT)
+    h.step(DT)
+    st = g.batch_stats()
+    assert st.cluster_scenes == 1 and st.cluster_size in (2, 4, 8), (st.cluster_scenes, st.cluster_size)
+    assert h.batch_stats().cluster_scenes == 0
+    o = Oracle(sc[0], P)
+    o.step(DT)
+    co = o.contacts()
+    part = _split(g.contacts(), sc)[0]
+    parth = _split(h.contacts(), sc)[0]
+    assert len(co["body1"]) > 1000
+    assert np.array_equal(part["body1"], co["body1"]) and np.array_equal(part["info"], co["info"])
+    scale = max(1.0, float(np.abs(co["lambda"]).max()))
+    err = float(np.abs(part["lambda"] - co["lambda"]).max()) / scale
+    errh = float(np.abs(parth["lambda"] - co["lambda"]).max()) / scale
+    print(f"cluster of {st.cluster_size}: {len(co['body1'])} contacts, rel err {err:.2e} (one CTA streaming {errh:.2e})")
+    assert err <= 2e-4 and errh <= 2e-4
