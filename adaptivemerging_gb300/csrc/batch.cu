@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     DBodies B, DContacts C, const int* sceneBodyOff, const int* sceneOrder, const int2* gInfo, const int2* glid,
     const int* chunkK, const int* nChunks, const int* contactOf, const float* __restrict__ rec, float* lamS, int cap,
     int nbMax, int iters, float omega, float comp, float tolRel, int check, float slide, int* sceneSweeps,
-    float* sceneRes, const float* lamAlt, int* sceneFall, int writeBack, int inner) {
+    float* sceneRes, const float* lamAlt, int* sceneFall, int writeBack, int inner, float relax, int sym) {
     extern __shared__ float sm[];
     const SweepSmem L(nbMax, cap);
     float* dv = sm + L.dv;
@@ -417,6 +417,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
                     float jd = group_jdv(a, b, j0, j1, j2);
                     float D = q == 0 ? tail.x : (q == 1 ? tail.y : tail.z);
                     float nl = (D * lam[q] - omega * (i1.z + jd)) * i1.w;
+                    nl = lam[q] + relax * (nl - lam[q]);   // over-relaxation (1: plain)
                     if (q == 0) nl = fmaxf(nl, 0.f);
                     else { float lim = tail.w * l0; nl = fminf(fmaxf(nl, -lim), lim); }
                     float d = nl - lam[q];
@@ -466,29 +467,43 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     // Otherwise chunks stream through the two buffers: chunk i + 1 is copied
     // in while chunk i is processed, and (sweeps only) a chunk's multipliers
     // go back to global memory after it.
-    auto pass = [&](int op) {
+    // colour heads of the chunk list (bit 30 marks a chunk that starts a colour)
+    __shared__ int s_head[MAXCB + 1];
+    __shared__ int s_nhead;
+    if (t == 0) {
+        int nh = 0;
+        for (int i = 0; i < nch; i++)
+            if ((ck[i] & HEAD) && nh < MAXCB) s_head[nh++] = i;
+        s_head[nh] = nch;
+        s_nhead = nh;
+    }
+    __syncthreads();
+    const int nhead = s_nhead;
+    auto pass = [&](int op, bool rev) {
         if (resident) {
-            int i = 0;
-            while (i < nch) {
-                int k0 = ck[i] & KMASK;
-                int i2 = i + 1;
-                while (i2 < nch && !(ck[i2] & HEAD)) i2++;
-                int k1 = ck[i2] & KMASK;
+            for (int hh = 0; hh < nhead; hh++) {
+                int h = rev ? nhead - 1 - hh : hh;
+                int k0 = ck[s_head[h]] & KMASK, k1 = ck[s_head[h + 1]] & KMASK;
                 for (int k = k0 + t; k < k1; k += T) {
                     int2 gi = sgi[k - kS0];
                     group(op, gi.x - slotS0, gi.x, gi.y, sgl[k - kS0]);
                 }
                 __syncthreads();
-                i = i2;
             }
             return;
         }
-        stage(0, ck[0] & KMASK, ck[1] & KMASK);
-        for (int i = 0; i < nch; i++) {
-            int buf = i & 1;
+        auto chunkAt = [&](int m) { return rev ? nch - 1 - m : m; };
+        {
+            int i = chunkAt(0);
+            stage(0, ck[i] & KMASK, ck[i + 1] & KMASK);
+        }
+        for (int m = 0; m < nch; m++) {
+            int buf = m & 1;
+            int i = chunkAt(m);
             int k0 = ck[i] & KMASK, k1 = ck[i + 1] & KMASK;
-            if (i + 1 < nch) {
-                stage(buf ^ 1, k1, ck[i + 2] & KMASK);
+            if (m + 1 < nch) {
+                int i2 = chunkAt(m + 1);
+                stage(buf ^ 1, ck[i2] & KMASK, ck[i2 + 1] & KMASK);
                 cp_async_wait_one();
             } else {
                 cp_async_wait_all();
@@ -533,17 +548,17 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         } else if (t == 0 && sceneFall) {
             sceneFall[s] = 0;
         }
-        pass(OP_WARM);
+        pass(OP_WARM, false);
         int done = 0;
         for (int it = 0; it < iters; it++) {
-            pass(OP_SWEEP);
+            pass(OP_SWEEP, sym && (it & 1));
             done = it + 1;
             if (check > 0 && (done % check == 0 || done == iters)) {
                 if (t == 0) { s_res = 0.f; s_lam = 0.f; }
                 rmax = 0.f;
                 lmax = 0.f;
                 __syncthreads();
-                pass(OP_RES);
+                pass(OP_RES, false);
                 atomicMax(reinterpret_cast<int*>(&s_res), __float_as_int(rmax));
                 atomicMax(reinterpret_cast<int*>(&s_lam), __float_as_int(lmax));
                 __syncthreads();
@@ -556,7 +571,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         total += done;
     }
     if (!writeBack) return;   // autotuner trial: results are discarded
-    pass(OP_FINAL);
+    pass(OP_FINAL, false);
     for (int b = t; b < nb; b += T)
         for (int k = 0; k < 6; k++) B.dv[6 * (b0 + b) + k] = (double)dv[6 * b + k];
     if (t == 0) { sceneSweeps[s] = total; sceneRes[s] = res; }
@@ -623,7 +638,7 @@ __global__ void __launch_bounds__(256) k_batch_sweep_cluster(
     DBodies B, DContacts C, const int* sceneBodyOff, const int* bigScenes, const int* colOff, const int2* gInfo,
     const int2* glid, const int* contactOf, const float* __restrict__ rec, const float* lamS, int cap, int nbMax,
     int K, int iters, float omega, float comp, float tolRel, int check, float slide, int* sceneSweeps,
-    float* sceneRes, int inner, int writeBack) {
+    float* sceneRes, int inner, int writeBack, float relax, int sym) {
     extern __shared__ float sm[];
     const ClusterSmem L(nbMax, K, cap);
     float* dvOwn = sm + L.dv;
@@ -751,6 +766,7 @@ __global__ void __launch_bounds__(256) k_batch_sweep_cluster(
                     float jd = group_jdv(a, b, j0, j1, j2);
                     float D = q == 0 ? tail.x : (q == 1 ? tail.y : tail.z);
                     float nl = (D * lam[q] - omega * (i1.z + jd)) * i1.w;
+                    nl = lam[q] + relax * (nl - lam[q]);   // over-relaxation (1: plain)
                     if (q == 0) nl = fmaxf(nl, 0.f);
                     else { float lim = tail.w * l0; nl = fminf(fmaxf(nl, -lim), lim); }
                     float d = nl - lam[q];
@@ -794,26 +810,27 @@ __global__ void __launch_bounds__(256) k_batch_sweep_cluster(
         }
     };
     // colours in order, a cluster barrier after each one that writes delta-v
-    auto pass = [&](int op) {
-        for (int col = 0; col < ncol; col++) {
+    auto pass = [&](int op, bool rev) {
+        for (int cc = 0; cc < ncol; cc++) {
+            int col = rev ? ncol - 1 - cc : cc;
             for (int kk = s_kb[col] + t; kk < s_kb[col + 1]; kk += T) group(op, col, kk);
             if (op == OP_WARM || op == OP_SWEEP) cluster_sync_all();
         }
     };
 
     cluster_sync_all();   // zeroed delta-v of every CTA visible before any remote access
-    pass(OP_WARM);
+    pass(OP_WARM, false);
     int done = 0;
     float res = 0.f;
     for (int it = 0; it < iters; it++) {
-        pass(OP_SWEEP);
+        pass(OP_SWEEP, sym && (it & 1));
         done = it + 1;
         if (check > 0 && (done % check == 0 || done == iters)) {
             if (t == 0) { s_res = 0; s_lam = 0; }
             rmax = 0.f;
             lmax = 0.f;
             __syncthreads();
-            pass(OP_RES);
+            pass(OP_RES, false);
             atomicMax(&s_res, __float_as_int(rmax));
             atomicMax(&s_lam, __float_as_int(lmax));
             __syncthreads();
@@ -831,7 +848,7 @@ __global__ void __launch_bounds__(256) k_batch_sweep_cluster(
         }
     }
     if (writeBack) {   // an autotuner trial discards its results
-        pass(OP_FINAL);
+        pass(OP_FINAL, false);
         // owners write their bodies' delta-v back
         for (int i = t; i < own; i += T) {
             int lb = i * K + (int)rank;
@@ -857,7 +874,7 @@ int Ctx::batchLaunchSweep(int threads, int cap, int iters, float tol, int check,
     k_batch_sweep<<<nGrid, threads, ssm, stream>>>(
         B, C[cur], sceneBodyOffDev, order, bGInfo, bLid, bChunkK, bNChunks, bContactOf, bRec, lamStart, cap,
         maxSceneBodies, iters, (float)P.omega, (float)comp, tol, check, (float)P.sliding_threshold, bSweeps, bRes,
-        lamAlt, fall, writeBack, batchInner);
+        lamAlt, fall, writeBack, batchInner, (float)batchRelax, batchSym);
     AM_LAUNCHED(1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { err = std::string("sweep launch: ") + cudaGetErrorString(e); return AM_E_CUDA; }
@@ -951,7 +968,8 @@ int Ctx::batchLaunchClusters(int iters, float tol, int check, int writeBack) {
                                            (const int*)bColOff, (const int2*)bGInfo, (const int2*)bLid,
                                            (const int*)bContactOf, (const float*)bRec, (const float*)bLam, clusterCap,
                                            maxSceneBodies, K, iters, (float)P.omega, (float)comp, tol, check,
-                                           (float)P.sliding_threshold, bSweeps, bRes, batchInner, writeBack);
+                                           (float)P.sliding_threshold, bSweeps, bRes, batchInner, writeBack,
+                                           (float)batchRelax, batchSym);
         AM_LAUNCHED(1);
         if (e == cudaSuccess) e = cudaGetLastError();
         if (e != cudaSuccess) { err = std::string("cluster sweep launch: ") + cudaGetErrorString(e); return AM_E_CUDA; }

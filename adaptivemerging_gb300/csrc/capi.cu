@@ -232,6 +232,14 @@ int32_t am_set_batch_stage(void* ctx, int32_t slots) {
     return AM_OK;
 }
 
+int32_t am_set_batch_relaxation(void* ctx, double relax, int32_t symmetric) {
+    if (!ctx || !(relax > 0.0 && relax < 2.0) || symmetric < 0 || symmetric > 1) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    c->batchRelax = relax;
+    c->batchSym = symmetric;
+    return AM_OK;
+}
+
 int32_t am_set_residual_target(void* ctx, double residual_target, int32_t check_every) {
     if (!ctx || check_every < 0 || !(residual_target >= 0)) return AM_E_ARG;
     Ctx* c = (Ctx*)ctx;

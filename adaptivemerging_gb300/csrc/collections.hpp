@@ -248,6 +248,8 @@ struct Ctx {
     int batchResident = 0;       // scenes solved with all records in shared memory, last step
     size_t batchSmemLimit = 0;   // dynamic shared memory the sweep kernel may use
     int batchInner = 1;          // passes over a body pair's contacts per sweep
+    double batchRelax = 1.0;     // over-relaxation of the batched sweep (1: plain projected Gauss-Seidel)
+    int batchSym = 0;            // 1: odd sweeps walk the colours backwards
     // scenes larger than one CTA's shared memory: thread-block clusters
     int2* bSceneSize = nullptr;  // per scene: slots, one group per colour (split overhead)
     std::vector<int> hSmall, hBigK[3];   // one-CTA scenes; clusters of 2, 4, 8 CTAs

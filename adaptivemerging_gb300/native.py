@@ -20,7 +20,7 @@ EXPORTS = [
     "am_params_default", "am_create", "am_destroy", "am_last_error", "am_set_params", "am_set_scene",
     "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
     "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats", "am_set_residual_target",
-    "am_set_batch_local_sweeps", "am_set_batch_clusters", "am_set_batch_stage",
+    "am_set_batch_local_sweeps", "am_set_batch_clusters", "am_set_batch_stage", "am_set_batch_relaxation",
     "am_learned_collect", "am_learned_train", "am_learned_use", "am_learned_scope", "am_learned_weights", "am_learned_info",
     "am_learned_grad", "am_learned_infer", "am_learned_infer_noalloc",
 ]
@@ -70,6 +70,7 @@ def lib():
         L.am_set_batch_local_sweeps.argtypes = [vp, C.c_int32]
         L.am_set_batch_clusters.argtypes = [vp, C.c_int32]
         L.am_set_batch_stage.argtypes = [vp, C.c_int32]
+        L.am_set_batch_relaxation.argtypes = [vp, C.c_double, C.c_int32]
         L.am_learned_collect.argtypes = [vp, C.c_int32, C.c_int32]
         L.am_learned_train.argtypes = [vp, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_double)]
         L.am_learned_use.argtypes = [vp, C.c_int32]
@@ -113,6 +114,9 @@ class BatchSystem:
         st = abi.am_batch_stats()
         self._check(lib().am_get_batch_stats(self.h, C.byref(st)))
         return st
+
+    def set_relaxation(self, relax=1.0, symmetric=False):
+        self._check(lib().am_set_batch_relaxation(self.h, relax, int(symmetric)))
 
     def set_stage(self, slots):
         self._check(lib().am_set_batch_stage(self.h, slots))

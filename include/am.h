@@ -255,6 +255,10 @@ int32_t am_set_batch_clusters(void* ctx, int32_t enable);
 /* contact records per shared-memory staging buffer of the one-CTA kernel
  * (a multiple of 32, at least 64; 0 = autotuned) */
 int32_t am_set_batch_stage(void* ctx, int32_t slots);
+/* batched sweep variants with the same fixed point (no reference counterpart):
+ * over-relaxation factor in (0, 2) applied before the projection (1 = plain
+ * PGS), and symmetric = 1 to walk the colours backwards on odd sweeps */
+int32_t am_set_batch_relaxation(void* ctx, double relax, int32_t symmetric);
 /* coloured full solve of a single scene (AM_ORDER_COLOURED): stop once the
  * relative natural-map residual is <= residual_target, tested every
  * check_every sweeps (0 disables; the reference's max-change tolerance still
