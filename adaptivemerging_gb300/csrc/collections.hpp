@@ -192,6 +192,7 @@ struct Ctx {
     int* colourFill = nullptr;
     static const int MAXC = 256;
     int coopBlocks = 0;
+    std::vector<int> hColOff;    // colour offsets of the coloured full solve (host copy)
     double* Mj = nullptr;     // coloured sweep: M^-1 J^T per row and lane (36 per contact)
     double* invD = nullptr;   // 1/(D + c) per row
     int mjCap = 0;

@@ -29,6 +29,10 @@ namespace am {
 using namespace amd;
 
 __device__ __forceinline__ bool barrier_x(DCount* dc, int nblocks) {
+    if (nblocks == 1) {   // one block: the block barrier orders global memory too
+        __syncthreads();
+        return *(volatile int*)&dc->error == 0;
+    }
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {

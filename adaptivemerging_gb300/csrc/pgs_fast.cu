@@ -53,6 +53,10 @@ __device__ __forceinline__ double hw_sum(double v, unsigned mask) {
 }
 
 __device__ __forceinline__ bool grid_barrier_f(DCount* dc, int nblocks) {
+    if (nblocks == 1) {   // one block: the block barrier orders global memory too
+        __syncthreads();
+        return *(volatile int*)&dc->error == 0;
+    }
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {

@@ -400,6 +400,10 @@ void colour_groups(const DBodies& B, const DContacts& C, DPairs& P, int npairs, 
 // iteration limit; on expiry the kernel records AM_E_TIMEOUT and all blocks
 // leave at their next barrier check.
 __device__ __forceinline__ bool grid_barrier(DCount* dc, int nblocks) {
+    if (nblocks == 1) {   // one block: the block barrier orders global memory too
+        __syncthreads();
+        return *(volatile int*)&dc->error == 0;
+    }
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {

@@ -665,8 +665,16 @@ int Ctx::runPGS(int nc, const int* order, int iters, bool inColl, double dt, boo
             if (alloc(&Mj, 36 * (size_t)cap2) || alloc(&invD, 3 * (size_t)cap2)) return AM_E_CUDA;
             mjCap = cap2;
         }
-        // 8 half-warp groups per block; enough blocks for every group of the largest colour
-        int blocks = std::min(coopBlocks, std::max(1, (nPairs + 7) / 8));
+        // 8 half-warp groups per block; enough blocks for every group of the
+        // largest colour (more blocks only make the grid barriers slower)
+        hColOff.resize(ncol + 1);
+        if (ncol > 0) {
+            cudaMemcpyAsync(hColOff.data(), colourOff, sizeof(int) * (ncol + 1), cudaMemcpyDeviceToHost, stream);
+            if ((r = syncErr())) return r;
+        }
+        int widest = 0;
+        for (int k = 0; k < ncol; k++) widest = std::max(widest, hColOff[k + 1] - hColOff[k]);
+        int blocks = std::min(coopBlocks, std::max(1, (widest + 7) / 8));
         if (timed) cudaEventRecord(evA, stream);   // time the sweep (prep + persistent kernel)
         launch_pgs_fast(B, c, PR, groupOrder, colourOff, ncol, nc, iters, P.omega, comp, P.tolerance, !inColl,
                         P.friction_override, P.friction, P.sliding_threshold, Mj, invD, mjCap, dc, blocks, stream,

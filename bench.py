@@ -218,16 +218,16 @@ def cpu_baseline(name, max_seconds=15.0, max_steps=400, warmup=20, steps=10):
         return {"value": v, "unit": "scene-steps/s", "cores": 1, "kind": "port", "sample": desc}
     P.solver_order = abi.AM_ORDER_REFERENCE
     o = Oracle(sc, P)
-    o.step(dt, 2)
+    o.step(dt, warmup)             # the GPU arm's warm-up, so both time the same steps
     t0 = time.perf_counter()
     n = 0
-    while n < max_steps and time.perf_counter() - t0 < max_seconds:
+    while n < steps and time.perf_counter() - t0 < max_seconds:
         o.step(dt)
         n += 1
     el = time.perf_counter() - t0
     return {"value": n / el, "unit": "steps/s", "cores": 1, "kind": "port",
-            "sample": f"{n} steps of the same scene from its initial state after 2 warm-up steps "
-                      f"({el:.1f} s, single thread)"}
+            "sample": f"steps {warmup + 1}..{warmup + n} of the same scene (the GPU arm times steps "
+                      f"{warmup + 1}..{warmup + steps}), {el:.1f} s, single thread, reference order"}
 
 
 def run_reference(args):
@@ -475,7 +475,8 @@ def run_ours(args):
     if batch and args.learned:
         out["learned_warm_start"] = learned_protocol(sc, P, dt)
     if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args.workload, warmup=args.warmup, steps=min(args.steps, 10))
+        out["cpu_baseline"] = cpu_baseline(args.workload, warmup=args.warmup,
+                                           steps=min(args.steps, 10) if batch else args.steps)
     print(json.dumps(out))
 
 

@@ -128,3 +128,52 @@ def test_cluster_path_converges_to_oracle(gpu_lib):
     errh = float(np.abs(parth["lambda"] - co["lambda"]).max()) / scale
     print(f"cluster of {st.cluster_size}: {len(co['body1'])} contacts, rel err {err:.2e} (one CTA streaming {errh:.2e})")
     assert err <= 2e-4 and errh <= 2e-4
+
+
+def test_batch_edge_cases(gpu_lib):
+    """Ragged batches: a scene without contacts (bodies far apart), a scene
+    with only pinned bodies and a plane, one-body scenes and ordinary bins
+    step together; every scene's stats are sane and the contact-free scenes
+    report no sweeps."""
+    from adaptivemerging_gb300 import native
+    b = scenes.Builder()
+    b.plane((0, 0, 0), (0, 1, 0))
+    for k in range(5):
+        b.sphere(0.2, (10.0 * k, 5.0, 0.0))          # far apart, falling: no contacts yet
+    apart = b.build()
+    b = scenes.Builder()
+    b.plane((0, 0, 0), (0, 1, 0))
+    b.box((1, 1, 1), (0, 0.5, 0), pinned=True)
+    pinned = b.build()
+    b = scenes.Builder()
+    b.plane((0, 0, 0), (0, 1, 0))
+    b.sphere(0.3, (0, 0.29, 0))                      # resting on the plane
+    single = b.build()
+    sc = [apart, scenes.bin_scene(50, 5, gap=-0.001), pinned, single, scenes.bin_scene(300, 6, gap=-0.001)]
+    g = native.BatchSystem(sc, params(friction_override=0, iterations=2000), threads=0, residual_target=1e-6,
+                           check_every=10)
+    for _ in range(3):
+        g.step(DT)
+    ss = g.scene_stats()
+    st = g.batch_stats()
+    assert st.n_scenes == len(sc)
+    assert ss["sweeps"][0] == 0 and ss["sweeps"][2] == 0
+    assert ss["sweeps"][3] > 0 and ss["sweeps"][1] > 0 and ss["sweeps"][4] > 0
+    assert (ss["residual"] <= 1e-6).all(), ss["residual"]
+    x = g.bodies()["x"]
+    assert np.isfinite(x).all()
+
+
+def test_batch_rejects_oversized_scene(gpu_lib):
+    """A scene whose body count exceeds the sweep's shared memory is refused
+    with AM_E_CAPACITY on the first step, not run."""
+    from adaptivemerging_gb300 import native
+    b = scenes.Builder()
+    b.plane((0, 0, 0), (0, 1, 0))
+    for k in range(9000):
+        b.sphere(0.05, ((k % 100) * 0.5, 0.049 + (k // 100) * 0.5, 0.0))
+    g = native.BatchSystem([b.build()], params(friction_override=0, iterations=100), threads=0,
+                           residual_target=1e-6, check_every=10)
+    with pytest.raises(native.AmError) as e:
+        g.step(DT)
+    assert e.value.code == -2
