@@ -278,7 +278,6 @@ struct Ctx {
     long long batchContactSweepsLast = 0;
     long long* bCS = nullptr;
     int batchConverged = 0;
-    std::vector<float> tuneMs;
     // learned warm start
     float *lW = nullptr, *lG = nullptr, *lM = nullptr, *lV = nullptr, *lNorm = nullptr, *lBias = nullptr,
           *lLoss = nullptr;
