@@ -185,6 +185,57 @@ def random_pile(n=30, seed=0, kinds=("box", "sphere"), extent=3.0, height=4.0):
     return B.build()
 
 
+def funnel_clumps(n_clumps=200, seed=5, top=3.0, bottom=0.5, height=3.0, base=1.0):
+    """Clumps poured into a funnel over a platform (the large-scene workload's
+    geometry, scaled by `n_clumps`).  Each clump is a sphere tree of 4-16
+    spheres, r U(0.02, 0.08) m, in a compact random cluster, density
+    U(500, 2000).  The funnel is four pinned box panels forming a truncated
+    pyramid (half-widths `top` to `bottom`) whose lower rim sits `base` m
+    above a pinned platform box on the ground plane.  The clumps start in a
+    jittered grid inside the funnel, so they meet the panels at once.  The
+    platform is static: oscillating (kinematic) bodies are not part of the
+    reference's contact path."""
+    rng = np.random.default_rng(seed)
+    B = Builder()
+    B.plane((0, 0, 0), (0, 1, 0), friction=0.7)
+    B.box((2.0 * (bottom + 1.0), 0.2, 2.0 * (bottom + 1.0)), (0.0, 0.1, 0.0), pinned=True, friction=0.7)
+    y0 = 0.2 + base
+    slope = math.atan2(top - bottom, height)          # panel tilt from vertical
+    length = math.hypot(top - bottom, height)
+    cy = y0 + height / 2
+    ch = (top + bottom) / 2
+    t = 0.05
+    for (ax, sx, sz, px, pz, sign) in ((2, 2 * top, t, 0.0, ch, 1.0), (2, 2 * top, t, 0.0, -ch, -1.0),
+                                      (0, t, 2 * top, ch, 0.0, -1.0), (0, t, 2 * top, -ch, 0.0, 1.0)):
+        # the panel's long side runs along the slope: tilt about the horizontal axis parallel to it
+        # (about +x, +angle tips the top towards +z; about +z, +angle tips it towards -x)
+        axis = (1.0, 0.0, 0.0) if ax == 2 else (0.0, 0.0, 1.0)
+        R = axis_angle(axis, sign * slope)
+        size = (sx, length, sz)
+        B.box(size, (px, cy, pz), R=R, pinned=True, friction=0.7)
+    pitch = 0.3
+    k = 0
+    layer = 0
+    while k < n_clumps:
+        y = y0 + height * 0.35 + layer * pitch
+        half = bottom + (top - bottom) * min(1.0, (y - y0) / height) - 0.25
+        m = max(1, int(2 * half / pitch))
+        for i in range(m):
+            for j in range(m):
+                if k >= n_clumps:
+                    break
+                x = -half + (i + 0.5) * (2 * half / m) + rng.uniform(-0.02, 0.02)
+                z = -half + (j + 0.5) * (2 * half / m) + rng.uniform(-0.02, 0.02)
+                nsph = int(rng.integers(4, 17))
+                rs = rng.uniform(0.02, 0.08, nsph)
+                cs = rng.normal(size=(nsph, 3)) * 0.04
+                B.clump(cs, rs, (x, y, z), density=float(rng.uniform(500, 2000)), friction=0.7,
+                        R=axis_angle(rng.normal(size=3), rng.uniform(0, math.pi)))
+                k += 1
+        layer += 1
+    return B.build()
+
+
 def bin_scene(n_bodies, seed, extent=10.0, wall_height=12.0, box_frac=0.5, gap=0.01):
     """One scene of the batched workload: `n_bodies` boxes (sides U(0.1, 1.0)
     m) and spheres (r U(0.05, 0.5) m), density U(500, 2000) kg/m3, in a 10 x
