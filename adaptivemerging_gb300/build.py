@@ -16,8 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libam.so")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["collide.cu", "solve.cu", "step.cu", "capi.cu", "pgs_fast.cu", "merging.cu", "gs_exact.cu", "batch.cu", "learned.cu"]
-# batch.cu computes in FP32 with FMA (not part of the bit-exact path)
-# translation units that may contract a*b+c (not part of the bit-exact path)
+# translation units that may contract a*b+c (the coloured FP64 solve and the
+# FP32 batched and learned paths; none of them is part of the bit-exact path)
 FMA_OK = {"pgs_fast.cu", "batch.cu", "learned.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",

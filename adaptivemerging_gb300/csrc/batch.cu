@@ -1221,8 +1221,13 @@ int Ctx::setBatch(const am_scene* sc, int n) {
         return AM_E_CUDA;
     bSceneOrder = nullptr;
     lastCost.clear();
+    // the cluster launches carry the longest bins: their streams get the
+    // highest priority so their CTAs are scheduled ahead of the one-CTA kernel's
+    int prLeast = 0, prGreatest = 0;
+    cudaDeviceGetStreamPriorityRange(&prLeast, &prGreatest);
     for (int q = 0; q < 3; q++) {
-        if (!clusterStream[q] && cudaStreamCreateWithFlags(&clusterStream[q], cudaStreamNonBlocking) != cudaSuccess) {
+        if (!clusterStream[q] &&
+            cudaStreamCreateWithPriority(&clusterStream[q], cudaStreamNonBlocking, prGreatest) != cudaSuccess) {
             err = "cluster stream";
             return AM_E_CUDA;
         }
@@ -1247,7 +1252,7 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     clusterUsable = false;
     if (cudaFuncGetAttributes(&fc, (const void*)k_batch_sweep_cluster) == cudaSuccess) {
         size_t lim = (size_t)optin > fc.sharedSizeBytes ? optin - fc.sharedSizeBytes : 0;
-        clusterCap = 640;
+        clusterCap = clusterCapUser > 0 ? clusterCapUser : 640;
         while (clusterCap > 64 && batch_cluster_smem(maxSceneBodies, 2, clusterCap) > lim) clusterCap -= 32;
         if (batch_cluster_smem(maxSceneBodies, 2, clusterCap) <= lim &&
             cudaFuncSetAttribute((const void*)k_batch_sweep_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -224,6 +224,12 @@ int32_t am_set_batch_clusters(void* ctx, int32_t enable) {
     return AM_OK;
 }
 
+int32_t am_set_batch_cluster_stage(void* ctx, int32_t slots) {
+    if (!ctx || slots < 0 || (slots && (slots < 64 || slots % 32))) return AM_E_ARG;
+    ((Ctx*)ctx)->clusterCapUser = slots;
+    return AM_OK;
+}
+
 int32_t am_set_batch_stage(void* ctx, int32_t slots) {
     if (!ctx || slots < 0 || (slots && (slots < 64 || slots % 32))) return AM_E_ARG;
     Ctx* c = (Ctx*)ctx;

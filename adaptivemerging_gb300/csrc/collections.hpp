@@ -256,6 +256,7 @@ struct Ctx {
     std::vector<int> hSmall, hBigK[3];   // one-CTA scenes; clusters of 2, 4, 8 CTAs
     std::vector<long long> lastCost;
     int clusterCap = 0;
+    int clusterCapUser = 0;      // cluster staging capacity fixed by the caller (0: largest that fits)
     bool clusterEnabled = false, clusterAllowed = true, clusterUsable = false;
     cudaStream_t clusterStream[3] = {nullptr, nullptr, nullptr};
     cudaEvent_t evFork = nullptr, evJoin[3] = {nullptr, nullptr, nullptr};

@@ -21,6 +21,7 @@ EXPORTS = [
     "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
     "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats", "am_set_residual_target",
     "am_set_batch_local_sweeps", "am_set_batch_clusters", "am_set_batch_stage", "am_set_batch_relaxation",
+    "am_set_batch_cluster_stage",
     "am_learned_collect", "am_learned_train", "am_learned_use", "am_learned_scope", "am_learned_weights", "am_learned_info",
     "am_learned_grad", "am_learned_infer", "am_learned_infer_noalloc",
 ]
@@ -70,6 +71,7 @@ def lib():
         L.am_set_batch_local_sweeps.argtypes = [vp, C.c_int32]
         L.am_set_batch_clusters.argtypes = [vp, C.c_int32]
         L.am_set_batch_stage.argtypes = [vp, C.c_int32]
+        L.am_set_batch_cluster_stage.argtypes = [vp, C.c_int32]
         L.am_set_batch_relaxation.argtypes = [vp, C.c_double, C.c_int32]
         L.am_learned_collect.argtypes = [vp, C.c_int32, C.c_int32]
         L.am_learned_train.argtypes = [vp, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_double)]
@@ -94,11 +96,13 @@ def lib():
 class BatchSystem:
     """Many independent scenes in one context (merging off); am_step advances all."""
 
-    def __init__(self, scene_list, params, threads=0, residual_target=1e-6, check_every=10):
+    def __init__(self, scene_list, params, threads=0, residual_target=1e-6, check_every=10, cluster_stage=0):
         self.params = params
         self.scenes = scene_list
         self.h = C.c_void_p()
         self._check(lib().am_create(C.byref(params), C.byref(self.h)))
+        if cluster_stage:
+            self._check(lib().am_set_batch_cluster_stage(self.h, cluster_stage))
         arr = (abi.am_scene * len(scene_list))()
         for k, s in enumerate(scene_list):
             arr[k] = s.struct()

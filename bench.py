@@ -349,7 +349,9 @@ def run_ours(args):
     from adaptivemerging_gb300 import build, native
     ws, rank, local = dist_init()
     torch.cuda.set_device(local)
-    build.build()
+    if local == 0:                    # one compiler per node; the others wait for the library
+        build.build()
+    barrier(ws)
     sc, P, dt, cfg = workload(args.workload)
     batch = args.workload == "batch"
     if batch:

@@ -255,6 +255,9 @@ int32_t am_set_batch_clusters(void* ctx, int32_t enable);
 /* contact records per shared-memory staging buffer of the one-CTA kernel
  * (a multiple of 32, at least 64; 0 = autotuned) */
 int32_t am_set_batch_stage(void* ctx, int32_t slots);
+/* contact records each CTA of a cluster holds (a multiple of 32, at least 64;
+ * 0 = the largest that fits, at most 640); takes effect at the next am_set_batch */
+int32_t am_set_batch_cluster_stage(void* ctx, int32_t slots);
 /* batched sweep variants with the same fixed point (no reference counterpart):
  * over-relaxation factor in (0, 2) applied before the projection (1 = plain
  * PGS), and symmetric = 1 to walk the colours backwards on odd sweeps */
