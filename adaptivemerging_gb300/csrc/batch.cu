@@ -1058,10 +1058,15 @@ int Ctx::batchSolve(double dt) {
                                             maxSceneBodies, dc);
     AM_LAUNCHED(2);
     // tune on the first solve and again whenever the contact count has grown
-    // by half since the last tuning (piles forming change the best shape)
-    if ((batchThreads == 0 || batchCap == 0 || 2 * (long long)nc > 3 * (long long)batchTunedContacts) &&
-        (r = batchAutotune(dt)))
+    // by half since the last tuning (piles forming change the best shape);
+    // a CTA size and staging capacity both given by the caller are used as is
+    if (batchThreadsUser && batchCapUser) {
+        batchThreads = batchThreadsUser;
+        batchCap = batchCapUser;
+    } else if ((batchThreads == 0 || batchCap == 0 || 2 * (long long)nc > 3 * (long long)batchTunedContacts) &&
+               (r = batchAutotune(dt))) {
         return r;
+    }
     int threads = batchThreads, cap = batchCap;
     if ((r = batchLayout(cap))) return r;
     if ((r = batchSplit(cap, !lUse && clusterEnabled))) return r;

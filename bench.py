@@ -355,7 +355,9 @@ def run_ours(args):
     sc, P, dt, cfg = workload(args.workload)
     batch = args.workload == "batch"
     if batch:
-        sysm = native.BatchSystem(sc, P, threads=0, residual_target=1e-6, check_every=10)
+        sysm = native.BatchSystem(sc, P, threads=args.threads, residual_target=RESIDUAL_TARGET, check_every=10)
+        if args.stage:
+            sysm.set_stage(args.stage)
         n_units = len(sc)
     else:
         sysm = native.System(sc, P)
@@ -492,6 +494,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain GPU PGS comparison arm")
     ap.add_argument("--learned", action="store_true", help="also run the learned warm-start protocol")
+    ap.add_argument("--threads", type=int, default=0, help="batched solve: CTA size (0: autotuned)")
+    ap.add_argument("--stage", type=int, default=0,
+                    help="batched solve: staging slots (0: autotuned; with --threads, no tuning launches)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
