@@ -1005,13 +1005,14 @@ int Ctx::batchLaunchClusters(int iters, float tol, int check, int writeBack) {
 }
 
 // the one-CTA kernel on `stream` with the cluster launches forked beside it
-int Ctx::batchLaunchAll(int threads, int cap, int iters, float tol, int check, float* lamStart, int writeBack) {
+int Ctx::batchLaunchAll(int threads, int cap, int iters, float tol, int check, float* lamStart, const float* lamAlt,
+                        int writeBack) {
     int r;
     cudaEventRecord(evFork, stream);
     for (int q = 0; q < 3; q++)
         if (!hBigK[q].empty()) cudaStreamWaitEvent(clusterStream[q], evFork, 0);
     if ((r = batchLaunchClusters(iters, tol, check, writeBack))) return r;
-    if ((r = batchLaunchSweep(threads, cap, iters, tol, check, lamStart, nullptr, writeBack ? bFall : nullptr,
+    if ((r = batchLaunchSweep(threads, cap, iters, tol, check, lamStart, lamAlt, writeBack ? bFall : nullptr,
                               writeBack, (int)hSmall.size(), bSceneOrderBuf)))
         return r;
     for (int q = 0; q < 3; q++)
@@ -1069,7 +1070,7 @@ int Ctx::batchSolve(double dt) {
     }
     int threads = batchThreads, cap = batchCap;
     if ((r = batchLayout(cap))) return r;
-    if ((r = batchSplit(cap, !lUse && clusterEnabled))) return r;
+    if ((r = batchSplit(cap, clusterEnabled))) return r;
     bSceneOrder = bSceneOrderBuf;
     if (evA) cudaEventRecord(evA, stream);
     if (lUse || lCollect) {
@@ -1084,16 +1085,11 @@ int Ctx::batchSolve(double dt) {
         lamStart = bLamL;
         lamAlt = bLam;
     }
-    if (lUse) {
-        // the learned start and its in-kernel fallback run in the one-CTA kernel
-        if ((r = batchLaunchSweep(threads, cap, P.iterations, (float)batchTol, batchCheck, lamStart, lamAlt, bFall, 1,
-                                  S, bSceneOrder)))
-            return r;
-    } else {
-        // scenes too large for one CTA run as clusters on their own streams,
-        // concurrently with the one-CTA kernel
-        if ((r = batchLaunchAll(threads, cap, P.iterations, (float)batchTol, batchCheck, lamStart, 1))) return r;
-    }
+    // scenes too large for one CTA run as clusters on their own streams,
+    // concurrently with the one-CTA kernel.  The learned start and its
+    // in-kernel fallback apply to the one-CTA scenes; clusters keep the plain
+    // previous-frame start.
+    if ((r = batchLaunchAll(threads, cap, P.iterations, (float)batchTol, batchCheck, lamStart, lamAlt, 1))) return r;
     if (evB) { cudaEventRecord(evB, stream); pgsPending = true; }
     if (lCollect && (r = learnedRecord())) return r;
     return AM_OK;
@@ -1304,12 +1300,12 @@ int Ctx::batchAutotune(double dt) {
     for (int cap : caps) {
         batchLayout(cap);
         // time the one-CTA kernel on the scenes it would get with this capacity
-        if ((r0 = batchSplit(cap, clusterEnabled && !lUse))) return r0;
+        if ((r0 = batchSplit(cap, clusterEnabled))) return r0;
         cudaMemcpyAsync(save, bLam, sizeof(float) * 4 * nc, cudaMemcpyDeviceToDevice, stream);
         for (int T : thr) {
             cudaMemcpyAsync(bLam, save, sizeof(float) * 4 * nc, cudaMemcpyDeviceToDevice, stream);
             cudaEventRecord(e0, stream);
-            int r = batchLaunchAll(T, cap, 8, 0.f, 0, bLam, 0);
+            int r = batchLaunchAll(T, cap, 8, 0.f, 0, bLam, nullptr, 0);
             if (r) return r;
             cudaEventRecord(e1, stream);
             cudaEventSynchronize(e1);

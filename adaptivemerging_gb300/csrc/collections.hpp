@@ -389,7 +389,8 @@ struct Ctx {
                          int* fall, int writeBack, int nGrid, const int* order);
     int batchSplit(int cap, bool useCluster);
     int batchLaunchClusters(int iters, float tol, int check, int writeBack);
-    int batchLaunchAll(int threads, int cap, int iters, float tol, int check, float* lamStart, int writeBack);
+    int batchLaunchAll(int threads, int cap, int iters, float tol, int check, float* lamStart, const float* lamAlt,
+                       int writeBack);
     int batchClusterScenes() const;
     int batchClusterMaxK() const;
     int learnedInit();
