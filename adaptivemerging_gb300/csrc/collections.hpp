@@ -284,7 +284,8 @@ struct Ctx {
           *lLoss = nullptr;
     __nv_bfloat16* lWb = nullptr;
     float *lX = nullptr, *lY = nullptr, *lDX = nullptr, *lDY = nullptr, *lZ1 = nullptr, *lZ2 = nullptr,
-          *lYh = nullptr;
+          *lYh = nullptr, *lXN = nullptr, *lA1 = nullptr, *lA2 = nullptr, *lD1 = nullptr, *lD2 = nullptr,
+          *lDYb = nullptr;
     int *lKeep = nullptr, *lPos = nullptr, *lIdx = nullptr;
     int lFeatCap = 0, lDcap = 0, lDn = 0, lTrainCap = 0, lIdxCap = 0;
     int lCollect = 0, lUse = 0;   // lUse: 0 off, 1 BF16 tensor cores, 2 FP32

@@ -10,8 +10,10 @@
 //   * k_labels    : (lambda - lambda_warm) * D of the converged solve, the
 //                   change from the previous-frame start (recorded for the
 //                   contacts in scope of scenes that reached the target);
-//   * training    : FP32 forward (k_fwd), backward with per-block weight-
-//                   gradient reduction (k_bwd), Adam (k_adam), MSE loss;
+//   * training    : FP32 forward (k_fwd), backward as per-sample deltas
+//                   (k_bwd_delta) then one thread per parameter and sample
+//                   chunk for the weight gradients (k_bwd_grad), Adam
+//                   (k_adam), MSE loss;
 //   * inference   : BF16 weights on the tensor cores (mma.sync m16n8k16,
 //                   FP32 accumulate); the 16 x 8 accumulator tiles of one
 //                   layer are re-packed in registers as the A operand of the
@@ -148,59 +150,87 @@ __global__ void k_fwd(const float* __restrict__ X, const float* __restrict__ nor
     for (int q = 0; q < NOUT; q++) Yh[(size_t)s * NOUT + q] = y[q];
 }
 
-// loss = mean over samples and outputs of (yhat - y)^2; grads accumulated into G
-__global__ void k_bwd(const float* __restrict__ X, const float* __restrict__ Yt, const float* __restrict__ norm,
-                      const float* __restrict__ W, const int* __restrict__ idx, int n, const float* Z1,
-                      const float* Z2, const float* Yh, float* G, float* loss) {
+// Backward in two kernels.  k_bwd_delta: one thread per sample computes the
+// per-sample deltas (dy, dz2, dz1), the activations the weight gradients need,
+// the normalised inputs and the MSE loss (mean over samples and outputs).
+__global__ void k_bwd_delta(const float* __restrict__ X, const float* __restrict__ Yt,
+                            const float* __restrict__ norm, const float* __restrict__ W, const int* __restrict__ idx,
+                            int n, const float* __restrict__ Z1, const float* __restrict__ Z2,
+                            const float* __restrict__ Yh, float* XN, float* A1, float* A2, float* D1, float* D2,
+                            float* DY, float* loss) {
     __shared__ float w[NPAR];
-    __shared__ float g[NPAR];
     __shared__ float nm[2 * NIN];
     __shared__ float sl;
-    for (int k = threadIdx.x; k < NPAR; k += blockDim.x) { w[k] = W[k]; g[k] = 0.f; }
+    for (int k = threadIdx.x; k < NPAR; k += blockDim.x) w[k] = W[k];
     for (int k = threadIdx.x; k < 2 * NIN; k += blockDim.x) nm[k] = norm[k];
     if (threadIdx.x == 0) sl = 0.f;
     __syncthreads();
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < n) {
         int src = idx ? idx[s] : s;
-        float x[NIN], dy[NOUT], dz2[NH];
-        for (int k = 0; k < NIN; k++) x[k] = (X[(size_t)src * NIN + k] - nm[k]) * nm[NIN + k];
-        float l = 0.f;
-        float scale = 2.f / (float)(n * NOUT);
+        for (int k = 0; k < NIN; k++) XN[(size_t)s * NIN + k] = (X[(size_t)src * NIN + k] - nm[k]) * nm[NIN + k];
+        float dy[NOUT], l = 0.f;
+        const float scale = 2.f / (float)(n * NOUT);
         for (int q = 0; q < NOUT; q++) {
             float e = Yh[(size_t)s * NOUT + q] - Yt[(size_t)src * NOUT + q];
             l += e * e;
             dy[q] = scale * e;
-            atomicAdd(&g[OB3 + q], dy[q]);
+            DY[(size_t)s * NOUT + q] = dy[q];
         }
         atomicAdd(&sl, l);
+        float dz2[NH];
         for (int o = 0; o < NH; o++) {
             float z = Z2[(size_t)s * NH + o];
-            float a = gelu(z);
+            A2[(size_t)s * NH + o] = gelu(z);
             float da = 0.f;
-            for (int q = 0; q < NOUT; q++) {
-                atomicAdd(&g[OW3 + q * NH + o], dy[q] * a);
-                da = fmaf(w[OW3 + q * NH + o], dy[q], da);
-            }
+            for (int q = 0; q < NOUT; q++) da = fmaf(w[OW3 + q * NH + o], dy[q], da);
             dz2[o] = da * gelu_d(z);
-            atomicAdd(&g[OB2 + o], dz2[o]);
+            D2[(size_t)s * NH + o] = dz2[o];
         }
         for (int k = 0; k < NH; k++) {
-            float z1 = Z1[(size_t)s * NH + k];
-            float a1 = gelu(z1);
-            float da1 = 0.f;
-            for (int o = 0; o < NH; o++) {
-                atomicAdd(&g[OW2 + o * NH + k], dz2[o] * a1);
-                da1 = fmaf(w[OW2 + o * NH + k], dz2[o], da1);
-            }
-            float dz1 = da1 * gelu_d(z1);
-            atomicAdd(&g[OB1 + k], dz1);
-            for (int i = 0; i < NIN; i++) atomicAdd(&g[OW1 + k * NIN + i], dz1 * x[i]);
+            float z = Z1[(size_t)s * NH + k];
+            A1[(size_t)s * NH + k] = gelu(z);
+            float da = 0.f;
+            for (int o = 0; o < NH; o++) da = fmaf(w[OW2 + o * NH + k], dz2[o], da);
+            D1[(size_t)s * NH + k] = da * gelu_d(z);
         }
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < NPAR; k += blockDim.x) atomicAdd(&G[k], g[k]);
     if (threadIdx.x == 0) atomicAdd(loss, sl / (float)(n * NOUT));
+}
+
+// k_bwd_grad: one thread per parameter and chunk of GCH samples sums that
+// parameter's gradient over the chunk (deltas x activations, no atomics
+// between samples) and adds it to G once.  Consecutive parameters read
+// consecutive activations of a sample, so the loads coalesce.
+static const int GCH = 128;
+__global__ void k_bwd_grad(const float* __restrict__ XN, const float* __restrict__ A1, const float* __restrict__ A2,
+                           const float* __restrict__ D1, const float* __restrict__ D2, const float* __restrict__ DY,
+                           int n, float* G) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= NPAR) return;
+    int s0 = blockIdx.y * GCH, s1 = min(n, s0 + GCH);
+    float acc = 0.f;
+    if (p < OB1) {
+        int o = p / NIN, i = p % NIN;
+        for (int s = s0; s < s1; s++) acc = fmaf(D1[(size_t)s * NH + o], XN[(size_t)s * NIN + i], acc);
+    } else if (p < OW2) {
+        int o = p - OB1;
+        for (int s = s0; s < s1; s++) acc += D1[(size_t)s * NH + o];
+    } else if (p < OB2) {
+        int o = (p - OW2) / NH, k = (p - OW2) % NH;
+        for (int s = s0; s < s1; s++) acc = fmaf(D2[(size_t)s * NH + o], A1[(size_t)s * NH + k], acc);
+    } else if (p < OW3) {
+        int o = p - OB2;
+        for (int s = s0; s < s1; s++) acc += D2[(size_t)s * NH + o];
+    } else if (p < OB3) {
+        int q = (p - OW3) / NH, o = (p - OW3) % NH;
+        for (int s = s0; s < s1; s++) acc = fmaf(DY[(size_t)s * NOUT + q], A2[(size_t)s * NH + o], acc);
+    } else {
+        int q = p - OB3;
+        for (int s = s0; s < s1; s++) acc += DY[(size_t)s * NOUT + q];
+    }
+    atomicAdd(&G[p], acc);
 }
 
 __global__ void k_adam(float* W, const float* G, float* M, float* V, int n, float lr, float b1, float b2, float eps,
@@ -513,7 +543,9 @@ int Ctx::learnedTrain(int epochs, int batch, float lr, float* lastLoss, int norm
     if (n < batch) { err = "not enough recorded samples"; return AM_E_STATE; }
     if (normalise && (r = learnedNormalise())) return r;
     if (batch > lTrainCap) {
-        if (alloc(&lZ1, (size_t)NH * batch) || alloc(&lZ2, (size_t)NH * batch) || alloc(&lYh, (size_t)NOUT * batch))
+        if (alloc(&lZ1, (size_t)NH * batch) || alloc(&lZ2, (size_t)NH * batch) || alloc(&lYh, (size_t)NOUT * batch) ||
+            alloc(&lXN, (size_t)NIN * batch) || alloc(&lA1, (size_t)NH * batch) || alloc(&lA2, (size_t)NH * batch) ||
+            alloc(&lD1, (size_t)NH * batch) || alloc(&lD2, (size_t)NH * batch) || alloc(&lDYb, (size_t)NOUT * batch))
             return AM_E_CUDA;
         lTrainCap = batch;
     }
@@ -538,11 +570,14 @@ int Ctx::learnedTrain(int epochs, int batch, float lr, float* lastLoss, int norm
             const int* idx = lIdx + (size_t)b * batch;
             cudaMemsetAsync(lG, 0, sizeof(float) * NPAR, stream);
             k_fwd<<<(batch + 127) / 128, 128, 0, stream>>>(lDX, lNorm, lW, idx, batch, lZ1, lZ2, lYh);
-            k_bwd<<<(batch + 127) / 128, 128, 0, stream>>>(lDX, lDY, lNorm, lW, idx, batch, lZ1, lZ2, lYh, lG, lLoss);
+            k_bwd_delta<<<(batch + 127) / 128, 128, 0, stream>>>(lDX, lDY, lNorm, lW, idx, batch, lZ1, lZ2, lYh, lXN,
+                                                                 lA1, lA2, lD1, lD2, lDYb, lLoss);
+            k_bwd_grad<<<dim3((NPAR + 127) / 128, (batch + GCH - 1) / GCH), 128, 0, stream>>>(lXN, lA1, lA2, lD1, lD2,
+                                                                                             lDYb, batch, lG);
             lAdamT++;
             float c1 = 1.f / (1.f - std::pow(0.9f, (float)lAdamT)), c2 = 1.f / (1.f - std::pow(0.999f, (float)lAdamT));
             k_adam<<<(NPAR + 255) / 256, 256, 0, stream>>>(lW, lG, lM, lV, NPAR, lr, 0.9f, 0.999f, 1e-8f, c1, c2);
-            AM_LAUNCHED(3);
+            AM_LAUNCHED(4);
         }
         float ls = 0;
         cudaMemcpyAsync(&ls, lLoss, sizeof(float), cudaMemcpyDeviceToHost, stream);
@@ -557,17 +592,22 @@ int Ctx::learnedTrain(int epochs, int batch, float lr, float* lastLoss, int norm
 int Ctx::learnedGrad(const float* X, const float* Y, int n, float* grad, float* loss) {
     int r = learnedInit();
     if (r) return r;
-    float *dX = nullptr, *dY = nullptr, *z1 = nullptr, *z2 = nullptr, *yh = nullptr;
+    float *dX = nullptr, *dY = nullptr, *z1 = nullptr, *z2 = nullptr, *yh = nullptr, *xn = nullptr, *a1 = nullptr,
+          *a2 = nullptr, *d1 = nullptr, *d2 = nullptr, *dyb = nullptr;
     if (tmpAlloc(&dX, (size_t)NIN * n) || tmpAlloc(&dY, (size_t)NOUT * n) || tmpAlloc(&z1, (size_t)NH * n) ||
-        tmpAlloc(&z2, (size_t)NH * n) || tmpAlloc(&yh, (size_t)NOUT * n))
+        tmpAlloc(&z2, (size_t)NH * n) || tmpAlloc(&yh, (size_t)NOUT * n) || tmpAlloc(&xn, (size_t)NIN * n) ||
+        tmpAlloc(&a1, (size_t)NH * n) || tmpAlloc(&a2, (size_t)NH * n) || tmpAlloc(&d1, (size_t)NH * n) ||
+        tmpAlloc(&d2, (size_t)NH * n) || tmpAlloc(&dyb, (size_t)NOUT * n))
         return tmpFree(AM_E_CUDA);
     cudaMemcpyAsync(dX, X, sizeof(float) * NIN * n, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(dY, Y, sizeof(float) * NOUT * n, cudaMemcpyHostToDevice, stream);
     cudaMemsetAsync(lG, 0, sizeof(float) * NPAR, stream);
     cudaMemsetAsync(lLoss, 0, sizeof(float), stream);
     k_fwd<<<(n + 127) / 128, 128, 0, stream>>>(dX, lNorm, lW, nullptr, n, z1, z2, yh);
-    k_bwd<<<(n + 127) / 128, 128, 0, stream>>>(dX, dY, lNorm, lW, nullptr, n, z1, z2, yh, lG, lLoss);
-    AM_LAUNCHED(2);
+    k_bwd_delta<<<(n + 127) / 128, 128, 0, stream>>>(dX, dY, lNorm, lW, nullptr, n, z1, z2, yh, xn, a1, a2, d1, d2, dyb,
+                                                     lLoss);
+    k_bwd_grad<<<dim3((NPAR + 127) / 128, (n + GCH - 1) / GCH), 128, 0, stream>>>(xn, a1, a2, d1, d2, dyb, n, lG);
+    AM_LAUNCHED(3);
     cudaMemcpyAsync(grad, lG, sizeof(float) * NPAR, cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(loss, lLoss, sizeof(float), cudaMemcpyDeviceToHost, stream);
     return tmpFree(syncErr());

@@ -395,6 +395,7 @@ int Ctx::setScene(const am_scene& s) {
     lW = lG = lM = lV = lNorm = lBias = lLoss = nullptr;
     lWb = nullptr;
     lX = lY = lDX = lDY = lZ1 = lZ2 = lYh = nullptr;
+    lXN = lA1 = lA2 = lD1 = lD2 = lDYb = nullptr;
     lKeep = lPos = lIdx = nullptr;
     lFeatCap = lDcap = lDn = lTrainCap = lIdxCap = 0;
     lCollect = lUse = 0;

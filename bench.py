@@ -47,16 +47,18 @@ SWEEP_CAP = 5000                     # sweep cap of the residual-targeted solves
 RESIDUAL_TARGET = 1e-6
 
 
-def workload(name):
-    """Scene (or list of scenes), parameters, dt and a description of the named workload."""
+def workload(name, n_scenes=BATCH_SCENES):
+    """Scene (or list of scenes), parameters, dt and a description of the named
+    workload.  `n_scenes` shrinks the batch for profiling runs only; the
+    benchmark figure is the 512-bin batch."""
     if name == "batch":
-        sc = scenes.batch_scenes(BATCH_SCENES, seed=3)
+        sc = scenes.batch_scenes(n_scenes, seed=3)
         P = abi.default_params(gravity_amount=9.81, friction_override=0, restitution_override=1,
                                restitution=0.0, iterations=SWEEP_CAP, enable_merging=0)
         return sc, P, 0.005, {
-            "workload": "512 independent bins, body counts log-uniform 20..2000, boxes U(0.1,1.0) m and "
+            "workload": f"{n_scenes} independent bins, body counts log-uniform 20..2000, boxes U(0.1,1.0) m and "
                         "spheres U(0.05,0.5) m, density U(500,2000), per-scene mu U(0.3,0.8), 4 pinned walls + plane",
-            "scenes": BATCH_SCENES, "bodies": int(sum(x.n for x in sc)), "dt": 0.005,
+            "scenes": n_scenes, "bodies": int(sum(x.n for x in sc)), "dt": 0.005,
             "pgs": f"FP32, one CTA per scene, previous-frame warm start, each scene swept until its relative "
                    f"LCP residual <= {RESIDUAL_TARGET:g} (checked every 10 sweeps, cap {SWEEP_CAP})",
             "merging": "off", "precision": "fp32 solve, fp64 collision/contact setup/integration"}
@@ -207,12 +209,12 @@ def oracle_batch_sample(sc_list, P, dt, warmup, steps, stride=BATCH_SAMPLE_STRID
         f"sweeps, cap {SWEEP_CAP}) like the GPU arm")
 
 
-def cpu_baseline(name, max_seconds=15.0, max_steps=400, warmup=20, steps=10):
+def cpu_baseline(name, max_seconds=15.0, max_steps=400, warmup=20, steps=10, n_scenes=BATCH_SCENES):
     """Oracle (single-threaded CPU restatement of the reference path) on the
     same workload: steps/s over a bounded sample."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_binding import Oracle
-    sc, P, dt, _ = workload(name)
+    sc, P, dt, _ = workload(name, n_scenes)
     if name == "batch":
         v, desc = oracle_batch_sample(sc, P, dt, warmup, steps)
         return {"value": v, "unit": "scene-steps/s", "cores": 1, "kind": "port", "sample": desc}
@@ -234,7 +236,7 @@ def run_reference(args):
     ws, rank, _ = dist_init()
     if rank != 0:
         return
-    sc, P, dt, cfg = workload(args.workload)
+    sc, P, dt, cfg = workload(args.workload, args.scenes)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_binding import Oracle
     P.solver_order = abi.AM_ORDER_REFERENCE
@@ -244,7 +246,7 @@ def run_reference(args):
         cores = max(1, len(os.sched_getaffinity(0)))
         v, desc = oracle_batch_sample(sc, P, dt, args.warmup, args.steps, stride=REFERENCE_SAMPLE_STRIDE,
                                       workers=cores)
-        el = args.steps * BATCH_SCENES / v
+        el = args.steps * len(sc) / v
         unit = "scene-steps/s"
     else:
         o = Oracle(sc, P)
@@ -352,7 +354,7 @@ def run_ours(args):
     if local == 0:                    # one compiler per node; the others wait for the library
         build.build()
     barrier(ws)
-    sc, P, dt, cfg = workload(args.workload)
+    sc, P, dt, cfg = workload(args.workload, args.scenes)
     batch = args.workload == "batch"
     if batch:
         sysm = native.BatchSystem(sc, P, threads=args.threads, residual_target=RESIDUAL_TARGET, check_every=10)
@@ -480,7 +482,7 @@ def run_ours(args):
         out["learned_warm_start"] = learned_protocol(sc, P, dt)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.workload, warmup=args.warmup,
-                                           steps=min(args.steps, 10) if batch else args.steps)
+                                           steps=min(args.steps, 10) if batch else args.steps, n_scenes=args.scenes)
     print(json.dumps(out))
 
 
@@ -495,6 +497,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain GPU PGS comparison arm")
     ap.add_argument("--learned", action="store_true", help="also run the learned warm-start protocol")
     ap.add_argument("--threads", type=int, default=0, help="batched solve: CTA size (0: autotuned)")
+    ap.add_argument("--scenes", type=int, default=BATCH_SCENES, help="bins in the batch (profiling runs only)")
     ap.add_argument("--stage", type=int, default=0,
                     help="batched solve: staging slots (0: autotuned; with --threads, no tuning launches)")
     args = ap.parse_args()
