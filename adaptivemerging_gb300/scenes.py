@@ -4,7 +4,7 @@ Mass properties follow the reference scene loader (XMLParser.java:360-447):
 box mass = sx*sy*sz*density, inertia = m/12 diag(sy^2+sz^2, sx^2+sz^2,
 sx^2+sy^2); sphere mass = 4/3 pi r^3 density, inertia = 2/5 m r^2 I.  The
 reference's benchmark scenes are not public datasets; these generators build
-the BASELINE workloads (tower, brick wall + projectile, batched bins, clumps)
+the benchmark workloads (tower, brick wall + projectile, batched bins, clumps)
 from a seed with the sizes and distributions the benchmark names.
 """
 import math
