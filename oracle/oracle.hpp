@@ -1,6 +1,6 @@
 // oracle.hpp -- TEST INFRASTRUCTURE ONLY.  CPU restatement of the reference's
 // per-step contact path (EulalieCoevoet/AdaptiveMerging, src/mergingBodies3D),
-// used by tests/ as the parity checker and by bench.py as the CPU baseline.
+// used by tests/ to check the device path and by bench.py as the CPU baseline.
 // Nothing in the product links or calls this code.
 //
 // Parity basis: the reference is Java with no tests for the 3D engine, so the
