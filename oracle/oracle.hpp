@@ -3,9 +3,12 @@
 // used by tests/ to check the device path and by bench.py as the CPU baseline.
 // Nothing in the product links or calls this code.
 //
-// Parity basis: the reference is Java with no tests for the 3D engine, so the
+// Parity unpinned: the reference is Java with no tests or golden vectors for
+// the 3D engine, and it cannot run here (no JDK, missing JOGL jar), so the
 // restatement follows the Java sources line by line (cited per function in
-// oracle.cpp) with javax.vecmath operation order (vm.hpp).  Identity-hashed
+// oracle.cpp) with javax.vecmath operation order (vm.hpp), and is held by
+// analytic known answers, invariants and its own committed fixture
+// (tests/test_oracle_cpu.py, tests/golden/).  Identity-hashed
 // Java HashSets are replaced by insertion-ordered sets (LinkedHashSet order),
 // which is the documented deterministic order of every parity test.
 #pragma once
