@@ -142,12 +142,18 @@ __global__ void k_adv_vel(DBodies B, const int* top, int ntop, const int* so, co
         for (int k = so[b]; k < so[b + 1]; k++) apply_vel_to(B, b, si[k]);
 }
 
-__global__ void k_adv_pos(DBodies B, const int* top, int ntop, const int* so, const int* si, double dt) {
+__global__ void k_adv_pos(DBodies B, const int* top, int ntop, const int* so, const int* si, double dt,
+                          DCount* dc) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ntop) return;
     int b = top[i];
     int f = B.flags[b];
     if ((f & F_PINNED) || (f & F_SLEEPING)) return;
+    // a non-finite velocity (from non-finite inputs or a diverged solve) is
+    // reported as AM_E_NONFINITE; the arithmetic itself is left as it is
+    bool fin = true;
+    for (int k = 0; k < 3; k++) fin = fin && isfinite(B.v[3 * b + k]) && isfinite(B.w[3 * b + k]);
+    if (!fin) atomicExch(&dc->error, AM_E_NONFINITE);
     adv_pos(B, b, dt);
     if (f & F_COLLECTION) coll_update_subs(B, b, so, si);
 }
@@ -546,7 +552,9 @@ int Ctx::readCounts() {
     if (e != cudaSuccess) { err = std::string("CUDA: ") + cudaGetErrorString(e); return AM_E_CUDA; }
     if (hc->error) {
         int code = hc->error;
-        err = code == AM_E_TIMEOUT ? "device wait gave up (grid barrier)" : "device capacity exceeded (tree stack or colours)";
+        err = code == AM_E_TIMEOUT     ? "device wait gave up (grid barrier)"
+              : code == AM_E_NONFINITE ? "a body velocity became NaN or infinite"
+                                       : "device capacity exceeded (tree stack, colours or staging chunks)";
         cudaMemsetAsync(&dc->error, 0, sizeof(int), stream);
         return code;
     }
@@ -752,7 +760,7 @@ void Ctx::advVel(double dt) {
 
 void Ctx::advPos(double dt) {
     if (ntop <= 0) return;
-    k_adv_pos<<<(ntop + 127) / 128, 128, 0, stream>>>(B, top, ntop, subOff, subIds, dt);
+    k_adv_pos<<<(ntop + 127) / 128, 128, 0, stream>>>(B, top, ntop, subOff, subIds, dt, dc);
     AM_LAUNCHED(1);
 }
 

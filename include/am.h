@@ -222,12 +222,15 @@ int32_t am_get_stats(void* ctx, am_solve_stats* out);
 /*
  * Batched scenes (no reference counterpart: the reference simulates one
  * scene).  n independent scenes are loaded into one context; am_step then
- * advances all of them (collision per scene, one CTA per scene in the solve).
- * Body ids in readbacks are global: scene s's body i is at
+ * advances all of them (collision per scene; in the solve one CTA per scene,
+ * or a thread-block cluster of 2-8 CTAs for a scene too large for one CTA's
+ * shared memory).  Body ids in readbacks are global: scene s's body i is at
  * (number of bodies of scenes < s) + i.  Merging must be off.  The batched
  * solve runs in FP32 with delta-v in shared memory and stops each scene when
  * its relative natural-map residual is <= residual_target (checked every
- * check_every sweeps) or after am_params.iterations sweeps.
+ * check_every sweeps) or after am_params.iterations sweeps.  A scene whose
+ * bodies do not fit one CTA's shared memory (about 7000 bodies) is refused
+ * with AM_E_CAPACITY.
  */
 typedef struct am_batch_stats {
     int32_t n_scenes;

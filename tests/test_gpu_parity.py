@@ -140,3 +140,15 @@ def test_coloured_residual_target_stops_at_target(gpu_lib):
     print(f"residual target 1e-7: sweeps {st.sweeps} residual_rel {st.residual_rel:.2e} rel err {err:.2e}")
     assert st.residual_rel <= 1e-7 and st.sweeps % 10 == 0 and st.sweeps < 60000
     assert err <= 1e-5
+
+
+def test_nonfinite_velocity_is_reported(gpu_lib):
+    """A NaN body velocity in the input is reported as AM_E_NONFINITE by the
+    step that integrates it (the arithmetic itself is not altered)."""
+    from adaptivemerging_gb300 import native
+    sc = scenes.tower(3, seed=2)
+    sc.a["v"][3] = np.nan            # body 1 (the lowest box), x velocity
+    g = native.System(sc, params(iterations=20))
+    with pytest.raises(native.AmError) as e:
+        g.step(DT)
+    assert e.value.code == -3
