@@ -40,9 +40,6 @@ static const int REC = 64;      // floats per packed contact record (global)
 static const int RECS = 68;     // shared-memory stride of a staged record (pads banks)
 static const int MAXCB = 64;    // colours per scene
 static const int MAXCH = 1024;  // staging chunks per scene
-// a residual pass runs only when the sweep's largest change, relative to the
-// largest multiplier, is within this factor of the target
-static const float RES_GATE = 4.f;
 
 // Packed record (floats): row r = 0..2 occupies [20r, 20r + 20):
 //   [20r .. 20r+11] J (a.v, a.w, b.v, b.w), [20r+12 .. 20r+14] jinv_a a.w,
@@ -389,7 +386,6 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     };
 
     float rmax = 0.f, lmax = 0.f;
-    float dmx = 0.f, lmx = 0.f;   // largest |change| and |lambda| of the current sweep
     // one group: its two bodies' delta-v in registers across its contacts;
     // sl0 is the group's first slot in the staging buffer, slA in the scene
     auto group = [&](int op, int sl0, int slA, int cnt, int2 id) {
@@ -425,8 +421,6 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
                     if (q == 0) nl = fmaxf(nl, 0.f);
                     else { float lim = tail.w * l0; nl = fminf(fmaxf(nl, -lim), lim); }
                     float d = nl - lam[q];
-                    dmx = fmaxf(dmx, fabsf(d));
-                    lmx = fmaxf(lmx, fabsf(nl));
                     if (q == 0) l0 = nl;
                     lam[q] = nl;
                     group_update(a, b, ma * d, mb * d, d, j0, j1, j2, i0, i1);
@@ -557,24 +551,11 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         pass(OP_WARM, false);
         int done = 0;
         for (int it = 0; it < iters; it++) {
-            dmx = 0.f;
-            lmx = 0.f;
             pass(OP_SWEEP, sym && (it & 1));
             done = it + 1;
-            bool full = false;
+            // the same check points as the cluster kernel, so a scene stops at
+            // the same sweep whichever kernel solves it
             if (check > 0 && (done % check == 0 || done == iters)) {
-                // the sweep's largest relative change gates the residual pass:
-                // far from the target the pass is skipped (the last sweep is
-                // always checked)
-                if (t == 0) { s_res = 0.f; s_lam = 0.f; }
-                __syncthreads();
-                atomicMax(reinterpret_cast<int*>(&s_res), __float_as_int(dmx));
-                atomicMax(reinterpret_cast<int*>(&s_lam), __float_as_int(lmx));
-                __syncthreads();
-                full = done == iters || s_res / fmaxf(1.f, s_lam) <= RES_GATE * tolRel;
-                __syncthreads();
-            }
-            if (full) {
                 if (t == 0) { s_res = 0.f; s_lam = 0.f; }
                 rmax = 0.f;
                 lmax = 0.f;
@@ -751,7 +732,6 @@ __global__ void __launch_bounds__(256) k_batch_sweep_cluster(
     __syncthreads();
 
     float rmax = 0.f, lmax = 0.f;
-    float dmx = 0.f, lmx = 0.f;   // largest |change| and |lambda| of the current sweep
     auto group = [&](int op, int col, int kk) {
         int2 gi = sgi[kk];
         int2 id = sgl[kk];
@@ -792,8 +772,6 @@ __global__ void __launch_bounds__(256) k_batch_sweep_cluster(
                     if (q == 0) nl = fmaxf(nl, 0.f);
                     else { float lim = tail.w * l0; nl = fminf(fmaxf(nl, -lim), lim); }
                     float d = nl - lam[q];
-                    dmx = fmaxf(dmx, fabsf(d));
-                    lmx = fmaxf(lmx, fabsf(nl));
                     if (q == 0) l0 = nl;
                     lam[q] = nl;
                     group_update(a, b, ma * d, mb * d, d, j0, j1, j2, i0, i1);
@@ -849,8 +827,6 @@ __global__ void __launch_bounds__(256) k_batch_sweep_cluster(
     for (int it = 0; it < iters; it++) {
         pass(OP_SWEEP, sym && (it & 1));
         done = it + 1;
-        // (no change gate here: a cluster-wide gate costs as many cluster
-        // barriers as the residual pass it would save)
         if (check > 0 && (done % check == 0 || done == iters)) {
             if (t == 0) { s_res = 0; s_lam = 0; }
             rmax = 0.f;
