@@ -44,9 +44,11 @@ static const int MAXCH = 1024;  // staging chunks per scene
 // Packed record (floats): row r = 0..2 occupies [20r, 20r + 20):
 //   [20r .. 20r+11] J (a.v, a.w, b.v, b.w), [20r+12 .. 20r+14] jinv_a a.w,
 //   [20r+15 .. 20r+17] jinv_b b.w, [20r+18] b, [20r+19] 1/(D + c);
-// [60 .. 62] D of the three rows, [63] mu.  The multipliers live in a
-// separate array in the same slot order, 4 floats per slot (the fourth is
-// padding, so a slot is one 16-byte copy); they are the only per-sweep writes.
+// [60 .. 62] the couplings G10, G20, G21 of the rows (Gqp = J_q M^-1 J_p^T,
+// with the sweep's own M^-1: minv of a pinned body counts as 0), [63] mu.
+// The multipliers live in a separate array in the same slot order, 4 floats
+// per slot (the fourth is padding, so a slot is one 16-byte copy); they are
+// the only per-sweep writes.
 
 __global__ void k_scene_ranges(const DPairs P, int npairs, const int* sceneOf, int nScenes, int* pairOff) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -72,10 +74,30 @@ __global__ void k_batch_pack(DBodies B, DContacts C, int nc, const int* slotOf, 
         double D = C.bD[(3 + q) * cap + c];
         r[20 * q + 18] = (float)C.bD[q * cap + c];
         r[20 * q + 19] = (float)(1.0 / (D + comp));
-        r[60 + q] = (float)D;
         lamf[4 * sl + q] = (float)C.lam[q * cap + c];
     }
     lamf[4 * sl + 3] = 0.f;
+    // row couplings: the change of J_q . dv when row p moves by 1, through the
+    // same delta-v update the sweep applies (linear parts scaled by minv, 0
+    // for a pinned body; angular parts by jinv J.w as stored above)
+    {
+        int ba = C.sb1[c], bb = C.sb2[c];
+        double ma = (B.flags[ba] & F_PINNED) ? 0. : B.minv[ba];
+        double mb = (B.flags[bb] & F_PINNED) ? 0. : B.minv[bb];
+        auto G = [&](int q, int p) {
+            double g = 0.;
+            for (int k = 0; k < 3; k++) {
+                g += ma * C.J[(12 * q + k) * cap + c] * C.J[(12 * p + k) * cap + c];
+                g += C.J[(12 * q + 3 + k) * cap + c] * C.Ia[(3 * p + k) * cap + c];
+                g += mb * C.J[(12 * q + 6 + k) * cap + c] * C.J[(12 * p + 6 + k) * cap + c];
+                g += C.J[(12 * q + 9 + k) * cap + c] * C.Ib[(3 * p + k) * cap + c];
+            }
+            return (float)g;
+        };
+        r[60] = G(1, 0);
+        r[61] = G(2, 0);
+        r[62] = G(2, 1);
+    }
     double mu;
     if (fo) mu = fv;
     else {
@@ -268,10 +290,10 @@ __device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret
 __device__ __forceinline__ float4 sld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 
 // J . dv of one row over the group's two bodies (record layout: a.v a.w b.v b.w
-// in j0..j2), as two independent half sums
+// in j0..j2), summed as a tree of pairs
 __device__ __forceinline__ float group_jdv(const float* a, const float* b, float4 j0, float4 j1, float4 j2) {
-    float sa = j0.x * a[0] + j0.y * a[1] + j0.z * a[2] + j0.w * a[3] + j1.x * a[4] + j1.y * a[5];
-    float sb = j1.z * b[0] + j1.w * b[1] + j2.x * b[2] + j2.y * b[3] + j2.z * b[4] + j2.w * b[5];
+    float sa = (fmaf(j0.y, a[1], j0.x * a[0]) + fmaf(j0.w, a[3], j0.z * a[2])) + fmaf(j1.y, a[5], j1.x * a[4]);
+    float sb = (fmaf(j1.w, b[1], j1.z * b[0]) + fmaf(j2.y, b[3], j2.x * b[2])) + fmaf(j2.w, b[5], j2.z * b[4]);
     return sa + sb;
 }
 
@@ -282,6 +304,47 @@ __device__ __forceinline__ void group_update(float* a, float* b, float la, float
     a[3] += d * i0.x; a[4] += d * i0.y; a[5] += d * i0.z;
     b[0] += lb * j1.z; b[1] += lb * j1.w; b[2] += lb * j2.x;
     b[3] += d * i0.w; b[4] += d * i1.x; b[5] += d * i1.y;
+}
+
+// One contact of a Gauss-Seidel sweep (PGS.java:120-160): the normal row,
+// then the two friction rows boxed by mu times the new normal multiplier.
+// All three rows take J . dv at the contact's start state, and the friction
+// rows add what the earlier rows of the same contact changed, through the
+// couplings G10, G20, G21 of the record.  In exact arithmetic this is the
+// row-by-row update; the dependent chain is one dot product and three scalar
+// updates instead of three dot products.  (D lam - w) / (D + c) is evaluated
+// as lam - (c lam + w) / (D + c), and the relaxation factor (1: plain)
+// scales 1 / (D + c).
+__device__ __forceinline__ void sweep_contact(float* a, float* b, float ma, float mb, const float* R, float* lp,
+                                              float omega, float comp, float relax) {
+    float4 J0[3], J1[3], J2[3], I0[3], I1[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        J0[q] = sld4(R + 20 * q); J1[q] = sld4(R + 20 * q + 4); J2[q] = sld4(R + 20 * q + 8);
+        I0[q] = sld4(R + 20 * q + 12); I1[q] = sld4(R + 20 * q + 16);
+    }
+    const float4 g = sld4(R + 60);
+    const float4 l = sld4(lp);
+    const float lq[3] = {l.x, l.y, l.z};
+    float p[3], k[3], ni[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        p[q] = group_jdv(a, b, J0[q], J1[q], J2[q]);
+        k[q] = fmaf(comp, lq[q], omega * I1[q].z);
+        ni[q] = -relax * I1[q].w;
+    }
+    const float n0 = fmaxf(fmaf(fmaf(omega, p[0], k[0]), ni[0], l.x), 0.f);
+    const float d0 = n0 - l.x;
+    const float lim = g.w * n0;
+    const float n1 = fminf(fmaxf(fmaf(fmaf(omega, fmaf(g.x, d0, p[1]), k[1]), ni[1], l.y), -lim), lim);
+    const float d1 = n1 - l.y;
+    const float n2 =
+        fminf(fmaxf(fmaf(fmaf(omega, fmaf(g.z, d1, fmaf(g.y, d0, p[2])), k[2]), ni[2], l.z), -lim), lim);
+    const float d2 = n2 - l.z;
+    *reinterpret_cast<float4*>(lp) = make_float4(n0, n1, n2, l.w);
+    group_update(a, b, ma * d0, mb * d0, d0, J0[0], J1[0], J2[0], I0[0], I1[0]);
+    group_update(a, b, ma * d1, mb * d1, d1, J0[1], J1[1], J2[1], I0[1], I1[1]);
+    group_update(a, b, ma * d2, mb * d2, d2, J0[2], J1[2], J2[2], I0[2], I1[2]);
 }
 
 // shared-memory layout of the sweep kernel (floats).  The staging arrays
@@ -409,23 +472,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
                     group_update(a, b, ma * lam[q], mb * lam[q], lam[q], j0, j1, j2, i0, i1);
                 }
             } else if (op == OP_SWEEP) {
-                float l0 = lam[0];
-#pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
-                    float4 i0 = sld4(R + 20 * q + 12), i1 = sld4(R + 20 * q + 16);
-                    float jd = group_jdv(a, b, j0, j1, j2);
-                    float D = q == 0 ? tail.x : (q == 1 ? tail.y : tail.z);
-                    float nl = (D * lam[q] - omega * (i1.z + jd)) * i1.w;
-                    nl = lam[q] + relax * (nl - lam[q]);   // over-relaxation (1: plain)
-                    if (q == 0) nl = fmaxf(nl, 0.f);
-                    else { float lim = tail.w * l0; nl = fminf(fmaxf(nl, -lim), lim); }
-                    float d = nl - lam[q];
-                    if (q == 0) l0 = nl;
-                    lam[q] = nl;
-                    group_update(a, b, ma * d, mb * d, d, j0, j1, j2, i0, i1);
-                }
-                lp[0] = lam[0]; lp[1] = lam[1]; lp[2] = lam[2];
+                sweep_contact(a, b, ma, mb, R, lp, omega, comp, relax);
             } else if (op == OP_RES) {
                 // natural-map residual at the current state
 #pragma unroll
@@ -760,23 +807,7 @@ __global__ void __launch_bounds__(256) k_batch_sweep_cluster(
                     group_update(a, b, ma * lam[q], mb * lam[q], lam[q], j0, j1, j2, i0, i1);
                 }
             } else if (op == OP_SWEEP) {
-                float l0 = lam[0];
-#pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
-                    float4 i0 = sld4(R + 20 * q + 12), i1 = sld4(R + 20 * q + 16);
-                    float jd = group_jdv(a, b, j0, j1, j2);
-                    float D = q == 0 ? tail.x : (q == 1 ? tail.y : tail.z);
-                    float nl = (D * lam[q] - omega * (i1.z + jd)) * i1.w;
-                    nl = lam[q] + relax * (nl - lam[q]);   // over-relaxation (1: plain)
-                    if (q == 0) nl = fmaxf(nl, 0.f);
-                    else { float lim = tail.w * l0; nl = fminf(fmaxf(nl, -lim), lim); }
-                    float d = nl - lam[q];
-                    if (q == 0) l0 = nl;
-                    lam[q] = nl;
-                    group_update(a, b, ma * d, mb * d, d, j0, j1, j2, i0, i1);
-                }
-                lp[0] = lam[0]; lp[1] = lam[1]; lp[2] = lam[2];
+                sweep_contact(a, b, ma, mb, R, lp, omega, comp, relax);
             } else if (op == OP_RES) {
 #pragma unroll
                 for (int q = 0; q < 3; q++) {
