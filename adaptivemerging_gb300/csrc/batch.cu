@@ -36,19 +36,25 @@
 namespace am {
 using namespace amd;
 
-static const int REC = 64;      // floats per packed contact record (global)
-static const int RECS = 68;     // shared-memory stride of a staged record (pads banks)
+static const int REC = 28;      // floats per packed contact record (global and shared memory)
+static const int RECS = 28;     // shared-memory stride of a staged record (28 mod 32 spreads banks)
 static const int MAXCB = 64;    // colours per scene
 static const int MAXCH = 1024;  // staging chunks per scene
 
-// Packed record (floats): row r = 0..2 occupies [20r, 20r + 20):
-//   [20r .. 20r+11] J (a.v, a.w, b.v, b.w), [20r+12 .. 20r+14] jinv_a a.w,
-//   [20r+15 .. 20r+17] jinv_b b.w, [20r+18] b, [20r+19] 1/(D + c);
-// [60 .. 62] the couplings G10, G20, G21 of the rows (Gqp = J_q M^-1 J_p^T,
-// with the sweep's own M^-1: minv of a pinned body counts as 0), [63] mu.
-// The multipliers live in a separate array in the same slot order, 4 floats
-// per slot (the fourth is padding, so a slot is one 16-byte copy); they are
-// the only per-sweep writes.
+// Packed record (floats), 7 x 16 bytes:
+//   [0..3]   n  and ra.x      [4..7]   t1 and ra.y      [8..11] t2 and ra.z
+//   [12..15] rb and mu        [16..19] b0 b1 b2 G10     [20..23] 1/(D + c) of the rows, G20
+//   [24]     G21, then padding
+// f = (n, t1, t2) is the contact frame, ra / rb the contact point from the
+// two solve bodies' centres of mass.  The Jacobian rows are those of
+// Contact.computeJacobian (Contact.java:199-255): (-f, f x ra, f, rb x f);
+// the sweep forms them, and jinv J.w, from this and the bodies' inverse
+// inertia, so a record is 112 bytes instead of the 256 of the full rows.
+// Gqp = J_q M^-1 J_p^T are the couplings of the rows (with the sweep's own
+// M^-1: minv and jinv of a pinned body count as 0).  The multipliers live in
+// a separate array in the same slot order, 4 floats per slot (the fourth is
+// padding, so a slot is one 16-byte copy); they are the only per-sweep
+// writes.
 
 __global__ void k_scene_ranges(const DPairs P, int npairs, const int* sceneOf, int nScenes, int* pairOff) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -65,23 +71,30 @@ __global__ void k_batch_pack(DBodies B, DContacts C, int nc, const int* slotOf, 
     int cap = C.cap;
     int sl = slotOf[c];
     float r[REC];
+    for (int k = 0; k < REC; k++) r[k] = 0.f;
+    const int ba = C.sb1[c], bb = C.sb2[c];
     for (int q = 0; q < 3; q++) {
-        for (int k = 0; k < 12; k++) r[20 * q + k] = (float)C.J[(12 * q + k) * cap + c];
-        for (int k = 0; k < 3; k++) {
-            r[20 * q + 12 + k] = (float)C.Ia[(3 * q + k) * cap + c];
-            r[20 * q + 15 + k] = (float)C.Ib[(3 * q + k) * cap + c];
-        }
+        // f_q is the b.v part of row q
+        for (int k = 0; k < 3; k++) r[4 * q + k] = (float)C.J[(12 * q + 6 + k) * cap + c];
         double D = C.bD[(3 + q) * cap + c];
-        r[20 * q + 18] = (float)C.bD[q * cap + c];
-        r[20 * q + 19] = (float)(1.0 / (D + comp));
+        r[16 + q] = (float)C.bD[q * cap + c];
+        r[20 + q] = (float)(1.0 / (D + comp));
         lamf[4 * sl + q] = (float)C.lam[q * cap + c];
     }
     lamf[4 * sl + 3] = 0.f;
-    // row couplings: the change of J_q . dv when row p moves by 1, through the
-    // same delta-v update the sweep applies (linear parts scaled by minv, 0
-    // for a pinned body; angular parts by jinv J.w as stored above)
+    // contact point (stored in body-1 coordinates) from both solve bodies
     {
-        int ba = C.sb1[c], bb = C.sb2[c];
+        const int b1 = C.b1[c];
+        v3 pB = mk(C.f[0 * cap + c], C.f[1 * cap + c], C.f[2 * cap + c]);
+        v3 pW = add(mxv(ldm(B.R + 9 * b1), pB), ldv(B.x + 3 * b1));
+        v3 ra = sub(pW, ldv(B.x + 3 * ba)), rb = sub(pW, ldv(B.x + 3 * bb));
+        r[3] = (float)ra.x; r[7] = (float)ra.y; r[11] = (float)ra.z;
+        r[12] = (float)rb.x; r[13] = (float)rb.y; r[14] = (float)rb.z;
+    }
+    // row couplings: the change of J_q . dv when row p moves by 1, through the
+    // same delta-v update the sweep applies (linear parts scaled by minv,
+    // angular parts by jinv J.w; both 0 for a pinned body)
+    {
         double ma = (B.flags[ba] & F_PINNED) ? 0. : B.minv[ba];
         double mb = (B.flags[bb] & F_PINNED) ? 0. : B.minv[bb];
         auto G = [&](int q, int p) {
@@ -94,9 +107,9 @@ __global__ void k_batch_pack(DBodies B, DContacts C, int nc, const int* slotOf, 
             }
             return (float)g;
         };
-        r[60] = G(1, 0);
-        r[61] = G(2, 0);
-        r[62] = G(2, 1);
+        r[19] = G(1, 0);
+        r[23] = G(2, 0);
+        r[24] = G(2, 1);
     }
     double mu;
     if (fo) mu = fv;
@@ -106,7 +119,7 @@ __global__ void k_batch_pack(DBodies B, DContacts C, int nc, const int* slotOf, 
         else if (f1 > 1. || f2 > 1.) mu = fmax(f1, f2);
         else mu = (f1 + f2) / 2.;
     }
-    r[63] = (float)mu;
+    r[15] = (float)mu;
     float4* dst = reinterpret_cast<float4*>(rec + (size_t)REC * sl);
     for (int k = 0; k < REC / 4; k++) dst[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
 }
@@ -124,7 +137,8 @@ __global__ void k_batch_colour(DBodies B, DContacts C, DPairs P, const int* pair
     extern __shared__ unsigned long long smemq[];
     unsigned long long* bodyMax = smemq;               // [maxBodies] largest uncoloured priority
     unsigned long long* used = smemq + maxBodies;      // [maxBodies] colours taken at the body
-    __shared__ int s_left, s_full, s_cnt[MAXCB + 1];
+    const int CNTB = 16;                 // contact-count buckets for the order within a colour
+    __shared__ int s_left, s_full, s_cnt[MAXCB + 1], s_bkt[MAXCB * CNTB];
     int s = blockIdx.x;
     int g0 = pairOff[s], g1 = pairOff[s + 1];
     int b0 = sceneBodyOff[s], nb = sceneBodyOff[s + 1] - b0;
@@ -177,18 +191,33 @@ __global__ void k_batch_colour(DBodies B, DContacts C, DPairs P, const int* pair
         if (left == 0) break;
     }
     __syncthreads();
+    // Within a colour the groups are ordered by contact count, largest first:
+    // a warp then takes groups of similar length, so its lanes idle less
+    // while the longest group of the warp runs.  (Groups of one colour share
+    // no body the sweep writes, so their order does not change results.)
+    for (int k = t; k < MAXCB * CNTB; k += T) s_bkt[k] = 0;
+    __syncthreads();
+    auto bucket = [&](int g) { return CNTB - 1 - min(P.count[g], CNTB - 1); };
+    for (int g = g0 + t; g < g1; g += T) {
+        int c = colourOf[g];
+        if (c >= 0) atomicAdd(&s_bkt[c * CNTB + bucket(g)], 1);
+    }
+    __syncthreads();
     if (t == 0) {
         if (s_left || s_full) dc->error = AM_E_CAPACITY;
         int ncol = 0;
         for (int k = 0; k < MAXCB; k++) if (s_cnt[k]) ncol = k + 1;
         int run = g0;
-        for (int k = 0; k < ncol; k++) { int n = s_cnt[k]; s_cnt[k] = run; colOff[s * (MAXCB + 1) + k] = run; run += n; }
+        for (int k = 0; k < ncol; k++) {
+            colOff[s * (MAXCB + 1) + k] = run;
+            for (int q = 0; q < CNTB; q++) { int n = s_bkt[k * CNTB + q]; s_bkt[k * CNTB + q] = run; run += n; }
+        }
         for (int k = ncol; k <= MAXCB; k++) colOff[s * (MAXCB + 1) + k] = run;
     }
     __syncthreads();
     for (int g = g0 + t; g < g1; g += T) {
         int c = colourOf[g];
-        if (c >= 0) gOrder[atomicAdd(&s_cnt[c], 1)] = g;
+        if (c >= 0) gOrder[atomicAdd(&s_bkt[c * CNTB + bucket(g)], 1)] = g;
     }
 }
 
@@ -288,22 +317,111 @@ __global__ void k_batch_slots(DContacts C, DPairs P, const int* pairOff, const i
 
 __device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 __device__ __forceinline__ float4 sld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
-
-// J . dv of one row over the group's two bodies (record layout: a.v a.w b.v b.w
-// in j0..j2), summed as a tree of pairs
-__device__ __forceinline__ float group_jdv(const float* a, const float* b, float4 j0, float4 j1, float4 j2) {
-    float sa = (fmaf(j0.y, a[1], j0.x * a[0]) + fmaf(j0.w, a[3], j0.z * a[2])) + fmaf(j1.y, a[5], j1.x * a[4]);
-    float sb = (fmaf(j1.w, b[1], j1.z * b[0]) + fmaf(j2.y, b[3], j2.x * b[2])) + fmaf(j2.w, b[5], j2.z * b[4]);
-    return sa + sb;
+__device__ __forceinline__ long long gtimer() {
+    long long v;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(v));
+    return v;
+}
+__device__ __forceinline__ int smid() {
+    int v;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(v));
+    return v;
+}
+// world inverse inertia of a body as its symmetric part (xx yy zz xy xz yz),
+// 0 for a pinned body
+__device__ __forceinline__ void load_jinv(const DBodies& B, int b, bool pinned, float* o) {
+    const double* J = B.jinv + 9 * (size_t)b;
+    const int idx[6] = {0, 4, 8, 1, 2, 5};
+    for (int k = 0; k < 6; k++) o[k] = pinned ? 0.f : (float)J[idx[k]];
+}
+// solve start and end of a scene and the SM that ran it
+__device__ __forceinline__ void trace_scene(long long* trace, int s, long long t0) {
+    if (!trace) return;
+    trace[3 * s] = t0;
+    trace[3 * s + 1] = gtimer();
+    trace[3 * s + 2] = smid();
 }
 
-// delta-v += (minv J.v, jinv J.w) * d for both bodies (i0, i1 hold jinv J.w)
-__device__ __forceinline__ void group_update(float* a, float* b, float la, float lb, float d, float4 j0, float4 j1,
-                                             float4 j2, float4 i0, float4 i1) {
-    a[0] += la * j0.x; a[1] += la * j0.y; a[2] += la * j0.z;
-    a[3] += d * i0.x; a[4] += d * i0.y; a[5] += d * i0.z;
-    b[0] += lb * j1.z; b[1] += lb * j1.w; b[2] += lb * j2.x;
-    b[3] += d * i0.w; b[4] += d * i1.x; b[5] += d * i1.y;
+// A body pair's state across one group: both bodies' delta-v (v, w), world
+// inverse inertia (symmetric: xx yy zz xy xz yz) and inverse mass (0 for a
+// pinned body, whose delta-v is never written back).
+struct Pair {
+    float a[6], b[6];
+    float ja[6], jb[6];
+    float ma, mb;
+};
+
+// One contact record in registers (layout above).
+struct Rec {
+    float f[3][3];      // n, t1, t2
+    float ra[3], rb[3]; // contact point from each body's centre of mass
+    float bq[3], iq[3]; // b and 1 / (D + c) of the three rows
+    float g10, g20, g21, mu;
+};
+
+__device__ __forceinline__ void load_rec(const float* R, Rec& c) {
+    const float4 q0 = sld4(R), q1 = sld4(R + 4), q2 = sld4(R + 8), q3 = sld4(R + 12), q4 = sld4(R + 16),
+                 q5 = sld4(R + 20), q6 = sld4(R + 24);
+    c.f[0][0] = q0.x; c.f[0][1] = q0.y; c.f[0][2] = q0.z; c.ra[0] = q0.w;
+    c.f[1][0] = q1.x; c.f[1][1] = q1.y; c.f[1][2] = q1.z; c.ra[1] = q1.w;
+    c.f[2][0] = q2.x; c.f[2][1] = q2.y; c.f[2][2] = q2.z; c.ra[2] = q2.w;
+    c.rb[0] = q3.x; c.rb[1] = q3.y; c.rb[2] = q3.z; c.mu = q3.w;
+    c.bq[0] = q4.x; c.bq[1] = q4.y; c.bq[2] = q4.z; c.g10 = q4.w;
+    c.iq[0] = q5.x; c.iq[1] = q5.y; c.iq[2] = q5.z; c.g20 = q5.w;
+    c.g21 = q6.x;
+}
+
+// w x r
+__device__ __forceinline__ void cross3(const float* w, const float* r, float* o) {
+    o[0] = fmaf(w[1], r[2], -w[2] * r[1]);
+    o[1] = fmaf(w[2], r[0], -w[0] * r[2]);
+    o[2] = fmaf(w[0], r[1], -w[1] * r[0]);
+}
+// symmetric matrix (xx yy zz xy xz yz) times v
+__device__ __forceinline__ void symv(const float* m, const float* v, float* o) {
+    o[0] = fmaf(m[4], v[2], fmaf(m[3], v[1], m[0] * v[0]));
+    o[1] = fmaf(m[5], v[2], fmaf(m[1], v[1], m[3] * v[0]));
+    o[2] = fmaf(m[2], v[2], fmaf(m[5], v[1], m[4] * v[0]));
+}
+
+// Velocity of the contact point on body b relative to body a:
+// J_q . dv = f_q . rv for the Jacobian rows of Contact.computeJacobian
+// (-f, f x ra, f, rb x f).
+__device__ __forceinline__ void rel_vel(const Pair& P, const Rec& c, float* rv) {
+    float wa[3], wb[3];
+    cross3(P.a + 3, c.ra, wa);
+    cross3(P.b + 3, c.rb, wb);
+    for (int k = 0; k < 3; k++) rv[k] = (P.b[k] - P.a[k]) + (wb[k] - wa[k]);
+}
+__device__ __forceinline__ float fdot(const float* f, const float* v) {
+    return fmaf(f[2], v[2], fmaf(f[1], v[1], f[0] * v[0]));
+}
+
+// jinv J.w of both bodies for row q: (f_q x ra) and (rb x f_q) mapped by the
+// world inverse inertia
+__device__ __forceinline__ void ang_row(const Pair& P, const Rec& c, int q, float* ia, float* ib) {
+    float u[3], w[3];
+    cross3(c.f[q], c.ra, u);
+    cross3(c.rb, c.f[q], w);
+    symv(P.ja, u, ia);
+    symv(P.jb, w, ib);
+}
+
+// delta-v += M^-1 J^T for the impulse F (world frame, the sum of d_q f_q of
+// the rows): linear parts -ma F and mb F, angular jinv (F x ra), jinv (rb x F)
+__device__ __forceinline__ void pair_impulse(Pair& P, const Rec& c, const float* F) {
+    float u[3], w[3], ia[3], ib[3];
+    cross3(F, c.ra, u);
+    cross3(c.rb, F, w);
+    symv(P.ja, u, ia);
+    symv(P.jb, w, ib);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        P.a[k] = fmaf(-P.ma, F[k], P.a[k]);
+        P.b[k] = fmaf(P.mb, F[k], P.b[k]);
+        P.a[3 + k] += ia[k];
+        P.b[3 + k] += ib[k];
+    }
 }
 
 // One contact of a Gauss-Seidel sweep (PGS.java:120-160): the normal row,
@@ -311,51 +429,97 @@ __device__ __forceinline__ void group_update(float* a, float* b, float la, float
 // All three rows take J . dv at the contact's start state, and the friction
 // rows add what the earlier rows of the same contact changed, through the
 // couplings G10, G20, G21 of the record.  In exact arithmetic this is the
-// row-by-row update; the dependent chain is one dot product and three scalar
-// updates instead of three dot products.  (D lam - w) / (D + c) is evaluated
-// as lam - (c lam + w) / (D + c), and the relaxation factor (1: plain)
-// scales 1 / (D + c).
-__device__ __forceinline__ void sweep_contact(float* a, float* b, float ma, float mb, const float* R, float* lp,
-                                              float omega, float comp, float relax) {
-    float4 J0[3], J1[3], J2[3], I0[3], I1[3];
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-        J0[q] = sld4(R + 20 * q); J1[q] = sld4(R + 20 * q + 4); J2[q] = sld4(R + 20 * q + 8);
-        I0[q] = sld4(R + 20 * q + 12); I1[q] = sld4(R + 20 * q + 16);
-    }
-    const float4 g = sld4(R + 60);
+// row-by-row update; the dependent chain is one relative velocity and three
+// scalar updates instead of three dot products.  The first two rows' changes
+// are applied as one impulse while the third row is computed; the third is
+// applied through its own jinv J.w, formed ahead.  (D lam - w) / (D + c) is
+// evaluated as lam - (c lam + w) / (D + c), and the relaxation factor (1:
+// plain) scales 1 / (D + c).
+__device__ __forceinline__ void sweep_contact(Pair& P, const float* R, float* lp, float omega, float comp,
+                                              float relax) {
+    Rec c;
+    load_rec(R, c);
     const float4 l = sld4(lp);
+    float rv[3];
+    rel_vel(P, c, rv);
     const float lq[3] = {l.x, l.y, l.z};
     float p[3], k[3], ni[3];
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-        p[q] = group_jdv(a, b, J0[q], J1[q], J2[q]);
-        k[q] = fmaf(comp, lq[q], omega * I1[q].z);
-        ni[q] = -relax * I1[q].w;
+        p[q] = fdot(c.f[q], rv);
+        k[q] = fmaf(comp, lq[q], omega * c.bq[q]);
+        ni[q] = -relax * c.iq[q];
     }
     const float n0 = fmaxf(fmaf(fmaf(omega, p[0], k[0]), ni[0], l.x), 0.f);
     const float d0 = n0 - l.x;
-    const float lim = g.w * n0;
-    const float n1 = fminf(fmaxf(fmaf(fmaf(omega, fmaf(g.x, d0, p[1]), k[1]), ni[1], l.y), -lim), lim);
+    const float lim = c.mu * n0;
+    const float n1 = fminf(fmaxf(fmaf(fmaf(omega, fmaf(c.g10, d0, p[1]), k[1]), ni[1], l.y), -lim), lim);
     const float d1 = n1 - l.y;
     const float n2 =
-        fminf(fmaxf(fmaf(fmaf(omega, fmaf(g.z, d1, fmaf(g.y, d0, p[2])), k[2]), ni[2], l.z), -lim), lim);
+        fminf(fmaxf(fmaf(fmaf(omega, fmaf(c.g21, d1, fmaf(c.g20, d0, p[2])), k[2]), ni[2], l.z), -lim), lim);
     const float d2 = n2 - l.z;
     *reinterpret_cast<float4*>(lp) = make_float4(n0, n1, n2, l.w);
-    group_update(a, b, ma * d0, mb * d0, d0, J0[0], J1[0], J2[0], I0[0], I1[0]);
-    group_update(a, b, ma * d1, mb * d1, d1, J0[1], J1[1], J2[1], I0[1], I1[1]);
-    group_update(a, b, ma * d2, mb * d2, d2, J0[2], J1[2], J2[2], I0[2], I1[2]);
+    float F[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) F[q] = fmaf(d2, c.f[2][q], fmaf(d1, c.f[1][q], d0 * c.f[0][q]));
+    pair_impulse(P, c, F);
+}
+
+// PGS.confidentWarmStart: delta-v += M^-1 J^T lambda
+__device__ __forceinline__ void warm_contact(Pair& P, const float* R, const float* lp) {
+    Rec c;
+    load_rec(R, c);
+    const float4 l = sld4(lp);
+    float F[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) F[q] = fmaf(l.z, c.f[2][q], fmaf(l.y, c.f[1][q], l.x * c.f[0][q]));
+    pair_impulse(P, c, F);
+}
+
+// natural-map residual of a contact at the current state:
+// |lambda - proj(lambda - (b + J dv + c lambda) / (D + c))|
+__device__ __forceinline__ void res_contact(const Pair& P, const float* R, const float* lp, float comp, float& rmax,
+                                            float& lmax) {
+    Rec c;
+    load_rec(R, c);
+    const float4 l = sld4(lp);
+    const float lq[3] = {l.x, l.y, l.z};
+    float rv[3];
+    rel_vel(P, c, rv);
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        float w = c.bq[q] + fdot(c.f[q], rv) + comp * lq[q];
+        float z = lq[q] - w * c.iq[q];
+        if (q == 0) z = fmaxf(z, 0.f);
+        else { float lim = c.mu * l.x; z = fminf(fmaxf(z, -lim), lim); }
+        rmax = fmaxf(rmax, fabsf(lq[q] - z));
+        lmax = fmaxf(lmax, fabsf(lq[q]));
+    }
+}
+
+// Contact.updateContactState after the final sweep: broken when the normal
+// multiplier vanished, on edge when a tangential velocity exceeds `slide`
+__device__ __forceinline__ int final_state(const Pair& P, const float* R, const float* lp, float slide) {
+    Rec c;
+    load_rec(R, c);
+    float rv[3];
+    rel_vel(P, c, rv);
+    const float w1 = c.bq[1] + fdot(c.f[1], rv), w2 = c.bq[2] + fdot(c.f[2], rv);
+    if (fabsf(lp[0]) <= 1e-14f) return AM_STATE_BROKEN;
+    if (fabsf(w1) > slide || fabsf(w2) > slide) return AM_STATE_ONEDGE;
+    return AM_STATE_CLEAR;
 }
 
 // shared-memory layout of the sweep kernel (floats).  The staging arrays
 // hold two buffers of `cap` slots each (double buffering of chunks); a
 // resident scene uses both as one buffer of 2 cap slots.
 struct SweepSmem {
-    int dv, mv, rec, lam, gi, gl, total;
+    int dv, mv, ji, rec, lam, gi, gl, total;
     __host__ __device__ SweepSmem(int nbMax, int cap) {
-        dv = 0;
-        mv = 6 * nbMax;
-        rec = (7 * nbMax + 3) & ~3;
+        dv = 0;                // 6 floats per body (even offsets: 8-byte aligned)
+        ji = 6 * nbMax;        // symmetric inverse inertia, 6 floats per body
+        mv = 12 * nbMax;
+        rec = (13 * nbMax + 3) & ~3;
         lam = rec + 2 * cap * RECS;
         gi = lam + 8 * cap;
         gl = gi + 4 * cap;
@@ -382,11 +546,14 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     DBodies B, DContacts C, const int* sceneBodyOff, const int* sceneOrder, const int2* gInfo, const int2* glid,
     const int* chunkK, const int* nChunks, const int* contactOf, const float* __restrict__ rec, float* lamS, int cap,
     int nbMax, int iters, float omega, float comp, float tolRel, int check, float slide, int* sceneSweeps,
-    float* sceneRes, const float* lamAlt, int* sceneFall, int writeBack, int inner, float relax, int sym) {
+    float* sceneRes, const float* lamAlt, int* sceneFall, int writeBack, int inner, float relax, int sym,
+    long long* trace) {
     extern __shared__ float sm[];
     const SweepSmem L(nbMax, cap);
+    const long long tStart = gtimer();
     float* dv = sm + L.dv;
     float* mv = sm + L.mv;
+    float* ji = sm + L.ji;
     float* srec = sm + L.rec;
     float* slam = sm + L.lam;
     int2* sgi = reinterpret_cast<int2*>(sm + L.gi);
@@ -399,19 +566,27 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     const int* ck = chunkK + s * (MAXCH + 1);
     const int nch = nChunks[s];
     const int HEAD = 1 << 30, KMASK = HEAD - 1;
+    // a scene without contacts touches no shared memory (its launch may lay
+    // out none for its bodies)
+    if (nch == 0) {
+        if (!writeBack) return;
+        for (int b = t; b < nb; b += T)
+            for (int k = 0; k < 6; k++) B.dv[6 * (b0 + b) + k] = 0.0;
+        if (t == 0) {
+            sceneSweeps[s] = 0;
+            sceneRes[s] = 0.f;
+            if (sceneFall) sceneFall[s] = 0;
+            trace_scene(trace, s, tStart);
+        }
+        return;
+    }
     // pinned bodies get 0 here, the same test the colouring uses to let groups
     // of one colour share them; their delta-v is never written
     for (int b = t; b < nb; b += T) {
-        mv[b] = (B.flags[b0 + b] & F_PINNED) ? 0.f : (float)B.minv[b0 + b];
+        const bool pin = (B.flags[b0 + b] & F_PINNED) != 0;
+        mv[b] = pin ? 0.f : (float)B.minv[b0 + b];
         for (int k = 0; k < 6; k++) dv[6 * b + k] = 0.f;
-    }
-    if (nch == 0) {
-        if (!writeBack) return;
-        __syncthreads();
-        for (int b = t; b < nb; b += T)
-            for (int k = 0; k < 6; k++) B.dv[6 * (b0 + b) + k] = 0.0;
-        if (t == 0) { sceneSweeps[s] = 0; sceneRes[s] = 0.f; if (sceneFall) sceneFall[s] = 0; }
-        return;
+        load_jinv(B, b0 + b, pin, ji + 6 * b);
     }
     const int kS0 = ck[0] & KMASK, kS1 = ck[nch] & KMASK;
     const int slotS0 = gInfo[kS0].x;
@@ -427,8 +602,8 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         int nsl = e.x + e.y - s0;
         float* R = srec + buf * cap * RECS;
         float* Lm = slam + buf * cap * 4;
-        for (int i = t; i < nsl * 16; i += T) {
-            int sl = i >> 4, q = i & 15;
+        for (int i = t; i < nsl * (REC / 4); i += T) {
+            int sl = i / (REC / 4), q = i - sl * (REC / 4);
             cp_async16(R + sl * RECS + 4 * q, rec + (size_t)(s0 + sl) * REC + 4 * q);
         }
         for (int i = t; i < nsl; i += T) cp_async16(Lm + 4 * i, lamS + 4 * ((size_t)s0 + i));
@@ -452,61 +627,46 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     // one group: its two bodies' delta-v in registers across its contacts;
     // sl0 is the group's first slot in the staging buffer, slA in the scene
     auto group = [&](int op, int sl0, int slA, int cnt, int2 id) {
-        float a[6], b[6];
-        for (int q = 0; q < 6; q++) { a[q] = dv[6 * id.x + q]; b[q] = dv[6 * id.y + q]; }
-        float ma = mv[id.x], mb = mv[id.y];
+        Pair P;
+        {   // 8-byte aligned: 6 floats per body from an even offset
+            const float2* da = reinterpret_cast<const float2*>(dv + 6 * id.x);
+            const float2* db = reinterpret_cast<const float2*>(dv + 6 * id.y);
+            const float2* ja = reinterpret_cast<const float2*>(ji + 6 * id.x);
+            const float2* jb = reinterpret_cast<const float2*>(ji + 6 * id.y);
+            for (int q = 0; q < 3; q++) {
+                float2 u = da[q], v = db[q], x = ja[q], y = jb[q];
+                P.a[2 * q] = u.x; P.a[2 * q + 1] = u.y;
+                P.b[2 * q] = v.x; P.b[2 * q + 1] = v.y;
+                P.ja[2 * q] = x.x; P.ja[2 * q + 1] = x.y;
+                P.jb[2 * q] = y.x; P.jb[2 * q + 1] = y.y;
+            }
+        }
+        P.ma = mv[id.x];
+        P.mb = mv[id.y];
         // sweeps may pass over a group's contacts `inner` times: Gauss-Seidel
         // on the body pair's own block before the sweep moves on
         const int reps = op == OP_SWEEP ? inner : 1;
-        for (int jj = 0; jj < reps * cnt; jj++) {
-            const int j = jj % cnt;
+        for (int rep = 0; rep < reps; rep++)
+        for (int j = 0; j < cnt; j++) {
             const float* R = srec + (sl0 + j) * RECS;
             float* lp = slam + 4 * (sl0 + j);
-            float4 tail = sld4(R + 60);
-            float lam[3] = {lp[0], lp[1], lp[2]};
-            if (op == OP_WARM) {   // PGS.confidentWarmStart
-#pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
-                    float4 i0 = sld4(R + 20 * q + 12), i1 = sld4(R + 20 * q + 16);
-                    group_update(a, b, ma * lam[q], mb * lam[q], lam[q], j0, j1, j2, i0, i1);
-                }
+            if (op == OP_WARM) {
+                warm_contact(P, R, lp);
             } else if (op == OP_SWEEP) {
-                sweep_contact(a, b, ma, mb, R, lp, omega, comp, relax);
+                sweep_contact(P, R, lp, omega, comp, relax);
             } else if (op == OP_RES) {
-                // natural-map residual at the current state
-#pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
-                    float4 i1 = sld4(R + 20 * q + 16);
-                    float w = i1.z + group_jdv(a, b, j0, j1, j2) + comp * lam[q];
-                    float z = lam[q] - w * i1.w;
-                    if (q == 0) z = fmaxf(z, 0.f);
-                    else { float lim = tail.w * lam[0]; z = fminf(fmaxf(z, -lim), lim); }
-                    rmax = fmaxf(rmax, fabsf(lam[q] - z));
-                    lmax = fmaxf(lmax, fabsf(lam[q]));
-                }
+                res_contact(P, R, lp, comp, rmax, lmax);
             } else {
-                // contact state after the final sweep (Contact.updateContactState)
-                float wt[2];
-#pragma unroll
-                for (int q = 1; q < 3; q++) {
-                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
-                    float4 i1 = sld4(R + 20 * q + 16);
-                    wt[q - 1] = i1.z + group_jdv(a, b, j0, j1, j2);
-                }
                 int c = contactOf[slA + j];
-                int st;
-                if (fabsf(lam[0]) <= 1e-14f) st = AM_STATE_BROKEN;
-                else if (fabsf(wt[0]) > slide || fabsf(wt[1]) > slide) st = AM_STATE_ONEDGE;
-                else st = AM_STATE_CLEAR;
-                C.state[c] = st;
-                for (int q = 0; q < 3; q++) C.lam[q * C.cap + c] = (double)lam[q];
+                C.state[c] = final_state(P, R, lp, slide);
+                for (int q = 0; q < 3; q++) C.lam[q * C.cap + c] = (double)lp[q];
             }
         }
         if (op == OP_WARM || op == OP_SWEEP) {
-            if (ma != 0.f) for (int q = 0; q < 6; q++) dv[6 * id.x + q] = a[q];
-            if (mb != 0.f) for (int q = 0; q < 6; q++) dv[6 * id.y + q] = b[q];
+            float2* da = reinterpret_cast<float2*>(dv + 6 * id.x);
+            float2* db = reinterpret_cast<float2*>(dv + 6 * id.y);
+            if (P.ma != 0.f) for (int q = 0; q < 3; q++) da[q] = make_float2(P.a[2 * q], P.a[2 * q + 1]);
+            if (P.mb != 0.f) for (int q = 0; q < 3; q++) db[q] = make_float2(P.b[2 * q], P.b[2 * q + 1]);
         }
     };
     // one pass of `op` over the scene, colour by colour.  Resident: the whole
@@ -515,7 +675,9 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     // in while chunk i is processed, and (sweeps only) a chunk's multipliers
     // go back to global memory after it.
     // colour heads of the chunk list (bit 30 marks a chunk that starts a colour)
-    __shared__ int s_head[MAXCB + 1];
+    // (and, for a resident scene, each colour's first group, kept here so a
+    // sweep reads no global memory)
+    __shared__ int s_head[MAXCB + 1], s_kh[MAXCB + 1];
     __shared__ int s_nhead;
     if (t == 0) {
         int nh = 0;
@@ -523,6 +685,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
             if ((ck[i] & HEAD) && nh < MAXCB) s_head[nh++] = i;
         s_head[nh] = nch;
         s_nhead = nh;
+        for (int h = 0; h <= nh; h++) s_kh[h] = ck[s_head[h]] & KMASK;
     }
     __syncthreads();
     const int nhead = s_nhead;
@@ -530,7 +693,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         if (resident) {
             for (int hh = 0; hh < nhead; hh++) {
                 int h = rev ? nhead - 1 - hh : hh;
-                int k0 = ck[s_head[h]] & KMASK, k1 = ck[s_head[h + 1]] & KMASK;
+                int k0 = s_kh[h], k1 = s_kh[h + 1];
                 for (int k = k0 + t; k < k1; k += T) {
                     int2 gi = sgi[k - kS0];
                     group(op, gi.x - slotS0, gi.x, gi.y, sgl[k - kS0]);
@@ -623,7 +786,11 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     pass(OP_FINAL, false);
     for (int b = t; b < nb; b += T)
         for (int k = 0; k < 6; k++) B.dv[6 * (b0 + b) + k] = (double)dv[6 * b + k];
-    if (t == 0) { sceneSweeps[s] = total; sceneRes[s] = res; }
+    if (t == 0) {
+        sceneSweeps[s] = total;
+        sceneRes[s] = res;
+        trace_scene(trace, s, tStart);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -654,6 +821,18 @@ __device__ __forceinline__ float2 dsm_ld2(unsigned a) {
     asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
     return v;
 }
+__device__ __forceinline__ float4 dsm_ld4(unsigned a) {
+    float4 v;
+    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(a)
+                 : "memory");
+    return v;
+}
+__device__ __forceinline__ void dsm_st4(unsigned a, float x, float y, float z, float w) {
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(x), "f"(y), "f"(z), "f"(w)
+                 : "memory");
+}
 __device__ __forceinline__ void dsm_st2(unsigned a, float x, float y) {
     asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(x), "f"(y) : "memory");
 }
@@ -673,9 +852,9 @@ struct ClusterSmem {
     int dv, mv, rec, lam, gi, gl, total;
     __host__ __device__ ClusterSmem(int nbMax, int K, int cap) {
         int own = (nbMax + K - 1) / K;
-        dv = 0;
-        mv = 6 * own;
-        rec = (6 * own + nbMax + 3) & ~3;
+        dv = 0;               // 12 floats per owned body: delta-v, then symmetric jinv
+        mv = 12 * own;
+        rec = (12 * own + nbMax + 3) & ~3;
         lam = rec + cap * RECS;
         gi = lam + 4 * cap;
         gl = gi + 2 * cap;
@@ -683,13 +862,14 @@ struct ClusterSmem {
     }
 };
 
-__global__ void __launch_bounds__(256) k_batch_sweep_cluster(
+__global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
     DBodies B, DContacts C, const int* sceneBodyOff, const int* bigScenes, const int* colOff, const int2* gInfo,
     const int2* glid, const int* contactOf, const float* __restrict__ rec, const float* lamS, int cap, int nbMax,
     int K, int iters, float omega, float comp, float tolRel, int check, float slide, int* sceneSweeps,
-    float* sceneRes, int inner, int writeBack, float relax, int sym) {
+    float* sceneRes, int inner, int writeBack, float relax, int sym, long long* trace) {
     extern __shared__ float sm[];
     const ClusterSmem L(nbMax, K, cap);
+    const long long tStart = gtimer();
     float* dvOwn = sm + L.dv;
     float* mv = sm + L.mv;
     float* srec = sm + L.rec;
@@ -708,7 +888,12 @@ __global__ void __launch_bounds__(256) k_batch_sweep_cluster(
     const int* co = colOff + s * (MAXCB + 1);
     const int ncol = scene_colours(co);
     for (int b = t; b < nb; b += T) mv[b] = (B.flags[b0 + b] & F_PINNED) ? 0.f : (float)B.minv[b0 + b];
-    for (int i = t; i < 6 * own; i += T) dvOwn[i] = 0.f;
+    for (int i = t; i < own; i += T) {
+        int lb = i * K + (int)rank;
+        for (int k = 0; k < 6; k++) dvOwn[12 * i + k] = 0.f;
+        if (lb < nb) load_jinv(B, b0 + lb, (B.flags[b0 + lb] & F_PINNED) != 0, dvOwn + 12 * i + 6);
+        else for (int k = 0; k < 6; k++) dvOwn[12 * i + 6 + k] = 0.f;
+    }
     // this CTA's part of every colour: groups starting in window `rank`
     for (int col = t; col < ncol; col += T) {
         int k0 = co[col], k1 = co[col + 1];
@@ -764,8 +949,8 @@ __global__ void __launch_bounds__(256) k_batch_sweep_cluster(
         int nsl = e.x + e.y - gs0;
         float* R = srec + s_sb[col] * RECS;
         float* Lm = slam + 4 * s_sb[col];
-        for (int i = t; i < nsl * 16; i += T) {
-            int sl = i >> 4, q = i & 15;
+        for (int i = t; i < nsl * (REC / 4); i += T) {
+            int sl = i / (REC / 4), q = i - sl * (REC / 4);
             cp_async16(R + sl * RECS + 4 * q, rec + (size_t)(gs0 + sl) * REC + 4 * q);
         }
         for (int i = t; i < nsl; i += T) cp_async16(Lm + 4 * i, lamS + 4 * ((size_t)gs0 + i));
@@ -783,63 +968,41 @@ __global__ void __launch_bounds__(256) k_batch_sweep_cluster(
         int2 gi = sgi[kk];
         int2 id = sgl[kk];
         int sl0 = s_sb[col] + (gi.x - s_gs[col]);
-        unsigned pa = dsm_map(dvOwn + 6 * (id.x / K), id.x % K);
-        unsigned pb = dsm_map(dvOwn + 6 * (id.y / K), id.y % K);
-        float a[6], b[6];
-        for (int q = 0; q < 3; q++) {
-            float2 u = dsm_ld2(pa + 8 * q), v = dsm_ld2(pb + 8 * q);
-            a[2 * q] = u.x; a[2 * q + 1] = u.y; b[2 * q] = v.x; b[2 * q + 1] = v.y;
+        // each body's delta-v and inverse inertia live with its owner CTA
+        unsigned pa = dsm_map(dvOwn + 12 * (id.x / K), id.x % K);
+        unsigned pb = dsm_map(dvOwn + 12 * (id.y / K), id.y % K);
+        Pair P;
+        {
+            float4 u0 = dsm_ld4(pa), u1 = dsm_ld4(pa + 16), u2 = dsm_ld4(pa + 32);
+            float4 v0 = dsm_ld4(pb), v1 = dsm_ld4(pb + 16), v2 = dsm_ld4(pb + 32);
+            P.a[0] = u0.x; P.a[1] = u0.y; P.a[2] = u0.z; P.a[3] = u0.w; P.a[4] = u1.x; P.a[5] = u1.y;
+            P.ja[0] = u1.z; P.ja[1] = u1.w; P.ja[2] = u2.x; P.ja[3] = u2.y; P.ja[4] = u2.z; P.ja[5] = u2.w;
+            P.b[0] = v0.x; P.b[1] = v0.y; P.b[2] = v0.z; P.b[3] = v0.w; P.b[4] = v1.x; P.b[5] = v1.y;
+            P.jb[0] = v1.z; P.jb[1] = v1.w; P.jb[2] = v2.x; P.jb[3] = v2.y; P.jb[4] = v2.z; P.jb[5] = v2.w;
         }
-        float ma = mv[id.x], mb = mv[id.y];
+        P.ma = mv[id.x];
+        P.mb = mv[id.y];
         const int cnt = gi.y;
         const int reps = op == OP_SWEEP ? inner : 1;
         for (int jj = 0; jj < reps * cnt; jj++) {
-            const int j = jj % cnt;
+            const int j = reps == 1 ? jj : jj % cnt;
             const float* R = srec + (sl0 + j) * RECS;
             float* lp = slam + 4 * (sl0 + j);
-            float4 tail = sld4(R + 60);
-            float lam[3] = {lp[0], lp[1], lp[2]};
             if (op == OP_WARM) {
-#pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
-                    float4 i0 = sld4(R + 20 * q + 12), i1 = sld4(R + 20 * q + 16);
-                    group_update(a, b, ma * lam[q], mb * lam[q], lam[q], j0, j1, j2, i0, i1);
-                }
+                warm_contact(P, R, lp);
             } else if (op == OP_SWEEP) {
-                sweep_contact(a, b, ma, mb, R, lp, omega, comp, relax);
+                sweep_contact(P, R, lp, omega, comp, relax);
             } else if (op == OP_RES) {
-#pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
-                    float4 i1 = sld4(R + 20 * q + 16);
-                    float w = i1.z + group_jdv(a, b, j0, j1, j2) + comp * lam[q];
-                    float z = lam[q] - w * i1.w;
-                    if (q == 0) z = fmaxf(z, 0.f);
-                    else { float lim = tail.w * lam[0]; z = fminf(fmaxf(z, -lim), lim); }
-                    rmax = fmaxf(rmax, fabsf(lam[q] - z));
-                    lmax = fmaxf(lmax, fabsf(lam[q]));
-                }
+                res_contact(P, R, lp, comp, rmax, lmax);
             } else {
-                float wt[2];
-#pragma unroll
-                for (int q = 1; q < 3; q++) {
-                    float4 j0 = sld4(R + 20 * q), j1 = sld4(R + 20 * q + 4), j2 = sld4(R + 20 * q + 8);
-                    float4 i1 = sld4(R + 20 * q + 16);
-                    wt[q - 1] = i1.z + group_jdv(a, b, j0, j1, j2);
-                }
                 int c = contactOf[gi.x + j];
-                int st;
-                if (fabsf(lam[0]) <= 1e-14f) st = AM_STATE_BROKEN;
-                else if (fabsf(wt[0]) > slide || fabsf(wt[1]) > slide) st = AM_STATE_ONEDGE;
-                else st = AM_STATE_CLEAR;
-                C.state[c] = st;
-                for (int q = 0; q < 3; q++) C.lam[q * C.cap + c] = (double)lam[q];
+                C.state[c] = final_state(P, R, lp, slide);
+                for (int q = 0; q < 3; q++) C.lam[q * C.cap + c] = (double)lp[q];
             }
         }
         if (op == OP_WARM || op == OP_SWEEP) {
-            if (ma != 0.f) for (int q = 0; q < 3; q++) dsm_st2(pa + 8 * q, a[2 * q], a[2 * q + 1]);
-            if (mb != 0.f) for (int q = 0; q < 3; q++) dsm_st2(pb + 8 * q, b[2 * q], b[2 * q + 1]);
+            if (P.ma != 0.f) { dsm_st4(pa, P.a[0], P.a[1], P.a[2], P.a[3]); dsm_st2(pa + 16, P.a[4], P.a[5]); }
+            if (P.mb != 0.f) { dsm_st4(pb, P.b[0], P.b[1], P.b[2], P.b[3]); dsm_st2(pb + 16, P.b[4], P.b[5]); }
         }
     };
     // colours in order, a cluster barrier after each one that writes delta-v
@@ -886,9 +1049,13 @@ __global__ void __launch_bounds__(256) k_batch_sweep_cluster(
         for (int i = t; i < own; i += T) {
             int lb = i * K + (int)rank;
             if (lb < nb)
-                for (int k = 0; k < 6; k++) B.dv[6 * (b0 + lb) + k] = (double)dvOwn[6 * i + k];
+                for (int k = 0; k < 6; k++) B.dv[6 * (b0 + lb) + k] = (double)dvOwn[12 * i + k];
         }
-        if (rank == 0 && t == 0) { sceneSweeps[s] = done; sceneRes[s] = res; }
+        if (rank == 0 && t == 0) {
+            sceneSweeps[s] = done;
+            sceneRes[s] = res;
+            trace_scene(trace, s, tStart);
+        }
     }
     cluster_sync_all();   // no CTA leaves while another may still read its shared memory
 }
@@ -900,14 +1067,14 @@ const void* batch_sweep_kernel() { return (const void*)k_batch_sweep; }
 size_t batch_sweep_smem(int nbMax, int cap) { return sizeof(float) * (size_t)SweepSmem(nbMax, cap).total; }
 
 int Ctx::batchLaunchSweep(int threads, int cap, int iters, float tol, int check, float* lamStart, const float* lamAlt,
-                          int* fall, int writeBack, int nGrid, const int* order) {
+                          int* fall, int writeBack, int nGrid, const int* order, int nbMax, cudaStream_t strm) {
     double comp = P.enable_compliance ? P.compliance : 0.;
-    size_t ssm = batch_sweep_smem(maxSceneBodies, cap);
+    size_t ssm = batch_sweep_smem(nbMax, cap);
     if (nGrid <= 0) return AM_OK;
-    k_batch_sweep<<<nGrid, threads, ssm, stream>>>(
+    k_batch_sweep<<<nGrid, threads, ssm, strm>>>(
         B, C[cur], sceneBodyOffDev, order, bGInfo, bLid, bChunkK, bNChunks, bContactOf, bRec, lamStart, cap,
-        maxSceneBodies, iters, (float)P.omega, (float)comp, tol, check, (float)P.sliding_threshold, bSweeps, bRes,
-        lamAlt, fall, writeBack, batchInner, (float)batchRelax, batchSym);
+        nbMax, iters, (float)P.omega, (float)comp, tol, check, (float)P.sliding_threshold, bSweeps, bRes,
+        lamAlt, fall, writeBack, batchInner, (float)batchRelax, batchSym, writeBack ? bTrace : nullptr);
     AM_LAUNCHED(1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { err = std::string("sweep launch: ") + cudaGetErrorString(e); return AM_E_CUDA; }
@@ -918,37 +1085,71 @@ int Ctx::batchLaunchSweep(int threads, int cap, int iters, float tol, int check,
 // whose records fit the one-CTA kernel's two buffers stays there; a larger one
 // goes to the cluster kernel with the smallest K in {2, 4, 8} whose CTAs can
 // hold it (its slots / K plus one group per colour within each CTA's
-// capacity), otherwise it streams through the one-CTA kernel.  Every list is
+// capacity), otherwise it streams through the one-CTA kernel.  Small scenes
+// that fit a size class go to that class's launch instead, whose CTAs are
+// sized for the class, so several of them share an SM.  Every list is
 // ordered costliest first (contacts x sweeps of the previous step) and they
-// are stored one after another: one-CTA scenes, then clusters of 2, 4 and 8.
+// are stored one after another: one-CTA scenes, the size classes, then
+// clusters of 2, 4 and 8.  Each launch lays out shared memory for the most
+// bodies among its scenes (and a cluster launch for its largest part).
 static const int CLUSTER_K[3] = {2, 4, 8};
+// Size classes of resident scenes: staging capacity (a scene of at most
+// 2 x cap slots and 4 x cap bodies whose layout fits shared memory) and CTA
+// size of each class launch.
+static const int NCLASS = 8;
+static const int CLASS_CAP[NCLASS] = {16, 32, 64, 128, 192, 256, 384, 512};
+static const int CLASS_THREADS[NCLASS] = {32, 32, 64, 128, 192, 256, 384, 512};
 
 int Ctx::batchSplit(int cap, bool useCluster) {
     int S = nScenes;
     hSmall.clear();
     for (auto& v : hBigK) v.clear();
-    if (useCluster) {
-        std::vector<int2> sz(S);
-        cudaMemcpyAsync(sz.data(), bSceneSize, sizeof(int2) * S, cudaMemcpyDeviceToHost, stream);
-        int r = syncErr();
-        if (r) return r;
-        for (int sc = 0; sc < S; sc++) {
-            int need = -1;
-            if (sz[sc].x > 2 * cap)
-                for (int q = 0; q < 3; q++) {
-                    int K = CLUSTER_K[q];
-                    if ((sz[sc].x + K - 1) / K + sz[sc].y <= clusterCap &&
-                        batch_cluster_smem(maxSceneBodies, K, clusterCap) <= batchSmemLimit) {
-                        need = q;
-                        break;
-                    }
-                }
-            if (need >= 0) hBigK[need].push_back(sc);
-            else hSmall.push_back(sc);
+    for (auto& v : hClass) v.clear();
+    std::vector<int2> sz(S);
+    cudaMemcpyAsync(sz.data(), bSceneSize, sizeof(int2) * S, cudaMemcpyDeviceToHost, stream);
+    int r = syncErr();
+    if (r) return r;
+    smallNb = 0;
+    for (int q = 0; q < NCLASS; q++) classNb[q] = 0;
+    for (int q = 0; q < 3; q++) { bigNb[q] = 0; bigCap[q] = 0; }
+    for (int sc = 0; sc < S; sc++) {
+        const int nb = hSceneNb[sc], slots = sz[sc].x;
+        // the smallest size class that holds the scene resident (a scene
+        // without contacts touches no shared memory: the smallest class)
+        int c = -1;
+        if (batchClasses)
+            for (int q = 0; q < NCLASS && c < 0; q++)
+                if (slots == 0 || (slots <= 2 * CLASS_CAP[q] && nb <= 4 * CLASS_CAP[q] &&
+                                   batch_sweep_smem(nb, CLASS_CAP[q]) <= batchSmemLimit))
+                    c = q;
+        if (c >= 0) {
+            hClass[c].push_back(sc);
+            if (slots > 0) classNb[c] = std::max(classNb[c], nb);
+            continue;
         }
-    } else {
-        for (int sc = 0; sc < S; sc++) hSmall.push_back(sc);
+        if (useCluster && (batchClasses || slots > 2 * cap)) {
+            int need = -1;
+            for (int q = 0; q < 3; q++) {
+                int K = CLUSTER_K[q];
+                int per = (slots + K - 1) / K + sz[sc].y;
+                if (per <= clusterCap && batch_cluster_smem(nb, K, clusterCap) <= clusterSmemLimit) {
+                    need = q;
+                    break;
+                }
+            }
+            if (need >= 0) {
+                int K = CLUSTER_K[need];
+                hBigK[need].push_back(sc);
+                bigNb[need] = std::max(bigNb[need], nb);
+                bigCap[need] = std::max(bigCap[need], (slots + K - 1) / K + sz[sc].y);
+                continue;
+            }
+        }
+        hSmall.push_back(sc);
+        if (slots > 0) smallNb = std::max(smallNb, nb);
     }
+    // a cluster launch stages what its largest scene needs (multiple of 32)
+    for (int q = 0; q < 3; q++) bigCap[q] = std::min(clusterCap, (bigCap[q] + 31) & ~31);
     auto byCost = [&](int a, int b) {
         long long ca = (size_t)a < lastCost.size() ? lastCost[a] : 0, cb = (size_t)b < lastCost.size() ? lastCost[b] : 0;
         return ca > cb;
@@ -956,6 +1157,10 @@ int Ctx::batchSplit(int cap, bool useCluster) {
     std::vector<int> all;
     std::stable_sort(hSmall.begin(), hSmall.end(), byCost);
     all.insert(all.end(), hSmall.begin(), hSmall.end());
+    for (auto& v : hClass) {
+        std::stable_sort(v.begin(), v.end(), byCost);
+        all.insert(all.end(), v.begin(), v.end());
+    }
     for (auto& v : hBigK) {
         std::stable_sort(v.begin(), v.end(), byCost);
         all.insert(all.end(), v.begin(), v.end());
@@ -977,56 +1182,88 @@ int Ctx::batchClusterMaxK() const {
     return k;
 }
 
-// one cluster launch per cluster size in use, each on its own stream
-int Ctx::batchLaunchClusters(int iters, float tol, int check, int writeBack) {
+// the cluster launch of cluster size CLUSTER_K[q] over `list`
+int Ctx::batchLaunchCluster(int q, const int* list, int nBig, cudaStream_t strm, int iters, float tol, int check,
+                            int writeBack) {
     double comp = P.enable_compliance ? P.compliance : 0.;
-    const int* list = bSceneOrderBuf + hSmall.size();
-    for (int q = 0; q < 3; q++) {
-        int nBig = (int)hBigK[q].size();
-        if (nBig == 0) continue;
-        int K = CLUSTER_K[q];
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(nBig * K);
-        cfg.blockDim = dim3(256);
-        cfg.dynamicSmemBytes = batch_cluster_smem(maxSceneBodies, K, clusterCap);
-        cfg.stream = clusterStream[q];
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = K;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        cudaError_t e = cudaLaunchKernelEx(&cfg, k_batch_sweep_cluster, B, C[cur], (const int*)sceneBodyOffDev, list,
-                                           (const int*)bColOff, (const int2*)bGInfo, (const int2*)bLid,
-                                           (const int*)bContactOf, (const float*)bRec, (const float*)bLam, clusterCap,
-                                           maxSceneBodies, K, iters, (float)P.omega, (float)comp, tol, check,
-                                           (float)P.sliding_threshold, bSweeps, bRes, batchInner, writeBack,
-                                           (float)batchRelax, batchSym);
-        AM_LAUNCHED(1);
-        if (e == cudaSuccess) e = cudaGetLastError();
-        if (e != cudaSuccess) { err = std::string("cluster sweep launch: ") + cudaGetErrorString(e); return AM_E_CUDA; }
-        list += nBig;
-    }
+    int K = CLUSTER_K[q];
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nBig * K);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = batch_cluster_smem(bigNb[q], K, bigCap[q]);
+    cfg.stream = strm;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = K;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_batch_sweep_cluster, B, C[cur], (const int*)sceneBodyOffDev, list,
+                                       (const int*)bColOff, (const int2*)bGInfo, (const int2*)bLid,
+                                       (const int*)bContactOf, (const float*)bRec, (const float*)bLam, bigCap[q],
+                                       bigNb[q], K, iters, (float)P.omega, (float)comp, tol, check,
+                                       (float)P.sliding_threshold, bSweeps, bRes, batchInner, writeBack,
+                                       (float)batchRelax, batchSym, writeBack ? bTrace : nullptr);
+    AM_LAUNCHED(1);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) { err = std::string("cluster sweep launch: ") + cudaGetErrorString(e); return AM_E_CUDA; }
     return AM_OK;
 }
 
-// the one-CTA kernel on `stream` with the cluster launches forked beside it
+// Every launch of the solve (the one-CTA kernel, the size classes, the
+// cluster sizes) on its own stream, forked from and joined back into the
+// context stream.  A scene's solve time is about its sweeps x (1024 +
+// contacts) of the previous step (the cost).  Each launch's list (costliest
+// first) is cut in two: the scenes within 40 % of the largest cost of the
+// batch, which bound the solve and must start at once, and the rest.  The
+// first parts of all launches are issued before the second parts, each group
+// costliest launch first, on streams of descending priority, so the CTA
+// scheduler starts the long solves first across launches.
 int Ctx::batchLaunchAll(int threads, int cap, int iters, float tol, int check, float* lamStart, const float* lamAlt,
                         int writeBack) {
-    int r;
+    struct L { int kind, q, n, tier; const int* list; long long cost; };
+    std::vector<L> ls;
+    long long top = 0;
+    for (long long c : lastCost) top = std::max(top, c);
+    const long long cut = (top * 2) / 5;
+    auto costAt = [&](int sc) { return (size_t)sc < lastCost.size() ? lastCost[sc] : 0; };
+    const int* list = bSceneOrderBuf;
+    auto add = [&](int kind, int q, const std::vector<int>& v) {
+        int n = (int)v.size(), n0 = 0;
+        while (n0 < n && costAt(v[n0]) >= cut) n0++;
+        if (n0 > 0) ls.push_back({kind, q, n0, 0, list, costAt(v[0])});
+        if (n > n0) ls.push_back({kind, q, n - n0, 1, list + n0, costAt(v[n0])});
+        list += n;
+    };
+    add(0, 0, hSmall);
+    for (int q = 0; q < NCLASS; q++) add(1, q, hClass[q]);
+    for (int q = 0; q < 3; q++) add(2, q, hBigK[q]);
+    std::stable_sort(ls.begin(), ls.end(), [](const L& a, const L& b) {
+        return a.tier != b.tier ? a.tier < b.tier : a.cost > b.cost;
+    });
+    if ((int)ls.size() > NPOOL) { err = "too many sweep launches"; return AM_E_STATE; }
     cudaEventRecord(evFork, stream);
-    for (int q = 0; q < 3; q++)
-        if (!hBigK[q].empty()) cudaStreamWaitEvent(clusterStream[q], evFork, 0);
-    if ((r = batchLaunchClusters(iters, tol, check, writeBack))) return r;
-    if ((r = batchLaunchSweep(threads, cap, iters, tol, check, lamStart, lamAlt, writeBack ? bFall : nullptr,
-                              writeBack, (int)hSmall.size(), bSceneOrderBuf)))
-        return r;
-    for (int q = 0; q < 3; q++)
-        if (!hBigK[q].empty()) {
-            cudaEventRecord(evJoin[q], clusterStream[q]);
-            cudaStreamWaitEvent(stream, evJoin[q], 0);
-        }
+    int* fall = writeBack ? bFall : nullptr;
+    for (size_t i = 0; i < ls.size(); i++) {
+        cudaStream_t st = pool[i];
+        cudaStreamWaitEvent(st, evFork, 0);
+        int r;
+        const L& l = ls[i];
+        if (l.kind == 0)
+            r = batchLaunchSweep(threads, cap, iters, tol, check, lamStart, lamAlt, fall, writeBack, l.n, l.list,
+                                 smallNb, st);
+        else if (l.kind == 1)
+            r = batchLaunchSweep(CLASS_THREADS[l.q], CLASS_CAP[l.q], iters, tol, check, lamStart, lamAlt, fall,
+                                 writeBack, l.n, l.list, classNb[l.q], st);
+        else
+            r = batchLaunchCluster(l.q, l.list, l.n, st, iters, tol, check, writeBack);
+        if (r) return r;
+    }
+    for (size_t i = 0; i < ls.size(); i++) {
+        cudaEventRecord(poolJoin[i], pool[i]);
+        cudaStreamWaitEvent(stream, poolJoin[i], 0);
+    }
     return AM_OK;
 }
 
@@ -1148,6 +1385,8 @@ int Ctx::batchStats() {
         long long ncs = sw[s] > 0 ? cs[s] / sw[s] : 0;
         resid += (ncs > 0 && ncs <= 2 * batchCap) ? 1 : 0;
     }
+    for (auto& v : hClass)
+        for (int s : v) resid += (sw[s] > 0 && cs[s] > 0) ? 1 : 0;
     for (int s = 0; s < nScenes; s++) {
         tot += sw[s];
         mx = std::max(mx, sw[s]);
@@ -1160,8 +1399,12 @@ int Ctx::batchStats() {
     batchSweepsTotal = tot;
     batchContactSweepsLast = 0;
     for (long long v : cs) batchContactSweepsLast += v;
-    // cost of every scene (contacts x sweeps) orders the next solve's launches
-    lastCost = cs;
+    // expected solve time of every scene orders the next solve's launches:
+    // sweeps x (1024 + contacts), as the time of a sweep grows slowly with
+    // the scene's size
+    lastCost.assign(nScenes, 0);
+    for (int sc = 0; sc < nScenes; sc++)
+        if (sw[sc] > 0) lastCost[sc] = cs[sc] + 1024LL * sw[sc];
     for (int sc = 0; sc < nScenes; sc++)
         if (sw[sc] < 0) { err = "a scene did not fit its cluster"; return AM_E_CAPACITY; }
     stats.sweeps = mx;
@@ -1218,9 +1461,10 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     bCS = nullptr;
     if (alloc(&sceneOfDev, cap) || alloc(&sceneBodyOffDev, n + 1) || alloc(&topEnd, all.n_bodies) ||
         alloc(&bPairOff, n + 1) || alloc(&bColOff, (size_t)n * (MAXCB + 1)) || alloc(&bSweeps, n) || alloc(&bRes, n) ||
-        alloc(&bFall, n))
+        alloc(&bFall, n) || alloc(&bTrace, 3 * (size_t)n))
         return AM_E_CUDA;
     cudaMemsetAsync(bFall, 0, sizeof(int) * n, stream);
+    cudaMemsetAsync(bTrace, 0, sizeof(long long) * 3 * n, stream);
     cudaMemcpyAsync(sceneOfDev, sOf.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(sceneBodyOffDev, bodyOff.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(topEnd, tEnd.data(), sizeof(int) * all.n_bodies, cudaMemcpyHostToDevice, stream);
@@ -1229,18 +1473,20 @@ int Ctx::setBatch(const am_scene* sc, int n) {
         return AM_E_CUDA;
     bSceneOrder = nullptr;
     lastCost.clear();
-    // the cluster launches carry the longest bins: their streams get the
-    // highest priority so their CTAs are scheduled ahead of the one-CTA kernel's
+    // streams of the sweep launches, in descending priority (the costliest
+    // launch of a solve takes the first)
     int prLeast = 0, prGreatest = 0;
     cudaDeviceGetStreamPriorityRange(&prLeast, &prGreatest);
-    for (int q = 0; q < 3; q++) {
-        if (!clusterStream[q] &&
-            cudaStreamCreateWithPriority(&clusterStream[q], cudaStreamNonBlocking, prGreatest) != cudaSuccess) {
-            err = "cluster stream";
+    for (int q = 0; q < NPOOL; q++) {
+        int pr = std::min(prLeast, prGreatest + q);
+        if (!pool[q] && cudaStreamCreateWithPriority(&pool[q], cudaStreamNonBlocking, pr) != cudaSuccess) {
+            err = "sweep stream";
             return AM_E_CUDA;
         }
-        if (!evJoin[q]) cudaEventCreateWithFlags(&evJoin[q], cudaEventDisableTiming);
+        if (!poolJoin[q]) cudaEventCreateWithFlags(&poolJoin[q], cudaEventDisableTiming);
     }
+    hSceneNb.assign(n, 0);
+    for (int q = 0; q < n; q++) hSceneNb[q] = bodyOff[q + 1] - bodyOff[q];
     if (!evFork) cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming);
     // dynamic shared memory the sweep may take: the opt-in limit less its static part
     int dev = 0, optin = 0;
@@ -1254,13 +1500,20 @@ int Ctx::setBatch(const am_scene* sc, int n) {
         err = "sweep kernel shared-memory limit";
         return AM_E_CUDA;
     }
+    // every sweep launch asks for the largest shared-memory carveout, so CTAs
+    // of the size classes and clusters can share an SM
+    cudaFuncSetAttribute(batch_sweep_kernel(), cudaFuncAttributePreferredSharedMemoryCarveout,
+                         (int)cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute((const void*)k_batch_sweep_cluster, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         (int)cudaSharedmemCarveoutMaxShared);
     // cluster kernel: the largest staging capacity (multiple of 32, at most
-    // 640 records) that fits for K = 2
+    // 1024 records) that fits for K = 2
     cudaFuncAttributes fc;
     clusterUsable = false;
     if (cudaFuncGetAttributes(&fc, (const void*)k_batch_sweep_cluster) == cudaSuccess) {
         size_t lim = (size_t)optin > fc.sharedSizeBytes ? optin - fc.sharedSizeBytes : 0;
-        clusterCap = clusterCapUser > 0 ? clusterCapUser : 640;
+        clusterSmemLimit = lim;
+        clusterCap = clusterCapUser > 0 ? clusterCapUser : 1024;
         while (clusterCap > 64 && batch_cluster_smem(maxSceneBodies, 2, clusterCap) > lim) clusterCap -= 32;
         if (batch_cluster_smem(maxSceneBodies, 2, clusterCap) <= lim &&
             cudaFuncSetAttribute((const void*)k_batch_sweep_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1269,7 +1522,7 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     }
     clusterEnabled = clusterAllowed && clusterUsable;
     size_t csm = 2 * sizeof(unsigned long long) * (size_t)maxSceneBodies;
-    if (csm > 48 * 1024 &&
+    if (csm > 40 * 1024 &&   // the kernel's static shared memory (4.4 KB) counts against the 48 KB default
         cudaFuncSetAttribute((const void*)k_batch_colour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm) !=
             cudaSuccess) {
         err = "a scene has too many bodies for the batched colouring's shared memory";

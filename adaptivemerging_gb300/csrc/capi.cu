@@ -224,6 +224,12 @@ int32_t am_set_batch_clusters(void* ctx, int32_t enable) {
     return AM_OK;
 }
 
+int32_t am_set_batch_size_classes(void* ctx, int32_t enable) {
+    if (!ctx) return AM_E_ARG;
+    ((Ctx*)ctx)->batchClasses = enable != 0;
+    return AM_OK;
+}
+
 int32_t am_set_batch_cluster_stage(void* ctx, int32_t slots) {
     if (!ctx || slots < 0 || (slots && (slots < 64 || slots % 32))) return AM_E_ARG;
     ((Ctx*)ctx)->clusterCapUser = slots;
@@ -264,6 +270,27 @@ int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, in
     if (fell_back) cudaMemcpyAsync(fell_back, c->bFall, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream);
     if (colours) return c->batchColours(colours);
     return c->syncErr();
+}
+
+int32_t am_get_batch_scene_times(void* ctx, int64_t* start_ns, int64_t* end_ns, int32_t* sm) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->nScenes || !c->bTrace) return AM_E_STATE;
+    int n = c->nScenes;
+    std::vector<long long> tr(3 * (size_t)n);
+    cudaMemcpyAsync(tr.data(), c->bTrace, sizeof(long long) * tr.size(), cudaMemcpyDeviceToHost, c->stream);
+    int r = c->syncErr();
+    if (r) return r;
+    long long t0 = 0;
+    bool any = false;
+    for (int s = 0; s < n; s++)
+        if (tr[3 * s] > 0 && (!any || tr[3 * s] < t0)) { t0 = tr[3 * s]; any = true; }
+    for (int s = 0; s < n; s++) {
+        if (start_ns) start_ns[s] = tr[3 * s] > 0 ? tr[3 * s] - t0 : 0;
+        if (end_ns) end_ns[s] = tr[3 * s] > 0 ? tr[3 * s + 1] - t0 : 0;
+        if (sm) sm[s] = (int32_t)tr[3 * s + 2];
+    }
+    return AM_OK;
 }
 
 int32_t am_learned_collect(void* ctx, int32_t enable, int32_t capacity) {

@@ -249,17 +249,28 @@ struct Ctx {
     int batchResident = 0;       // scenes solved with all records in shared memory, last step
     size_t batchSmemLimit = 0;   // dynamic shared memory the sweep kernel may use
     int batchInner = 1;          // passes over a body pair's contacts per sweep
+    int batchClasses = 1;        // small scenes in size-class launches (0: all in the one-CTA launch)
     double batchRelax = 1.0;     // over-relaxation of the batched sweep (1: plain projected Gauss-Seidel)
     int batchSym = 0;            // 1: odd sweeps walk the colours backwards
     // scenes larger than one CTA's shared memory: thread-block clusters
     int2* bSceneSize = nullptr;  // per scene: slots, one group per colour (split overhead)
+    long long* bTrace = nullptr; // per scene, last solve: start and end (device timer, ns), SM of the (first) CTA
     std::vector<int> hSmall, hBigK[3];   // one-CTA scenes; clusters of 2, 4, 8 CTAs
+    // small resident scenes in size classes: one launch per class, each with
+    // shared memory and CTA size for its largest scene, so several CTAs share
+    // an SM
+    std::vector<int> hClass[8];
+    std::vector<int> hSceneNb;           // bodies per scene
+    int smallNb = 0, classNb[8] = {};    // largest scene (bodies) of each launch
+    int bigNb[3] = {0, 0, 0}, bigCap[3] = {0, 0, 0};
+    size_t clusterSmemLimit = 0;
     std::vector<long long> lastCost;
     int clusterCap = 0;
     int clusterCapUser = 0;      // cluster staging capacity fixed by the caller (0: largest that fits)
     bool clusterEnabled = false, clusterAllowed = true, clusterUsable = false;
-    cudaStream_t clusterStream[3] = {nullptr, nullptr, nullptr};
-    cudaEvent_t evFork = nullptr, evJoin[3] = {nullptr, nullptr, nullptr};
+    static const int NPOOL = 24;         // sweep launches: one-CTA, 8 size classes, 3 cluster sizes; two parts each
+    cudaStream_t pool[NPOOL] = {};
+    cudaEvent_t evFork = nullptr, poolJoin[NPOOL] = {};
     float* bLam = nullptr;
     int bRecCap = 0;
     int* bColour = nullptr;
@@ -387,9 +398,10 @@ struct Ctx {
     int batchColours(int* out);
     int batchLayout(int cap);
     int batchLaunchSweep(int threads, int cap, int iters, float tol, int check, float* lamStart, const float* lamAlt,
-                         int* fall, int writeBack, int nGrid, const int* order);
+                         int* fall, int writeBack, int nGrid, const int* order, int nbMax, cudaStream_t strm);
     int batchSplit(int cap, bool useCluster);
-    int batchLaunchClusters(int iters, float tol, int check, int writeBack);
+    int batchLaunchCluster(int q, const int* list, int nBig, cudaStream_t strm, int iters, float tol, int check,
+                           int writeBack);
     int batchLaunchAll(int threads, int cap, int iters, float tol, int check, float* lamStart, const float* lamAlt,
                        int writeBack);
     int batchClusterScenes() const;

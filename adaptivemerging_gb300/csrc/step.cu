@@ -315,11 +315,11 @@ void Ctx::release() {
     flagStageCap = 0;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
-    for (int q = 0; q < 3; q++) {
-        if (clusterStream[q]) { cudaStreamSynchronize(clusterStream[q]); cudaStreamDestroy(clusterStream[q]); }
-        clusterStream[q] = nullptr;
-        if (evJoin[q]) cudaEventDestroy(evJoin[q]);
-        evJoin[q] = nullptr;
+    for (int q = 0; q < NPOOL; q++) {
+        if (pool[q]) { cudaStreamSynchronize(pool[q]); cudaStreamDestroy(pool[q]); }
+        pool[q] = nullptr;
+        if (poolJoin[q]) cudaEventDestroy(poolJoin[q]);
+        poolJoin[q] = nullptr;
     }
     if (evFork) cudaEventDestroy(evFork);
     evFork = nullptr;

@@ -19,9 +19,9 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libam.so")
 EXPORTS = [
     "am_params_default", "am_create", "am_destroy", "am_last_error", "am_set_params", "am_set_scene",
     "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
-    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats", "am_set_residual_target",
+    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats", "am_get_batch_scene_times", "am_set_residual_target",
     "am_set_batch_local_sweeps", "am_set_batch_clusters", "am_set_batch_stage", "am_set_batch_relaxation",
-    "am_set_batch_cluster_stage",
+    "am_set_batch_cluster_stage", "am_set_batch_size_classes",
     "am_learned_collect", "am_learned_train", "am_learned_use", "am_learned_scope", "am_learned_weights", "am_learned_info",
     "am_learned_grad", "am_learned_infer", "am_learned_infer_noalloc",
 ]
@@ -67,9 +67,11 @@ def lib():
         fp = C.POINTER(C.c_float)
         ip = C.POINTER(C.c_int32)
         L.am_get_batch_scene_stats.argtypes = [vp, ip, fp, ip, ip]
+        L.am_get_batch_scene_times.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), ip]
         L.am_set_residual_target.argtypes = [vp, C.c_double, C.c_int32]
         L.am_set_batch_local_sweeps.argtypes = [vp, C.c_int32]
         L.am_set_batch_clusters.argtypes = [vp, C.c_int32]
+        L.am_set_batch_size_classes.argtypes = [vp, C.c_int32]
         L.am_set_batch_stage.argtypes = [vp, C.c_int32]
         L.am_set_batch_cluster_stage.argtypes = [vp, C.c_int32]
         L.am_set_batch_relaxation.argtypes = [vp, C.c_double, C.c_int32]
@@ -128,6 +130,9 @@ class BatchSystem:
     def set_clusters(self, enable=True):
         self._check(lib().am_set_batch_clusters(self.h, int(enable)))
 
+    def set_size_classes(self, enable=True):
+        self._check(lib().am_set_batch_size_classes(self.h, int(enable)))
+
     def set_local_sweeps(self, passes):
         self._check(lib().am_set_batch_local_sweeps(self.h, passes))
 
@@ -141,6 +146,18 @@ class BatchSystem:
         self._check(lib().am_get_batch_scene_stats(self.h, sw.ctypes.data_as(ip), rs.ctypes.data_as(C.POINTER(C.c_float)),
                                                    fb.ctypes.data_as(ip), nc.ctypes.data_as(ip)))
         return {"sweeps": sw, "residual": rs, "fell_back": fb, "colours": nc}
+
+    def scene_times(self):
+        """Per scene, last solve: start and end of its sweep CTA in ns
+        (relative to the earliest start) and the SM it ran on."""
+        n = len(self.scenes)
+        t0 = np.zeros(n, np.int64)
+        t1 = np.zeros(n, np.int64)
+        sm = np.zeros(n, np.int32)
+        i64 = C.POINTER(C.c_int64)
+        self._check(lib().am_get_batch_scene_times(self.h, t0.ctypes.data_as(i64), t1.ctypes.data_as(i64),
+                                                   sm.ctypes.data_as(C.POINTER(C.c_int32))))
+        return {"start_ns": t0, "end_ns": t1, "sm": sm}
 
     # learned warm start
     def learned_collect(self, enable=True, capacity=2_000_000):

@@ -223,13 +223,13 @@ int32_t am_get_stats(void* ctx, am_solve_stats* out);
  * Batched scenes (no reference counterpart: the reference simulates one
  * scene).  n independent scenes are loaded into one context; am_step then
  * advances all of them (collision per scene; in the solve one CTA per scene,
- * or a thread-block cluster of 2-8 CTAs for a scene too large for one CTA's
- * shared memory).  Body ids in readbacks are global: scene s's body i is at
+ * launched in size classes, or a thread-block cluster of 2-8 CTAs for a scene
+ * too large for one CTA's shared memory).  Body ids in readbacks are global: scene s's body i is at
  * (number of bodies of scenes < s) + i.  Merging must be off.  The batched
  * solve runs in FP32 with delta-v in shared memory and stops each scene when
  * its relative natural-map residual is <= residual_target (checked every
  * check_every sweeps) or after am_params.iterations sweeps.  A scene whose
- * bodies do not fit one CTA's shared memory (about 7000 bodies) is refused
+ * bodies do not fit one CTA's shared memory (about 4000 bodies) is refused
  * with AM_E_CAPACITY.
  */
 typedef struct am_batch_stats {
@@ -255,11 +255,17 @@ int32_t am_set_batch_local_sweeps(void* ctx, int32_t passes);
 /* 1 (default): scenes too large for one CTA's shared memory are solved by a
  * thread-block cluster of 2-8 CTAs; 0: they stream through one CTA. */
 int32_t am_set_batch_clusters(void* ctx, int32_t enable);
+/* 1 (default): every scene that fits one CTA's shared memory is solved by one
+ * of the size-class launches, whose CTAs are sized for the class (small ones
+ * several to an SM); 0: such scenes share the one-CTA launch, whose staging
+ * capacity is autotuned.  Results are the same either way.  No reference
+ * counterpart. */
+int32_t am_set_batch_size_classes(void* ctx, int32_t enable);
 /* contact records per shared-memory staging buffer of the one-CTA kernel
  * (a multiple of 32, at least 64; 0 = autotuned) */
 int32_t am_set_batch_stage(void* ctx, int32_t slots);
 /* contact records each CTA of a cluster holds (a multiple of 32, at least 64;
- * 0 = the largest that fits, at most 640); takes effect at the next am_set_batch */
+ * 0 = the largest that fits, at most 1024); takes effect at the next am_set_batch */
 int32_t am_set_batch_cluster_stage(void* ctx, int32_t slots);
 /* batched sweep variants with the same fixed point (no reference counterpart):
  * over-relaxation factor in (0, 2) applied before the projection (1 = plain
@@ -273,6 +279,10 @@ int32_t am_set_residual_target(void* ctx, double residual_target, int32_t check_
 /* per-scene figures of the last step (arrays of n_scenes; NULL skips one):
  * sweeps, relative residual, learned start fell back, colours of the contact groups */
 int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, int32_t* fell_back, int32_t* colours);
+/* per scene, last batched solve: start and end of its sweep kernel CTA (ns,
+ * relative to the earliest start) and the SM it ran on (a cluster: its first
+ * CTA).  Any pointer may be null.  No reference counterpart. */
+int32_t am_get_batch_scene_times(void* ctx, int64_t* start_ns, int64_t* end_ns, int32_t* sm);
 
 /*
  * Learned warm start for the batched solve (no reference counterpart).  An

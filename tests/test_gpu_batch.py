@@ -134,21 +134,24 @@ def test_cluster_path_converges_to_oracle(gpu_lib):
 
 def test_results_do_not_depend_on_kernel_shape(gpu_lib):
     """A batch stepped with the residual target gives bit-identical states
-    whatever CTA size, staging capacity and cluster use it runs with (the
-    scenes stop at the same check and the per-group arithmetic is shared)."""
+    whatever CTA size, staging capacity, size classes and cluster use it runs
+    with (the scenes stop at the same check and the per-group arithmetic is
+    shared)."""
     from adaptivemerging_gb300 import native
-    sc = [scenes.bin_scene(n, 500 + n, gap=0.01) for n in (40, 300, 900, 1500)]
+    sc = [scenes.bin_scene(n, 500 + n, gap=0.01) for n in (25, 40, 120, 300, 900, 1500)]
     P = params(friction_override=0, iterations=3000)
     runs = []
-    for threads, stage, clusters in ((128, 64, True), (256, 256, True), (512, 128, False)):
+    for threads, stage, clusters, classes in ((128, 64, True, True), (256, 256, True, False),
+                                              (512, 128, False, True), (256, 256, True, True)):
         g = native.BatchSystem(sc, P, threads=threads, residual_target=1e-6, check_every=10)
         g.set_stage(stage)
         g.set_clusters(clusters)
+        g.set_size_classes(classes)
         for _ in range(25):
             g.step(DT)
         runs.append((g.bodies()["x"], g.contacts()["lambda"], g.batch_stats().cluster_scenes))
         g.close()
-    assert runs[0][2] > 0 and runs[2][2] == 0
+    assert runs[1][2] > 0 and runs[2][2] == 0
     for x, lam, _ in runs[1:]:
         assert np.array_equal(x, runs[0][0]) and np.array_equal(lam, runs[0][1])
 
