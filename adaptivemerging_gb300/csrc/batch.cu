@@ -234,7 +234,8 @@ __device__ __forceinline__ int scene_colours(const int* co) {
 __global__ void k_batch_slots(DContacts C, DPairs P, const int* pairOff, const int* gOrder, const int* colOff,
                               const int* sceneBodyOff, int nc, int npairs, int cap, int2* gInfo, int2* glid,
                               int* slotOf, int* contactOf, int* chunkK, int* nChunks, int2* sceneSize,
-                              DCount* dc) {
+                              int* lidOf, int* bodyOf, int* sceneActive, DCount* dc) {
+    extern __shared__ int s_lid[];   // [bodies of the scene]: active flag, then compact id (-1: inactive)
     __shared__ int s_carry, s_maxcnt, s_warp[32], s_colch[MAXCB + 1];
     const unsigned FULL = 0xffffffffu;
     int s = blockIdx.x, t = threadIdx.x, T = blockDim.x;
@@ -280,10 +281,61 @@ __global__ void k_batch_slots(DContacts C, DPairs P, const int* pairOff, const i
         if (t == 0) s_carry += s_warp[nw - 1];
         __syncthreads();
     }
-    int maxc = s_maxcnt;
+    const int maxc = s_maxcnt, nslots = s_carry;
+    // Active bodies (those in some group of the scene) get compact ids in
+    // body order: the sweep keeps delta-v, inverse mass and inertia only for
+    // them, and a body without contacts gets delta-v 0.
+    {
+        const int nb = sceneBodyOff[s + 1] - b0;
+        for (int b = t; b < nb; b += T) s_lid[b] = 0;
+        __syncthreads();
+        for (int k = g0 + t; k < kEnd; k += T) {
+            int2 l = glid[k];
+            s_lid[l.x] = 1;
+            s_lid[l.y] = 1;
+        }
+        __syncthreads();
+        if (t == 0) s_carry = 0;
+        __syncthreads();
+        for (int base = 0; base < nb; base += T) {
+            int b = base + t;
+            int f = b < nb ? s_lid[b] : 0;
+            int x = f;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(FULL, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) s_warp[w] = x;
+            __syncthreads();
+            if (w == 0) {
+                int v = lane < nw ? s_warp[lane] : 0;
+                for (int o = 1; o < 32; o <<= 1) {
+                    int y = __shfl_up_sync(FULL, v, o);
+                    if (lane >= o) v += y;
+                }
+                if (lane < nw) s_warp[lane] = v;
+            }
+            __syncthreads();
+            int id = s_carry + (w ? s_warp[w - 1] : 0) + x - f;
+            if (b < nb) {
+                s_lid[b] = f ? id : -1;
+                lidOf[b0 + b] = f ? id : -1;
+                if (f) bodyOf[b0 + id] = b0 + b;
+            }
+            __syncthreads();
+            if (t == 0) s_carry += s_warp[nw - 1];
+            __syncthreads();
+        }
+        if (t == 0) sceneActive[s] = s_carry;
+        for (int k = g0 + t; k < kEnd; k += T) {
+            int2 l = glid[k];
+            glid[k] = make_int2(s_lid[l.x], s_lid[l.y]);
+        }
+        __syncthreads();
+    }
     // slots of the scene, and the most a split of every colour into equal
     // slot windows can add to one part (one group per colour)
-    if (t == 0) sceneSize[s] = make_int2(s_carry, ncol * maxc);
+    if (t == 0) sceneSize[s] = make_int2(nslots, ncol * maxc);
     int win = cap - maxc;
     if (win < maxc || win <= 0) {   // a group larger than half the staging buffer
         if (t == 0) { dc->error = AM_E_CAPACITY; nChunks[s] = 0; }
@@ -377,11 +429,12 @@ __device__ __forceinline__ void cross3(const float* w, const float* r, float* o)
     o[1] = fmaf(w[2], r[0], -w[0] * r[2]);
     o[2] = fmaf(w[0], r[1], -w[1] * r[0]);
 }
-// symmetric matrix (xx yy zz xy xz yz) times v
-__device__ __forceinline__ void symv(const float* m, const float* v, float* o) {
-    o[0] = fmaf(m[4], v[2], fmaf(m[3], v[1], m[0] * v[0]));
-    o[1] = fmaf(m[5], v[2], fmaf(m[1], v[1], m[3] * v[0]));
-    o[2] = fmaf(m[2], v[2], fmaf(m[5], v[1], m[4] * v[0]));
+// o += symmetric matrix (xx yy zz xy xz yz) times v, accumulated inside the
+// FMA chain
+__device__ __forceinline__ void symv_acc(const float* m, const float* v, float* o) {
+    o[0] = fmaf(m[4], v[2], fmaf(m[3], v[1], fmaf(m[0], v[0], o[0])));
+    o[1] = fmaf(m[5], v[2], fmaf(m[1], v[1], fmaf(m[3], v[0], o[1])));
+    o[2] = fmaf(m[2], v[2], fmaf(m[5], v[1], fmaf(m[4], v[0], o[2])));
 }
 
 // Velocity of the contact point on body b relative to body a:
@@ -397,30 +450,18 @@ __device__ __forceinline__ float fdot(const float* f, const float* v) {
     return fmaf(f[2], v[2], fmaf(f[1], v[1], f[0] * v[0]));
 }
 
-// jinv J.w of both bodies for row q: (f_q x ra) and (rb x f_q) mapped by the
-// world inverse inertia
-__device__ __forceinline__ void ang_row(const Pair& P, const Rec& c, int q, float* ia, float* ib) {
-    float u[3], w[3];
-    cross3(c.f[q], c.ra, u);
-    cross3(c.rb, c.f[q], w);
-    symv(P.ja, u, ia);
-    symv(P.jb, w, ib);
-}
-
 // delta-v += M^-1 J^T for the impulse F (world frame, the sum of d_q f_q of
 // the rows): linear parts -ma F and mb F, angular jinv (F x ra), jinv (rb x F)
 __device__ __forceinline__ void pair_impulse(Pair& P, const Rec& c, const float* F) {
-    float u[3], w[3], ia[3], ib[3];
+    float u[3], w[3];
     cross3(F, c.ra, u);
     cross3(c.rb, F, w);
-    symv(P.ja, u, ia);
-    symv(P.jb, w, ib);
+    symv_acc(P.ja, u, P.a + 3);
+    symv_acc(P.jb, w, P.b + 3);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         P.a[k] = fmaf(-P.ma, F[k], P.a[k]);
         P.b[k] = fmaf(P.mb, F[k], P.b[k]);
-        P.a[3 + k] += ia[k];
-        P.b[3 + k] += ib[k];
     }
 }
 
@@ -429,10 +470,9 @@ __device__ __forceinline__ void pair_impulse(Pair& P, const Rec& c, const float*
 // All three rows take J . dv at the contact's start state, and the friction
 // rows add what the earlier rows of the same contact changed, through the
 // couplings G10, G20, G21 of the record.  In exact arithmetic this is the
-// row-by-row update; the dependent chain is one relative velocity and three
-// scalar updates instead of three dot products.  The first two rows' changes
-// are applied as one impulse while the third row is computed; the third is
-// applied through its own jinv J.w, formed ahead.  (D lam - w) / (D + c) is
+// row-by-row update; the dependent chain is one relative velocity, three
+// scalar updates and one impulse (the three rows' changes applied together)
+// instead of three dot products and three updates.  (D lam - w) / (D + c) is
 // evaluated as lam - (c lam + w) / (D + c), and the relaxation factor (1:
 // plain) scales 1 / (D + c).
 __device__ __forceinline__ void sweep_contact(Pair& P, const float* R, float* lp, float omega, float comp,
@@ -443,20 +483,23 @@ __device__ __forceinline__ void sweep_contact(Pair& P, const float* R, float* lp
     float rv[3];
     rel_vel(P, c, rv);
     const float lq[3] = {l.x, l.y, l.z};
-    float p[3], k[3], ni[3];
+    // row q unclamped: lam_q + ni_q (k_q + omega (p_q + sum_p G_qp d_p)), with
+    // ni = -relax / (D + c) and k = c lam + omega b; the base at the start state
+    // and the coupling factors are formed off the dependent chain
+    float base[3], ni[3];
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-        p[q] = fdot(c.f[q], rv);
-        k[q] = fmaf(comp, lq[q], omega * c.bq[q]);
         ni[q] = -relax * c.iq[q];
+        const float k = fmaf(comp, lq[q], omega * c.bq[q]);
+        base[q] = fmaf(ni[q], fmaf(omega, fdot(c.f[q], rv), k), lq[q]);
     }
-    const float n0 = fmaxf(fmaf(fmaf(omega, p[0], k[0]), ni[0], l.x), 0.f);
+    const float c10 = ni[1] * omega * c.g10, c20 = ni[2] * omega * c.g20, c21 = ni[2] * omega * c.g21;
+    const float n0 = fmaxf(base[0], 0.f);
     const float d0 = n0 - l.x;
     const float lim = c.mu * n0;
-    const float n1 = fminf(fmaxf(fmaf(fmaf(omega, fmaf(c.g10, d0, p[1]), k[1]), ni[1], l.y), -lim), lim);
+    const float n1 = fminf(fmaxf(fmaf(c10, d0, base[1]), -lim), lim);
     const float d1 = n1 - l.y;
-    const float n2 =
-        fminf(fmaxf(fmaf(fmaf(omega, fmaf(c.g21, d1, fmaf(c.g20, d0, p[2])), k[2]), ni[2], l.z), -lim), lim);
+    const float n2 = fminf(fmaxf(fmaf(c21, d1, fmaf(c20, d0, base[2])), -lim), lim);
     const float d2 = n2 - l.z;
     *reinterpret_cast<float4*>(lp) = make_float4(n0, n1, n2, l.w);
     float F[3];
@@ -547,7 +590,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     const int* chunkK, const int* nChunks, const int* contactOf, const float* __restrict__ rec, float* lamS, int cap,
     int nbMax, int iters, float omega, float comp, float tolRel, int check, float slide, int* sceneSweeps,
     float* sceneRes, const float* lamAlt, int* sceneFall, int writeBack, int inner, float relax, int sym,
-    long long* trace) {
+    long long* trace, const int* lidOf, const int* bodyOf, const int* sceneActive) {
     extern __shared__ float sm[];
     const SweepSmem L(nbMax, cap);
     const long long tStart = gtimer();
@@ -580,13 +623,16 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         }
         return;
     }
-    // pinned bodies get 0 here, the same test the colouring uses to let groups
-    // of one colour share them; their delta-v is never written
-    for (int b = t; b < nb; b += T) {
-        const bool pin = (B.flags[b0 + b] & F_PINNED) != 0;
-        mv[b] = pin ? 0.f : (float)B.minv[b0 + b];
+    // the scene's active bodies (compact ids).  Pinned bodies get 0 here, the
+    // same test the colouring uses to let groups of one colour share them;
+    // their delta-v is never written
+    const int nbA = sceneActive[s];
+    for (int b = t; b < nbA; b += T) {
+        const int gb = bodyOf[b0 + b];
+        const bool pin = (B.flags[gb] & F_PINNED) != 0;
+        mv[b] = pin ? 0.f : (float)B.minv[gb];
         for (int k = 0; k < 6; k++) dv[6 * b + k] = 0.f;
-        load_jinv(B, b0 + b, pin, ji + 6 * b);
+        load_jinv(B, gb, pin, ji + 6 * b);
     }
     const int kS0 = ck[0] & KMASK, kS1 = ck[nch] & KMASK;
     const int slotS0 = gInfo[kS0].x;
@@ -751,7 +797,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
                 for (int i = t; i < nslots * 4; i += T) slam[i] = lamAlt[(size_t)slotS0 * 4 + i];
             else
                 for (int i = t; i < nslots * 4; i += T) lamS[(size_t)slotS0 * 4 + i] = lamAlt[(size_t)slotS0 * 4 + i];
-            for (int b = t; b < nb; b += T)
+            for (int b = t; b < nbA; b += T)
                 for (int k = 0; k < 6; k++) dv[6 * b + k] = 0.f;
             if (t == 0 && sceneFall) sceneFall[s] = 1;
             __syncthreads();
@@ -784,8 +830,10 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     }
     if (!writeBack) return;   // autotuner trial: results are discarded
     pass(OP_FINAL, false);
-    for (int b = t; b < nb; b += T)
-        for (int k = 0; k < 6; k++) B.dv[6 * (b0 + b) + k] = (double)dv[6 * b + k];
+    for (int b = t; b < nb; b += T) {
+        const int l = lidOf[b0 + b];
+        for (int k = 0; k < 6; k++) B.dv[6 * (b0 + b) + k] = l >= 0 ? (double)dv[6 * l + k] : 0.0;
+    }
     if (t == 0) {
         sceneSweeps[s] = total;
         sceneRes[s] = res;
@@ -866,7 +914,8 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
     DBodies B, DContacts C, const int* sceneBodyOff, const int* bigScenes, const int* colOff, const int2* gInfo,
     const int2* glid, const int* contactOf, const float* __restrict__ rec, const float* lamS, int cap, int nbMax,
     int K, int iters, float omega, float comp, float tolRel, int check, float slide, int* sceneSweeps,
-    float* sceneRes, int inner, int writeBack, float relax, int sym, long long* trace) {
+    float* sceneRes, int inner, int writeBack, float relax, int sym, long long* trace, const int* lidOf,
+    const int* bodyOf, const int* sceneActive) {
     extern __shared__ float sm[];
     const ClusterSmem L(nbMax, K, cap);
     const long long tStart = gtimer();
@@ -884,15 +933,23 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
     const int s = bigScenes[blockIdx.x / K];
     const int t = threadIdx.x, T = blockDim.x;
     const int b0 = sceneBodyOff[s], nb = sceneBodyOff[s + 1] - b0;
-    const int own = (nb + K - 1) / K;
+    const int nbA = sceneActive[s];     // active bodies (compact ids); owner of id b: CTA b % K
+    const int own = (nbA + K - 1) / K;
     const int* co = colOff + s * (MAXCB + 1);
     const int ncol = scene_colours(co);
-    for (int b = t; b < nb; b += T) mv[b] = (B.flags[b0 + b] & F_PINNED) ? 0.f : (float)B.minv[b0 + b];
+    for (int b = t; b < nbA; b += T) {
+        const int gb = bodyOf[b0 + b];
+        mv[b] = (B.flags[gb] & F_PINNED) ? 0.f : (float)B.minv[gb];
+    }
     for (int i = t; i < own; i += T) {
         int lb = i * K + (int)rank;
         for (int k = 0; k < 6; k++) dvOwn[12 * i + k] = 0.f;
-        if (lb < nb) load_jinv(B, b0 + lb, (B.flags[b0 + lb] & F_PINNED) != 0, dvOwn + 12 * i + 6);
-        else for (int k = 0; k < 6; k++) dvOwn[12 * i + 6 + k] = 0.f;
+        if (lb < nbA) {
+            const int gb = bodyOf[b0 + lb];
+            load_jinv(B, gb, (B.flags[gb] & F_PINNED) != 0, dvOwn + 12 * i + 6);
+        } else {
+            for (int k = 0; k < 6; k++) dvOwn[12 * i + 6 + k] = 0.f;
+        }
     }
     // this CTA's part of every colour: groups starting in window `rank`
     for (int col = t; col < ncol; col += T) {
@@ -1045,12 +1102,19 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
     }
     if (writeBack) {   // an autotuner trial discards its results
         pass(OP_FINAL, false);
-        // owners write their bodies' delta-v back
+        // owners write their bodies' delta-v back; CTA 0 clears the bodies
+        // without contacts
         for (int i = t; i < own; i += T) {
             int lb = i * K + (int)rank;
-            if (lb < nb)
-                for (int k = 0; k < 6; k++) B.dv[6 * (b0 + lb) + k] = (double)dvOwn[12 * i + k];
+            if (lb < nbA) {
+                const int gb = bodyOf[b0 + lb];
+                for (int k = 0; k < 6; k++) B.dv[6 * gb + k] = (double)dvOwn[12 * i + k];
+            }
         }
+        if (rank == 0)
+            for (int b = t; b < nb; b += T)
+                if (lidOf[b0 + b] < 0)
+                    for (int k = 0; k < 6; k++) B.dv[6 * (b0 + b) + k] = 0.0;
         if (rank == 0 && t == 0) {
             sceneSweeps[s] = done;
             sceneRes[s] = res;
@@ -1074,7 +1138,8 @@ int Ctx::batchLaunchSweep(int threads, int cap, int iters, float tol, int check,
     k_batch_sweep<<<nGrid, threads, ssm, strm>>>(
         B, C[cur], sceneBodyOffDev, order, bGInfo, bLid, bChunkK, bNChunks, bContactOf, bRec, lamStart, cap,
         nbMax, iters, (float)P.omega, (float)comp, tol, check, (float)P.sliding_threshold, bSweeps, bRes,
-        lamAlt, fall, writeBack, batchInner, (float)batchRelax, batchSym, writeBack ? bTrace : nullptr);
+        lamAlt, fall, writeBack, batchInner, (float)batchRelax, batchSym, writeBack ? bTrace : nullptr, bLidOf, bBodyOf,
+        bSceneActive);
     AM_LAUNCHED(1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { err = std::string("sweep launch: ") + cudaGetErrorString(e); return AM_E_CUDA; }
@@ -1096,9 +1161,9 @@ static const int CLUSTER_K[3] = {2, 4, 8};
 // Size classes of resident scenes: staging capacity (a scene of at most
 // 2 x cap slots and 4 x cap bodies whose layout fits shared memory) and CTA
 // size of each class launch.
-static const int NCLASS = 8;
-static const int CLASS_CAP[NCLASS] = {16, 32, 64, 128, 192, 256, 384, 512};
-static const int CLASS_THREADS[NCLASS] = {32, 32, 64, 128, 192, 256, 384, 512};
+static const int NCLASS = 9;
+static const int CLASS_CAP[NCLASS] = {16, 32, 64, 128, 192, 256, 384, 512, 576};
+static const int CLASS_THREADS[NCLASS] = {32, 32, 64, 128, 192, 256, 384, 512, 512};
 
 int Ctx::batchSplit(int cap, bool useCluster) {
     int S = nScenes;
@@ -1106,14 +1171,16 @@ int Ctx::batchSplit(int cap, bool useCluster) {
     for (auto& v : hBigK) v.clear();
     for (auto& v : hClass) v.clear();
     std::vector<int2> sz(S);
+    std::vector<int> act(S);
     cudaMemcpyAsync(sz.data(), bSceneSize, sizeof(int2) * S, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(act.data(), bSceneActive, sizeof(int) * S, cudaMemcpyDeviceToHost, stream);
     int r = syncErr();
     if (r) return r;
     smallNb = 0;
     for (int q = 0; q < NCLASS; q++) classNb[q] = 0;
     for (int q = 0; q < 3; q++) { bigNb[q] = 0; bigCap[q] = 0; }
     for (int sc = 0; sc < S; sc++) {
-        const int nb = hSceneNb[sc], slots = sz[sc].x;
+        const int nb = act[sc], slots = sz[sc].x;   // active bodies: the ones the sweep keeps
         // the smallest size class that holds the scene resident (a scene
         // without contacts touches no shared memory: the smallest class)
         int c = -1;
@@ -1204,7 +1271,8 @@ int Ctx::batchLaunchCluster(int q, const int* list, int nBig, cudaStream_t strm,
                                        (const int*)bContactOf, (const float*)bRec, (const float*)bLam, bigCap[q],
                                        bigNb[q], K, iters, (float)P.omega, (float)comp, tol, check,
                                        (float)P.sliding_threshold, bSweeps, bRes, batchInner, writeBack,
-                                       (float)batchRelax, batchSym, writeBack ? bTrace : nullptr);
+                                       (float)batchRelax, batchSym, writeBack ? bTrace : nullptr, (const int*)bLidOf,
+                                       (const int*)bBodyOf, (const int*)bSceneActive);
     AM_LAUNCHED(1);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) { err = std::string("cluster sweep launch: ") + cudaGetErrorString(e); return AM_E_CUDA; }
@@ -1271,8 +1339,9 @@ int Ctx::batchLaunchAll(int threads, int cap, int iters, float tol, int check, f
 int Ctx::batchLayout(int cap) {
     double comp = P.enable_compliance ? P.compliance : 0.;
     int nc = nContacts;
-    k_batch_slots<<<nScenes, 256, 0, stream>>>(C[cur], PR, bPairOff, bOrder, bColOff, sceneBodyOffDev, nc, nPairs, cap,
-                                               bGInfo, bLid, bSlotOf, bContactOf, bChunkK, bNChunks, bSceneSize, dc);
+    k_batch_slots<<<nScenes, 256, sizeof(int) * (size_t)maxSceneBodies, stream>>>(
+        C[cur], PR, bPairOff, bOrder, bColOff, sceneBodyOffDev, nc, nPairs, cap, bGInfo, bLid, bSlotOf, bContactOf,
+        bChunkK, bNChunks, bSceneSize, bLidOf, bBodyOf, bSceneActive, dc);
     k_batch_pack<<<(nc + 127) / 128, 128, 0, stream>>>(B, C[cur], nc, bSlotOf, comp, P.friction_override, P.friction,
                                                      bRec, bLam);
     AM_LAUNCHED(2);
@@ -1461,7 +1530,8 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     bCS = nullptr;
     if (alloc(&sceneOfDev, cap) || alloc(&sceneBodyOffDev, n + 1) || alloc(&topEnd, all.n_bodies) ||
         alloc(&bPairOff, n + 1) || alloc(&bColOff, (size_t)n * (MAXCB + 1)) || alloc(&bSweeps, n) || alloc(&bRes, n) ||
-        alloc(&bFall, n) || alloc(&bTrace, 3 * (size_t)n))
+        alloc(&bFall, n) || alloc(&bTrace, 3 * (size_t)n) || alloc(&bSceneActive, n) ||
+        alloc(&bLidOf, (size_t)bodyOff[n] + 1) || alloc(&bBodyOf, (size_t)bodyOff[n] + 1))
         return AM_E_CUDA;
     cudaMemsetAsync(bFall, 0, sizeof(int) * n, stream);
     cudaMemsetAsync(bTrace, 0, sizeof(long long) * 3 * n, stream);
@@ -1485,8 +1555,6 @@ int Ctx::setBatch(const am_scene* sc, int n) {
         }
         if (!poolJoin[q]) cudaEventCreateWithFlags(&poolJoin[q], cudaEventDisableTiming);
     }
-    hSceneNb.assign(n, 0);
-    for (int q = 0; q < n; q++) hSceneNb[q] = bodyOff[q + 1] - bodyOff[q];
     if (!evFork) cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming);
     // dynamic shared memory the sweep may take: the opt-in limit less its static part
     int dev = 0, optin = 0;
@@ -1521,6 +1589,13 @@ int Ctx::setBatch(const am_scene* sc, int n) {
             clusterUsable = true;
     }
     clusterEnabled = clusterAllowed && clusterUsable;
+    size_t lsm = sizeof(int) * (size_t)maxSceneBodies;
+    if (lsm > 40 * 1024 &&
+        cudaFuncSetAttribute((const void*)k_batch_slots, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsm) !=
+            cudaSuccess) {
+        err = "a scene has too many bodies for the batched slot layout's shared memory";
+        return AM_E_CAPACITY;
+    }
     size_t csm = 2 * sizeof(unsigned long long) * (size_t)maxSceneBodies;
     if (csm > 40 * 1024 &&   // the kernel's static shared memory (4.4 KB) counts against the 48 KB default
         cudaFuncSetAttribute((const void*)k_batch_colour, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm) !=

@@ -255,20 +255,22 @@ struct Ctx {
     // scenes larger than one CTA's shared memory: thread-block clusters
     int2* bSceneSize = nullptr;  // per scene: slots, one group per colour (split overhead)
     long long* bTrace = nullptr; // per scene, last solve: start and end (device timer, ns), SM of the (first) CTA
+    int* bSceneActive = nullptr; // per scene: bodies in contact (the ones the sweep keeps)
+    int* bLidOf = nullptr;       // per body: compact id among its scene's active bodies, -1 if inactive
+    int* bBodyOf = nullptr;      // scene body offset + compact id -> body
     std::vector<int> hSmall, hBigK[3];   // one-CTA scenes; clusters of 2, 4, 8 CTAs
     // small resident scenes in size classes: one launch per class, each with
     // shared memory and CTA size for its largest scene, so several CTAs share
     // an SM
-    std::vector<int> hClass[8];
-    std::vector<int> hSceneNb;           // bodies per scene
-    int smallNb = 0, classNb[8] = {};    // largest scene (bodies) of each launch
+    std::vector<int> hClass[9];
+    int smallNb = 0, classNb[9] = {};    // largest scene (active bodies) of each launch
     int bigNb[3] = {0, 0, 0}, bigCap[3] = {0, 0, 0};
     size_t clusterSmemLimit = 0;
     std::vector<long long> lastCost;
     int clusterCap = 0;
     int clusterCapUser = 0;      // cluster staging capacity fixed by the caller (0: largest that fits)
     bool clusterEnabled = false, clusterAllowed = true, clusterUsable = false;
-    static const int NPOOL = 24;         // sweep launches: one-CTA, 8 size classes, 3 cluster sizes; two parts each
+    static const int NPOOL = 26;         // sweep launches: one-CTA, 9 size classes, 3 cluster sizes; two parts each
     cudaStream_t pool[NPOOL] = {};
     cudaEvent_t evFork = nullptr, poolJoin[NPOOL] = {};
     float* bLam = nullptr;
