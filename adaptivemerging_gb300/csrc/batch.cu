@@ -1161,9 +1161,9 @@ static const int CLUSTER_K[3] = {2, 4, 8};
 // Size classes of resident scenes: staging capacity (a scene of at most
 // 2 x cap slots and 4 x cap bodies whose layout fits shared memory) and CTA
 // size of each class launch.
-static const int NCLASS = 9;
-static const int CLASS_CAP[NCLASS] = {16, 32, 64, 128, 192, 256, 384, 512, 576};
-static const int CLASS_THREADS[NCLASS] = {32, 32, 64, 128, 192, 256, 384, 512, 512};
+static const int NCLASS = 10;
+static const int CLASS_CAP[NCLASS] = {16, 32, 64, 128, 192, 256, 384, 512, 576, 640};
+static const int CLASS_THREADS[NCLASS] = {32, 32, 64, 128, 192, 256, 384, 512, 512, 512};
 
 int Ctx::batchSplit(int cap, bool useCluster) {
     int S = nScenes;
@@ -1178,6 +1178,9 @@ int Ctx::batchSplit(int cap, bool useCluster) {
     if (r) return r;
     smallNb = 0;
     for (int q = 0; q < NCLASS; q++) classNb[q] = 0;
+    auto costOf = [&](int sc) { return (size_t)sc < lastCost.size() ? lastCost[sc] : 0; };
+    long long costTop = 0;
+    for (long long c : lastCost) costTop = std::max(costTop, c);
     for (int q = 0; q < 3; q++) { bigNb[q] = 0; bigCap[q] = 0; }
     for (int sc = 0; sc < S; sc++) {
         const int nb = act[sc], slots = sz[sc].x;   // active bodies: the ones the sweep keeps
@@ -1196,27 +1199,31 @@ int Ctx::batchSplit(int cap, bool useCluster) {
         }
         if (useCluster && (batchClasses || slots > 2 * cap)) {
             int need = -1;
+            // the smallest cluster whose launch, with this scene added, still
+            // fits shared memory (the launch lays out its most bodies and its
+            // largest part).  A scene among the longest solves of the last
+            // step (cost at least 3/4 of the largest) holds at most 640
+            // records per CTA: a sweep takes less time the fewer records each
+            // CTA holds, and these scenes bound the whole solve.
+            const bool critical = costTop > 0 && costOf(sc) * 4 >= costTop * 3;
+            const int capK = critical ? std::min(clusterCap, 640) : clusterCap;
             for (int q = 0; q < 3; q++) {
                 int K = CLUSTER_K[q];
-                int per = (slots + K - 1) / K + sz[sc].y;
-                if (per <= clusterCap && batch_cluster_smem(nb, K, clusterCap) <= clusterSmemLimit) {
+                int per = ((slots + K - 1) / K + sz[sc].y + 31) & ~31;
+                if (per <= capK && batch_cluster_smem(std::max(bigNb[q], nb), K, std::max(bigCap[q], per)) <=
+                                             clusterSmemLimit) {
                     need = q;
+                    hBigK[q].push_back(sc);
+                    bigNb[q] = std::max(bigNb[q], nb);
+                    bigCap[q] = std::max(bigCap[q], per);
                     break;
                 }
             }
-            if (need >= 0) {
-                int K = CLUSTER_K[need];
-                hBigK[need].push_back(sc);
-                bigNb[need] = std::max(bigNb[need], nb);
-                bigCap[need] = std::max(bigCap[need], (slots + K - 1) / K + sz[sc].y);
-                continue;
-            }
+            if (need >= 0) continue;
         }
         hSmall.push_back(sc);
         if (slots > 0) smallNb = std::max(smallNb, nb);
     }
-    // a cluster launch stages what its largest scene needs (multiple of 32)
-    for (int q = 0; q < 3; q++) bigCap[q] = std::min(clusterCap, (bigCap[q] + 31) & ~31);
     auto byCost = [&](int a, int b) {
         long long ca = (size_t)a < lastCost.size() ? lastCost[a] : 0, cb = (size_t)b < lastCost.size() ? lastCost[b] : 0;
         return ca > cb;
@@ -1575,15 +1582,17 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     cudaFuncSetAttribute((const void*)k_batch_sweep_cluster, cudaFuncAttributePreferredSharedMemoryCarveout,
                          (int)cudaSharedmemCarveoutMaxShared);
     // cluster kernel: the largest staging capacity (multiple of 32, at most
-    // 1024 records) that fits for K = 2
+    // 2048 records) that fits
     cudaFuncAttributes fc;
     clusterUsable = false;
     if (cudaFuncGetAttributes(&fc, (const void*)k_batch_sweep_cluster) == cudaSuccess) {
         size_t lim = (size_t)optin > fc.sharedSizeBytes ? optin - fc.sharedSizeBytes : 0;
         clusterSmemLimit = lim;
-        clusterCap = clusterCapUser > 0 ? clusterCapUser : 1024;
-        while (clusterCap > 64 && batch_cluster_smem(maxSceneBodies, 2, clusterCap) > lim) clusterCap -= 32;
-        if (batch_cluster_smem(maxSceneBodies, 2, clusterCap) <= lim &&
+        // the most records a CTA of a cluster may hold (a scene's part; its
+        // bodies are checked when the scenes are split)
+        clusterCap = clusterCapUser > 0 ? clusterCapUser : 2048;
+        while (clusterCap > 64 && batch_cluster_smem(64, 2, clusterCap) > lim) clusterCap -= 32;
+        if (batch_cluster_smem(64, 2, clusterCap) <= lim &&
             cudaFuncSetAttribute((const void*)k_batch_sweep_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)lim) == cudaSuccess)
             clusterUsable = true;

@@ -262,15 +262,15 @@ struct Ctx {
     // small resident scenes in size classes: one launch per class, each with
     // shared memory and CTA size for its largest scene, so several CTAs share
     // an SM
-    std::vector<int> hClass[9];
-    int smallNb = 0, classNb[9] = {};    // largest scene (active bodies) of each launch
+    std::vector<int> hClass[10];
+    int smallNb = 0, classNb[10] = {};    // largest scene (active bodies) of each launch
     int bigNb[3] = {0, 0, 0}, bigCap[3] = {0, 0, 0};
     size_t clusterSmemLimit = 0;
     std::vector<long long> lastCost;
     int clusterCap = 0;
     int clusterCapUser = 0;      // cluster staging capacity fixed by the caller (0: largest that fits)
     bool clusterEnabled = false, clusterAllowed = true, clusterUsable = false;
-    static const int NPOOL = 26;         // sweep launches: one-CTA, 9 size classes, 3 cluster sizes; two parts each
+    static const int NPOOL = 28;         // sweep launches: one-CTA, 10 size classes, 3 cluster sizes; two parts each
     cudaStream_t pool[NPOOL] = {};
     cudaEvent_t evFork = nullptr, poolJoin[NPOOL] = {};
     float* bLam = nullptr;

@@ -265,7 +265,7 @@ int32_t am_set_batch_size_classes(void* ctx, int32_t enable);
  * (a multiple of 32, at least 64; 0 = autotuned) */
 int32_t am_set_batch_stage(void* ctx, int32_t slots);
 /* contact records each CTA of a cluster holds (a multiple of 32, at least 64;
- * 0 = the largest that fits, at most 1024); takes effect at the next am_set_batch */
+ * 0 = the largest that fits, at most 2048); takes effect at the next am_set_batch */
 int32_t am_set_batch_cluster_stage(void* ctx, int32_t slots);
 /* batched sweep variants with the same fixed point (no reference counterpart):
  * over-relaxation factor in (0, 2) applied before the projection (1 = plain
