@@ -36,25 +36,24 @@
 namespace am {
 using namespace amd;
 
-static const int REC = 28;      // floats per packed contact record (global and shared memory)
-static const int RECS = 28;     // shared-memory stride of a staged record (28 mod 32 spreads banks)
+static const int REC = 24;      // floats per packed contact record (global memory)
+static const int RECS = 28;     // shared-memory stride of a staged record: 7 float4 positions, see rec_pos
 static const int MAXCB = 64;    // colours per scene
 static const int MAXCH = 1024;  // staging chunks per scene
 
-// Packed record (floats), 7 x 16 bytes:
+// Packed record (floats), 6 x 16 bytes:
 //   [0..3]   n  and ra.x      [4..7]   t1 and ra.y      [8..11] t2 and ra.z
-//   [12..15] rb and mu        [16..19] b0 b1 b2 G10     [20..23] 1/(D + c) of the rows, G20
-//   [24]     G21, then padding
+//   [12..15] rb and G21       [16..19] b0 b1 b2 G10     [20..23] 1/(D + c) of the rows, G20
 // f = (n, t1, t2) is the contact frame, ra / rb the contact point from the
 // two solve bodies' centres of mass.  The Jacobian rows are those of
 // Contact.computeJacobian (Contact.java:199-255): (-f, f x ra, f, rb x f);
 // the sweep forms them, and jinv J.w, from this and the bodies' inverse
-// inertia, so a record is 112 bytes instead of the 256 of the full rows.
+// inertia, so a record is 96 bytes instead of the 256 of the full rows.
 // Gqp = J_q M^-1 J_p^T are the couplings of the rows (with the sweep's own
 // M^-1: minv and jinv of a pinned body count as 0).  The multipliers live in
-// a separate array in the same slot order, 4 floats per slot (the fourth is
-// padding, so a slot is one 16-byte copy); they are the only per-sweep
-// writes.
+// a separate array in the same slot order, 4 floats per slot: lambda of the
+// three rows and the contact's friction coefficient mu (so a slot is one
+// 16-byte copy); the multipliers are the only per-sweep writes.
 
 __global__ void k_scene_ranges(const DPairs P, int npairs, const int* sceneOf, int nScenes, int* pairOff) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -81,7 +80,6 @@ __global__ void k_batch_pack(DBodies B, DContacts C, int nc, const int* slotOf, 
         r[20 + q] = (float)(1.0 / (D + comp));
         lamf[4 * sl + q] = (float)C.lam[q * cap + c];
     }
-    lamf[4 * sl + 3] = 0.f;
     // contact point (stored in body-1 coordinates) from both solve bodies
     {
         const int b1 = C.b1[c];
@@ -109,7 +107,7 @@ __global__ void k_batch_pack(DBodies B, DContacts C, int nc, const int* slotOf, 
         };
         r[19] = G(1, 0);
         r[23] = G(2, 0);
-        r[24] = G(2, 1);
+        r[15] = G(2, 1);
     }
     double mu;
     if (fo) mu = fv;
@@ -119,7 +117,7 @@ __global__ void k_batch_pack(DBodies B, DContacts C, int nc, const int* slotOf, 
         else if (f1 > 1. || f2 > 1.) mu = fmax(f1, f2);
         else mu = (f1 + f2) / 2.;
     }
-    r[15] = (float)mu;
+    lamf[4 * sl + 3] = (float)mu;
     float4* dst = reinterpret_cast<float4*>(rec + (size_t)REC * sl);
     for (int k = 0; k < REC / 4; k++) dst[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
 }
@@ -408,19 +406,28 @@ struct Rec {
     float f[3][3];      // n, t1, t2
     float ra[3], rb[3]; // contact point from each body's centre of mass
     float bq[3], iq[3]; // b and 1 / (D + c) of the three rows
-    float g10, g20, g21, mu;
+    float g10, g20, g21;
 };
 
-__device__ __forceinline__ void load_rec(const float* R, Rec& c) {
-    const float4 q0 = sld4(R), q1 = sld4(R + 4), q2 = sld4(R + 8), q3 = sld4(R + 12), q4 = sld4(R + 16),
-                 q5 = sld4(R + 20), q6 = sld4(R + 24);
+// Position (in float4 units) of 16-byte piece q of the record staged at
+// shared-memory slot `slot`: the pieces rotate by (slot / 8) mod 7 through the
+// slot's 7 positions.  Threads of a warp read the same piece of records whose
+// slots differ by a group's contact count; without the rotation the pieces of
+// groups with 4 or 8 contacts fall on the same shared-memory banks.
+__device__ __forceinline__ int rec_rot(int slot) { return (slot >> 3) % 7; }
+__device__ __forceinline__ int rec_pos(int rot, int q) { int p = q + rot; return p >= 7 ? p - 7 : p; }
+
+__device__ __forceinline__ void load_rec(const float* R, int slot, Rec& c) {
+    const int rot = rec_rot(slot);
+    const float4 q0 = sld4(R + 4 * rec_pos(rot, 0)), q1 = sld4(R + 4 * rec_pos(rot, 1)),
+                 q2 = sld4(R + 4 * rec_pos(rot, 2)), q3 = sld4(R + 4 * rec_pos(rot, 3)),
+                 q4 = sld4(R + 4 * rec_pos(rot, 4)), q5 = sld4(R + 4 * rec_pos(rot, 5));
     c.f[0][0] = q0.x; c.f[0][1] = q0.y; c.f[0][2] = q0.z; c.ra[0] = q0.w;
     c.f[1][0] = q1.x; c.f[1][1] = q1.y; c.f[1][2] = q1.z; c.ra[1] = q1.w;
     c.f[2][0] = q2.x; c.f[2][1] = q2.y; c.f[2][2] = q2.z; c.ra[2] = q2.w;
-    c.rb[0] = q3.x; c.rb[1] = q3.y; c.rb[2] = q3.z; c.mu = q3.w;
+    c.rb[0] = q3.x; c.rb[1] = q3.y; c.rb[2] = q3.z; c.g21 = q3.w;
     c.bq[0] = q4.x; c.bq[1] = q4.y; c.bq[2] = q4.z; c.g10 = q4.w;
     c.iq[0] = q5.x; c.iq[1] = q5.y; c.iq[2] = q5.z; c.g20 = q5.w;
-    c.g21 = q6.x;
 }
 
 // w x r
@@ -475,10 +482,10 @@ __device__ __forceinline__ void pair_impulse(Pair& P, const Rec& c, const float*
 // instead of three dot products and three updates.  (D lam - w) / (D + c) is
 // evaluated as lam - (c lam + w) / (D + c), and the relaxation factor (1:
 // plain) scales 1 / (D + c).
-__device__ __forceinline__ void sweep_contact(Pair& P, const float* R, float* lp, float omega, float comp,
-                                              float relax) {
+__device__ __forceinline__ void sweep_contact(Pair& P, const float* R, int slot, float* lp, float omega,
+                                              float comp, float relax) {
     Rec c;
-    load_rec(R, c);
+    load_rec(R, slot, c);
     const float4 l = sld4(lp);
     float rv[3];
     rel_vel(P, c, rv);
@@ -496,7 +503,7 @@ __device__ __forceinline__ void sweep_contact(Pair& P, const float* R, float* lp
     const float c10 = ni[1] * omega * c.g10, c20 = ni[2] * omega * c.g20, c21 = ni[2] * omega * c.g21;
     const float n0 = fmaxf(base[0], 0.f);
     const float d0 = n0 - l.x;
-    const float lim = c.mu * n0;
+    const float lim = l.w * n0;   // mu n0
     const float n1 = fminf(fmaxf(fmaf(c10, d0, base[1]), -lim), lim);
     const float d1 = n1 - l.y;
     const float n2 = fminf(fmaxf(fmaf(c21, d1, fmaf(c20, d0, base[2])), -lim), lim);
@@ -509,9 +516,9 @@ __device__ __forceinline__ void sweep_contact(Pair& P, const float* R, float* lp
 }
 
 // PGS.confidentWarmStart: delta-v += M^-1 J^T lambda
-__device__ __forceinline__ void warm_contact(Pair& P, const float* R, const float* lp) {
+__device__ __forceinline__ void warm_contact(Pair& P, const float* R, int slot, const float* lp) {
     Rec c;
-    load_rec(R, c);
+    load_rec(R, slot, c);
     const float4 l = sld4(lp);
     float F[3];
 #pragma unroll
@@ -521,10 +528,11 @@ __device__ __forceinline__ void warm_contact(Pair& P, const float* R, const floa
 
 // natural-map residual of a contact at the current state:
 // |lambda - proj(lambda - (b + J dv + c lambda) / (D + c))|
-__device__ __forceinline__ void res_contact(const Pair& P, const float* R, const float* lp, float comp, float& rmax,
+__device__ __forceinline__ void res_contact(const Pair& P, const float* R, int slot, const float* lp, float comp,
+                                            float& rmax,
                                             float& lmax) {
     Rec c;
-    load_rec(R, c);
+    load_rec(R, slot, c);
     const float4 l = sld4(lp);
     const float lq[3] = {l.x, l.y, l.z};
     float rv[3];
@@ -534,7 +542,7 @@ __device__ __forceinline__ void res_contact(const Pair& P, const float* R, const
         float w = c.bq[q] + fdot(c.f[q], rv) + comp * lq[q];
         float z = lq[q] - w * c.iq[q];
         if (q == 0) z = fmaxf(z, 0.f);
-        else { float lim = c.mu * l.x; z = fminf(fmaxf(z, -lim), lim); }
+        else { float lim = l.w * l.x; z = fminf(fmaxf(z, -lim), lim); }
         rmax = fmaxf(rmax, fabsf(lq[q] - z));
         lmax = fmaxf(lmax, fabsf(lq[q]));
     }
@@ -542,9 +550,9 @@ __device__ __forceinline__ void res_contact(const Pair& P, const float* R, const
 
 // Contact.updateContactState after the final sweep: broken when the normal
 // multiplier vanished, on edge when a tangential velocity exceeds `slide`
-__device__ __forceinline__ int final_state(const Pair& P, const float* R, const float* lp, float slide) {
+__device__ __forceinline__ int final_state(const Pair& P, const float* R, int slot, const float* lp, float slide) {
     Rec c;
-    load_rec(R, c);
+    load_rec(R, slot, c);
     float rv[3];
     rel_vel(P, c, rv);
     const float w1 = c.bq[1] + fdot(c.f[1], rv), w2 = c.bq[2] + fdot(c.f[2], rv);
@@ -646,11 +654,11 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         int s0 = gInfo[k0].x;
         int2 e = gInfo[k1 - 1];
         int nsl = e.x + e.y - s0;
-        float* R = srec + buf * cap * RECS;
         float* Lm = slam + buf * cap * 4;
         for (int i = t; i < nsl * (REC / 4); i += T) {
             int sl = i / (REC / 4), q = i - sl * (REC / 4);
-            cp_async16(R + sl * RECS + 4 * q, rec + (size_t)(s0 + sl) * REC + 4 * q);
+            int bs = buf * cap + sl;   // slot in the staging buffers
+            cp_async16(srec + bs * RECS + 4 * rec_pos(rec_rot(bs), q), rec + (size_t)(s0 + sl) * REC + 4 * q);
         }
         for (int i = t; i < nsl; i += T) cp_async16(Lm + 4 * i, lamS + 4 * ((size_t)s0 + i));
         for (int i = t; i < k1 - k0; i += T) {
@@ -694,17 +702,18 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         const int reps = op == OP_SWEEP ? inner : 1;
         for (int rep = 0; rep < reps; rep++)
         for (int j = 0; j < cnt; j++) {
-            const float* R = srec + (sl0 + j) * RECS;
+            const int slot = sl0 + j;
+            const float* R = srec + slot * RECS;
             float* lp = slam + 4 * (sl0 + j);
             if (op == OP_WARM) {
-                warm_contact(P, R, lp);
+                warm_contact(P, R, slot, lp);
             } else if (op == OP_SWEEP) {
-                sweep_contact(P, R, lp, omega, comp, relax);
+                sweep_contact(P, R, slot, lp, omega, comp, relax);
             } else if (op == OP_RES) {
-                res_contact(P, R, lp, comp, rmax, lmax);
+                res_contact(P, R, slot, lp, comp, rmax, lmax);
             } else {
                 int c = contactOf[slA + j];
-                C.state[c] = final_state(P, R, lp, slide);
+                C.state[c] = final_state(P, R, slot, lp, slide);
                 for (int q = 0; q < 3; q++) C.lam[q * C.cap + c] = (double)lp[q];
             }
         }
@@ -1004,11 +1013,11 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
         int gs0 = gInfo[lo].x;
         int2 e = gInfo[hi - 1];
         int nsl = e.x + e.y - gs0;
-        float* R = srec + s_sb[col] * RECS;
         float* Lm = slam + 4 * s_sb[col];
         for (int i = t; i < nsl * (REC / 4); i += T) {
             int sl = i / (REC / 4), q = i - sl * (REC / 4);
-            cp_async16(R + sl * RECS + 4 * q, rec + (size_t)(gs0 + sl) * REC + 4 * q);
+            int bs = s_sb[col] + sl;   // slot in the staged records
+            cp_async16(srec + bs * RECS + 4 * rec_pos(rec_rot(bs), q), rec + (size_t)(gs0 + sl) * REC + 4 * q);
         }
         for (int i = t; i < nsl; i += T) cp_async16(Lm + 4 * i, lamS + 4 * ((size_t)gs0 + i));
         for (int i = t; i < hi - lo; i += T) {
@@ -1043,17 +1052,18 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
         const int reps = op == OP_SWEEP ? inner : 1;
         for (int jj = 0; jj < reps * cnt; jj++) {
             const int j = reps == 1 ? jj : jj % cnt;
-            const float* R = srec + (sl0 + j) * RECS;
+            const int slot = sl0 + j;
+            const float* R = srec + slot * RECS;
             float* lp = slam + 4 * (sl0 + j);
             if (op == OP_WARM) {
-                warm_contact(P, R, lp);
+                warm_contact(P, R, slot, lp);
             } else if (op == OP_SWEEP) {
-                sweep_contact(P, R, lp, omega, comp, relax);
+                sweep_contact(P, R, slot, lp, omega, comp, relax);
             } else if (op == OP_RES) {
-                res_contact(P, R, lp, comp, rmax, lmax);
+                res_contact(P, R, slot, lp, comp, rmax, lmax);
             } else {
                 int c = contactOf[gi.x + j];
-                C.state[c] = final_state(P, R, lp, slide);
+                C.state[c] = final_state(P, R, slot, lp, slide);
                 for (int q = 0; q < 3; q++) C.lam[q * C.cap + c] = (double)lp[q];
             }
         }

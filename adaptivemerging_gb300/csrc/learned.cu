@@ -430,7 +430,7 @@ __global__ void k_apply_prediction(DBodies B, DContacts C, int nc, const float* 
     double lim = mu * l[0];
     for (int r = 1; r < 3; r++) l[r] = fmin(fmax(l[r], -lim), lim);
     for (int r = 0; r < 3; r++) lamL[4 * sl + r] = (float)l[r];
-    lamL[4 * sl + 3] = 0.f;
+    lamL[4 * sl + 3] = (float)mu;   // the slot's fourth float carries mu for the sweep
 }
 
 // ---------------------------------------------------------------------------
