@@ -417,6 +417,12 @@ struct Rec {
 __device__ __forceinline__ int rec_rot(int slot) { return (slot >> 3) % 7; }
 __device__ __forceinline__ int rec_pos(int rot, int q) { int p = q + rot; return p >= 7 ? p - 7 : p; }
 
+// Shared-memory slot of the multipliers of staged slot `slot`: the low three
+// bits are XORed with the next three (a permutation within each aligned run
+// of 8 slots), so the groups of one warp, whose slots differ by their contact
+// count, read and write different banks.
+__device__ __forceinline__ int lam_pos(int slot) { return slot ^ ((slot >> 3) & 7); }
+
 __device__ __forceinline__ void load_rec(const float* R, int slot, Rec& c) {
     const int rot = rec_rot(slot);
     const float4 q0 = sld4(R + 4 * rec_pos(rot, 0)), q1 = sld4(R + 4 * rec_pos(rot, 1)),
@@ -654,13 +660,12 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         int s0 = gInfo[k0].x;
         int2 e = gInfo[k1 - 1];
         int nsl = e.x + e.y - s0;
-        float* Lm = slam + buf * cap * 4;
         for (int i = t; i < nsl * (REC / 4); i += T) {
             int sl = i / (REC / 4), q = i - sl * (REC / 4);
             int bs = buf * cap + sl;   // slot in the staging buffers
             cp_async16(srec + bs * RECS + 4 * rec_pos(rec_rot(bs), q), rec + (size_t)(s0 + sl) * REC + 4 * q);
         }
-        for (int i = t; i < nsl; i += T) cp_async16(Lm + 4 * i, lamS + 4 * ((size_t)s0 + i));
+        for (int i = t; i < nsl; i += T) cp_async16(slam + 4 * lam_pos(buf * cap + i), lamS + 4 * ((size_t)s0 + i));
         for (int i = t; i < k1 - k0; i += T) {
             cp_async8(sgi + buf * cap + i, gInfo + k0 + i);
             cp_async8(sgl + buf * cap + i, glid + k0 + i);
@@ -672,9 +677,9 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         int s0 = gInfo[k0].x;
         int2 e = gInfo[k1 - 1];
         int nsl = e.x + e.y - s0;
-        const float* Lm = slam + buf * cap * 4;
         for (int i = t; i < nsl; i += T)
-            *reinterpret_cast<float4*>(lamS + 4 * ((size_t)s0 + i)) = *reinterpret_cast<const float4*>(Lm + 4 * i);
+            *reinterpret_cast<float4*>(lamS + 4 * ((size_t)s0 + i)) =
+                *reinterpret_cast<const float4*>(slam + 4 * lam_pos(buf * cap + i));
     };
 
     float rmax = 0.f, lmax = 0.f;
@@ -704,7 +709,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         for (int j = 0; j < cnt; j++) {
             const int slot = sl0 + j;
             const float* R = srec + slot * RECS;
-            float* lp = slam + 4 * (sl0 + j);
+            float* lp = slam + 4 * lam_pos(slot);
             if (op == OP_WARM) {
                 warm_contact(P, R, slot, lp);
             } else if (op == OP_SWEEP) {
@@ -803,7 +808,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         if (attempt == 1) {
             if (res <= tolRel) break;   // uniform: res comes from shared memory
             if (resident)
-                for (int i = t; i < nslots * 4; i += T) slam[i] = lamAlt[(size_t)slotS0 * 4 + i];
+                for (int i = t; i < nslots * 4; i += T) slam[4 * lam_pos(i >> 2) + (i & 3)] = lamAlt[(size_t)slotS0 * 4 + i];
             else
                 for (int i = t; i < nslots * 4; i += T) lamS[(size_t)slotS0 * 4 + i] = lamAlt[(size_t)slotS0 * 4 + i];
             for (int b = t; b < nbA; b += T)
@@ -1013,13 +1018,12 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
         int gs0 = gInfo[lo].x;
         int2 e = gInfo[hi - 1];
         int nsl = e.x + e.y - gs0;
-        float* Lm = slam + 4 * s_sb[col];
         for (int i = t; i < nsl * (REC / 4); i += T) {
             int sl = i / (REC / 4), q = i - sl * (REC / 4);
             int bs = s_sb[col] + sl;   // slot in the staged records
             cp_async16(srec + bs * RECS + 4 * rec_pos(rec_rot(bs), q), rec + (size_t)(gs0 + sl) * REC + 4 * q);
         }
-        for (int i = t; i < nsl; i += T) cp_async16(Lm + 4 * i, lamS + 4 * ((size_t)gs0 + i));
+        for (int i = t; i < nsl; i += T) cp_async16(slam + 4 * lam_pos(s_sb[col] + i), lamS + 4 * ((size_t)gs0 + i));
         for (int i = t; i < hi - lo; i += T) {
             cp_async8(sgi + s_kb[col] + i, gInfo + lo + i);
             cp_async8(sgl + s_kb[col] + i, glid + lo + i);
@@ -1054,7 +1058,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
             const int j = reps == 1 ? jj : jj % cnt;
             const int slot = sl0 + j;
             const float* R = srec + slot * RECS;
-            float* lp = slam + 4 * (sl0 + j);
+            float* lp = slam + 4 * lam_pos(slot);
             if (op == OP_WARM) {
                 warm_contact(P, R, slot, lp);
             } else if (op == OP_SWEEP) {
