@@ -23,6 +23,11 @@ AM_BOX, AM_SPHERE, AM_PLANE, AM_TREE = 0, 1, 2, 3
 AM_STATE_BROKEN, AM_STATE_ONEDGE, AM_STATE_CLEAR = 0, 1, 2
 AM_BV_NULL = -1
 AM_ORDER_REFERENCE, AM_ORDER_COLOURED = 0, 1
+# am_get_phase_times order: the reference's CSV time columns
+# (RigidBodySystem.exportDataToFile, RigidBodySystem.java:495-542)
+PHASES = ("detection", "warmstart", "LCPSolve", "updateCollections", "contactOrdering", "singleItPGS",
+          "merging", "mergingBuild", "unmerging", "unmergingBuild", "computeTime")
+AM_NUM_PHASES = len(PHASES)
 
 
 def AM_BV_PLANE(b):

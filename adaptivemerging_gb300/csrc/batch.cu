@@ -1685,11 +1685,17 @@ int Ctx::batchAutotune(double dt) {
 int Ctx::stepBatch(double dt) {
     int r;
     if ((r = beginStep(0))) return r;
+    double t = phaseNow();
     if ((r = collisionDetection())) return r;
+    phaseAdd(AM_PHASE_DETECTION, t);
+    t = phaseNow();
     if ((r = warmStart())) return r;
+    phaseAdd(AM_PHASE_WARMSTART, t);
     if ((r = wake())) return r;
     if (!evA) { cudaEventCreate(&evA); cudaEventCreate(&evB); }
+    t = phaseNow();
     if ((r = batchSolve(dt))) return r;
+    phaseAdd(AM_PHASE_LCP_SOLVE, t);
     if ((r = finishStep(dt))) return r;
     if ((r = readCounts())) return r;
     if (pgsPending) {

@@ -439,6 +439,21 @@ int32_t am_get_contacts(void* ctx, am_contacts* out, int32_t capacity, int32_t* 
     return c->getContacts(out, capacity, n);
 }
 
+int32_t am_set_phase_timing(void* ctx, int32_t enable) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    c->phaseOn = enable != 0;
+    for (double& v : c->phase) v = 0.;
+    return AM_OK;
+}
+
+int32_t am_get_phase_times(void* ctx, double* seconds) {
+    if (!ctx || !seconds) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    for (int k = 0; k < AM_NUM_PHASES; k++) seconds[k] = c->phase[k];
+    return AM_OK;
+}
+
 int32_t am_get_perf(void* ctx, am_perf* out) {
     if (!ctx || !out) return AM_E_ARG;
     Ctx* c = (Ctx*)ctx;

@@ -6,6 +6,7 @@
 // RigidBody.java:182-206, PlaneRigidBody.java:49-57).  Contacts, pairs and
 // the per-step state live on the device.
 #pragma once
+#include <chrono>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -250,6 +251,16 @@ struct Ctx {
     size_t batchSmemLimit = 0;   // dynamic shared memory the sweep kernel may use
     int batchInner = 1;          // passes over a body pair's contacts per sweep
     int batchClasses = 1;        // small scenes in size-class launches (0: all in the one-CTA launch)
+    // per-phase wall times of the last step (the reference's CSV columns), on request
+    bool phaseOn = false;
+    double phase[AM_NUM_PHASES] = {};
+    // wall clock in seconds after the stream's work so far (0 when phase timing is off)
+    double phaseNow() {
+        if (!phaseOn) return 0.;
+        cudaStreamSynchronize(stream);
+        return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+    }
+    void phaseAdd(int k, double t0) { if (phaseOn) phase[k] += phaseNow() - t0; }
     double batchRelax = 1.0;     // over-relaxation of the batched sweep (1: plain projected Gauss-Seidel)
     int batchSym = 0;            // 1: odd sweeps walk the colours backwards
     // scenes larger than one CTA's shared memory: thread-block clusters
@@ -335,6 +346,7 @@ struct Ctx {
     int finishStep(double dt);
     int step(double dt);
     int stepWithMerging(double dt);
+    int stepPlain(double dt);
     int collectStats();
     void foldTiming();
     int getBodies(am_body_state* out);

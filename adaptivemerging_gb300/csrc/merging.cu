@@ -395,6 +395,7 @@ int Ctx::singleSweep(double dt) {
         int r = syncErr();
         if (r) return r;
     }
+    const double tOrder = phaseNow();   // CollisionProcessor.java:256-258 contactOrderingTime
     std::vector<int> ordered;
     for (int p : M.coll.v)
         for (int ref : M.bpc[p].list)
@@ -409,6 +410,7 @@ int Ctx::singleSweep(double dt) {
         if ((host.flags[b] & F_COLLECTION) && !(host.flags[b] & F_SLEEPING))
             for (int p : M.bodyBpcs[b].v)
                 if (!M.bpc[p].checked) { ordered.push_back(p); M.bpc[p].checked = true; }
+    phaseAdd(AM_PHASE_CONTACT_ORDERING, tOrder);
     std::vector<int> ext, extPos, in, inPos;
     int n = 0;
     for (int p : ordered)
@@ -425,7 +427,9 @@ int Ctx::singleSweep(double dt) {
         k_recompute_J<<<(n + 127) / 128, 128, 0, stream>>>(B, Sw, n, 1);
         AM_LAUNCHED(1);
         launch_solve_prep(B, Sw, n, dt, P.feedback_stiffness, true, P.restitution_override, P.restitution, 0, stream);
+        const double tPgs = phaseNow();   // CollisionProcessor.java:284-287 singleItPGSTime
         if ((r = exactSweep(Sw, n, P.iterations_in_collection, true))) return r;
+        phaseAdd(AM_PHASE_SINGLE_IT_PGS, tPgs);
         if ((r = copyContacts(Sw, extPos, C[cur], ext, 2))) return r;
         if ((r = copyContacts(Sw, inPos, I, in, 2))) return r;
     }
@@ -873,6 +877,7 @@ int Ctx::merge() {
         q.mm.clear();
         q.sh.clear();
         removal.push_back(p);
+        const double tb = phaseNow();   // Merging.java:80-155 mergingBuildTime
         int b1 = q.a, b2 = q.b;
         int p1 = host.parent[b1], p2 = host.parent[b2];
         if (p1 < 0 && p2 < 0) {
@@ -907,6 +912,7 @@ int Ctx::merge() {
             if ((r = collAddIncomplete(b1, removal))) return r;
             collAddBPCs(p);
         }
+        phaseAdd(AM_PHASE_MERGING_BUILD, tb);
     }
     for (int p : removal) M.coll.remove(p);
     if (pulled) return pushBodies();
@@ -1028,6 +1034,7 @@ int Ctx::unmerge() {
         }
         if (sel.empty()) continue;
         if (!pulled) { if ((r = pullBodies())) return r; pulled = true; }
+        const double tb = phaseNow();   // Merging.java:219-265 unmergingBuildTime
         std::vector<int> nb;
         bool removeC = false;
         if ((r = unmergeSelected(b, sel, nb, removeC))) return r;
@@ -1037,6 +1044,7 @@ int Ctx::unmerge() {
             for (int q : nb) additionQ.push_back(q);
             if (removeC) removalQ.push_back(b);
         }
+        phaseAdd(AM_PHASE_UNMERGING_BUILD, tb);
     }
     for (int q : additionQ) host.top.push_back(q);
     if (!removalQ.empty()) {
@@ -1163,13 +1171,20 @@ int Ctx::stepWithMerging(double dt) {
     int r;
     appended = 0;
     if ((r = beginStep(0))) return r;
+    double t = phaseNow();
     if ((r = collisionDetection())) return r;
+    phaseAdd(AM_PHASE_DETECTION, t);
     if ((r = updateBodyPairContacts())) return r;
+    t = phaseNow();
     if ((r = warmStart())) return r;
+    phaseAdd(AM_PHASE_WARMSTART, t);
     if ((r = wake())) return r;
     cudaMemcpyAsync(host.flags.data(), B.flags, sizeof(int) * host.cap, cudaMemcpyDeviceToHost, stream);
     if ((r = syncErr())) return r;
+    t = phaseNow();
     if ((r = singleSweep(dt))) return r;
+    phaseAdd(AM_PHASE_UPDATE_COLLECTIONS, t);
+    t = phaseNow();
     if ((r = accumulateForUnmerging())) return r;
     if ((r = unmerge())) return r;
     if (appended) {   // contacts handed back by unmerge join the full solve (lambda = lambdaXwarm)
@@ -1178,18 +1193,25 @@ int Ctx::stepWithMerging(double dt) {
         if ((r = flushAppendedPairs())) return r;
     }
     if (mergingEvent && (r = beginStep(1))) return r;
+    phaseAdd(AM_PHASE_UNMERGING, t);
     if (nContacts > 0) {
         k_solve_bodies<<<(nContacts + 127) / 128, 128, 0, stream>>>(B, C[cur], nContacts);
         k_recompute_J<<<(nContacts + 127) / 128, 128, 0, stream>>>(B, C[cur], nContacts, 0);
         AM_LAUNCHED(2);
     }
+    t = phaseNow();
     if ((r = solveLCP(dt, P.warm_start != 0))) return r;
+    phaseAdd(AM_PHASE_LCP_SOLVE, t);
     if ((r = clearBodyPairContacts())) return r;
     advVel(dt);
+    t = phaseNow();
     if ((r = accumulateForMerging())) return r;
+    phaseAdd(AM_PHASE_MERGING, t);
     advPos(dt);
+    t = phaseNow();
     if ((totalSteps % P.steps_between_merge_events) == 0)
         if ((r = merge())) return r;
+    phaseAdd(AM_PHASE_MERGING, t);
     if ((r = uploadExternalFlags())) return r;
     if ((r = sleepDecay())) return r;
     if ((r = readCounts())) return r;

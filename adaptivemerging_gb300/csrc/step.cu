@@ -789,13 +789,29 @@ int Ctx::finishStep(double dt) {
 int Ctx::step(double dt) {
     totalSteps++;
     int r;
-    if (nScenes > 0) return stepBatch(dt);
-    if (host.anyMerging()) return stepWithMerging(dt);
+    for (double& v : phase) v = 0.;
+    const double t0 = phaseNow();
+    if (nScenes > 0) r = stepBatch(dt);
+    else if (host.anyMerging()) r = stepWithMerging(dt);
+    else r = stepPlain(dt);
+    phaseAdd(AM_PHASE_COMPUTE, t0);
+    return r;
+}
+
+// RigidBodySystem.advanceTime without merging
+int Ctx::stepPlain(double dt) {
+    int r;
     if ((r = beginStep(0))) return r;
+    double t = phaseNow();
     if ((r = collisionDetection())) return r;
+    phaseAdd(AM_PHASE_DETECTION, t);
+    t = phaseNow();
     if ((r = warmStart())) return r;
+    phaseAdd(AM_PHASE_WARMSTART, t);
     if ((r = wake())) return r;
+    t = phaseNow();
     if ((r = solveLCP(dt, P.warm_start != 0))) return r;
+    phaseAdd(AM_PHASE_LCP_SOLVE, t);
     if ((r = finishStep(dt))) return r;
     if ((r = readCounts())) return r;
     foldTiming();

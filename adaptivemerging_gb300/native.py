@@ -21,7 +21,7 @@ EXPORTS = [
     "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
     "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats", "am_get_batch_scene_times", "am_set_residual_target",
     "am_set_batch_local_sweeps", "am_set_batch_clusters", "am_set_batch_stage", "am_set_batch_relaxation",
-    "am_set_batch_cluster_stage", "am_set_batch_size_classes",
+    "am_set_batch_cluster_stage", "am_set_batch_size_classes", "am_set_phase_timing", "am_get_phase_times",
     "am_learned_collect", "am_learned_train", "am_learned_use", "am_learned_scope", "am_learned_weights", "am_learned_info",
     "am_learned_grad", "am_learned_infer", "am_learned_infer_noalloc",
 ]
@@ -87,6 +87,8 @@ def lib():
         L.am_get_topology.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32,
                                       C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.am_reset_perf.argtypes = [vp]
+        L.am_set_phase_timing.argtypes = [vp, C.c_int32]
+        L.am_get_phase_times.argtypes = [vp, C.POINTER(C.c_double)]
         L.am_get_stream.argtypes = [vp, C.POINTER(vp)]
         for f in EXPORTS:
             if f not in ("am_params_default", "am_last_error"):
@@ -273,6 +275,16 @@ class System:
     def reset_perf(self):
         self._check(lib().am_reset_perf(self.h))
 
+    def set_phase_timing(self, enable=True):
+        """Per-phase wall times of each step (the reference's CSV columns)."""
+        self._check(lib().am_set_phase_timing(self.h, int(enable)))
+
+    def phase_times(self):
+        """Seconds per phase of the last step, in abi.PHASES order."""
+        out = np.zeros(abi.AM_NUM_PHASES, np.float64)
+        self._check(lib().am_get_phase_times(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
     def stream_handle(self):
         s = C.c_void_p()
         self._check(lib().am_get_stream(self.h, C.byref(s)))
@@ -328,6 +340,7 @@ class System:
 
 
 for _name in ("_check", "close", "__del__", "step", "advance_time", "stats", "num_contacts", "contacts", "bodies",
-              "perf", "reset_perf", "stream_handle", "set_params", "topology", "put_bodies_struct",
+              "perf", "reset_perf", "set_phase_timing", "phase_times", "stream_handle", "set_params", "topology",
+              "put_bodies_struct",
               "get_bodies_struct", "collision_detection", "warm_start", "solve_lcp", "integrate"):
     setattr(BatchSystem, _name, getattr(System, _name))

@@ -341,6 +341,30 @@ int32_t am_get_topology(void* ctx, int32_t* items, int32_t* item_off, int32_t ca
 /* Instrumentation (no reference counterpart). */
 int32_t am_get_perf(void* ctx, am_perf* out);
 int32_t am_reset_perf(void* ctx);
+
+/* Per-phase wall times of the last am_step, in seconds, in the order of the
+ * reference's CSV columns (RigidBodySystem.exportDataToFile,
+ * RigidBodySystem.java:495-542; measured at RigidBodySystem.java:102-175,
+ * CollisionProcessor.java:91-302, Merging.java:73-273).  Off by default: when
+ * on, every phase boundary synchronises the context stream, so the phases
+ * are wall times of the device work, as the reference's are of its Java
+ * work.  Phases that do not run (no merging, no collections) read 0. */
+enum {
+    AM_PHASE_DETECTION = 0,          /* collisionDetectTime  */
+    AM_PHASE_WARMSTART = 1,          /* warmStartTime        */
+    AM_PHASE_LCP_SOLVE = 2,          /* collisionSolveTime   */
+    AM_PHASE_UPDATE_COLLECTIONS = 3, /* collectionUpdateTime */
+    AM_PHASE_CONTACT_ORDERING = 4,   /* contactOrderingTime  */
+    AM_PHASE_SINGLE_IT_PGS = 5,      /* singleItPGSTime      */
+    AM_PHASE_MERGING = 6,            /* mergingTime          */
+    AM_PHASE_MERGING_BUILD = 7,      /* mergingBuildTime     */
+    AM_PHASE_UNMERGING = 8,          /* unmergingTime        */
+    AM_PHASE_UNMERGING_BUILD = 9,    /* unmergingBuildTime   */
+    AM_PHASE_COMPUTE = 10,           /* computeTime          */
+    AM_NUM_PHASES = 11
+};
+int32_t am_set_phase_timing(void* ctx, int32_t enable);
+int32_t am_get_phase_times(void* ctx, double* seconds /* [AM_NUM_PHASES] */);
 /* the context's cudaStream_t, for callers that order their own work after a step */
 int32_t am_get_stream(void* ctx, void** stream);
 

@@ -188,6 +188,13 @@ def test_batch_edge_cases(gpu_lib):
     assert (ss["residual"] <= 1e-6).all(), ss["residual"]
     x = g.bodies()["x"]
     assert np.isfinite(x).all()
+    # per-scene solve times of the last step: every scene ran on a real SM,
+    # inside the step, longer solves for the scenes that swept
+    tm = g.scene_times()
+    assert (tm["start_ns"] >= 0).all() and (tm["end_ns"] >= tm["start_ns"]).all()
+    assert tm["start_ns"].min() == 0 and tm["end_ns"].max() < 10**9
+    assert ((tm["sm"] >= 0) & (tm["sm"] < 1024)).all()
+    assert tm["end_ns"][4] > tm["start_ns"][4]
 
 
 def test_batch_rejects_oversized_scene(gpu_lib):
