@@ -96,6 +96,7 @@ struct DPairs {
     int* count;      // contacts of the pair
     int* off;        // first contact
     int* keep;       // pair survives clearBodyPairContacts
+    int* perm;       // narrow-phase processing order: pairs grouped by body-type class
 };
 
 struct Scratch {
@@ -130,6 +131,10 @@ struct DCount {
 void launch_begin_step(const DBodies& B, const int* top, int ntop, double gx, double gy, double gz,
                        int mergingReapply, cudaStream_t s);
 void launch_bv_update(const DBodies& B, const DNodes& N, cudaStream_t s);
+// narrow-phase order: pairs grouped by body-type class (box-plane, sphere-tree
+// on plane, box-box, box-tree, tree-tree), so a warp runs one collider; cls
+// is 16 ints of device scratch
+void launch_pair_order(const DBodies& B, DPairs& P, int n, int* cls, cudaStream_t s);
 int launch_broadphase(const DBodies& B, const DNodes& N, const int* top, int ntop, int* candA, int* candB,
                       int candCap, int* rowCount, int* rowOff, Scratch& sc, DCount* dc, cudaStream_t s,
                       const int* topEnd = nullptr);

@@ -171,6 +171,7 @@ struct Ctx {
     DContacts C[2];
     int cur = 0;
     DPairs PR;
+    int* pairCls = nullptr;      // narrow-phase order: per-class counters
     DHash H;
     Scratch SC;
     DCount* dc = nullptr;

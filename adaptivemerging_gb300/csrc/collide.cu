@@ -215,21 +215,28 @@ __global__ void k_broad_rows(DBodies B, DNodes N, const int* top, int ntop, int*
     if (!WRITE && lane == 0) rowCount[i] = run;
 }
 
+// candA == nullptr: the count pass (bounding-sphere pack, per-row counts,
+// their scan into rowOff and dc->n_cand).  Otherwise the emit pass only, into
+// the rows' offsets from the count pass of the same step.
 int launch_broadphase(const DBodies& B, const DNodes& N, const int* top, int ntop, int* candA, int* candB,
                       int candCap, int* rowCount, int* rowOff, Scratch& sc, DCount* dc, cudaStream_t s,
                       const int* topEnd) {
     if (ntop < 2) {
-        cudaMemsetAsync(&dc->n_cand, 0, sizeof(int), s);
+        if (!candA) cudaMemsetAsync(&dc->n_cand, 0, sizeof(int), s);
         return 0;
     }
-    k_broad_pack<<<(ntop + 127) / 128, 128, 0, s>>>(B, N, top, ntop);
-    AM_LAUNCHED(1);
     int warps = ntop - 1;
     int blocks = (warps * 32 + 255) / 256;
-    k_broad_rows<false><<<blocks, 256, 0, s>>>(B, N, top, ntop, rowCount, nullptr, nullptr, nullptr, 0, topEnd);
+    if (!candA) {
+        k_broad_pack<<<(ntop + 127) / 128, 128, 0, s>>>(B, N, top, ntop);
+        AM_LAUNCHED(1);
+        k_broad_rows<false><<<blocks, 256, 0, s>>>(B, N, top, ntop, rowCount, nullptr, nullptr, nullptr, 0, topEnd);
+        AM_LAUNCHED(1);
+        launch_scan(rowCount, rowOff, ntop - 1, sc, &dc->n_cand, s);
+        return 0;
+    }
+    k_broad_rows<true><<<blocks, 256, 0, s>>>(B, N, top, ntop, nullptr, rowOff, candA, candB, candCap, topEnd);
     AM_LAUNCHED(1);
-    launch_scan(rowCount, rowOff, ntop - 1, sc, &dc->n_cand, s);
-    if (candA) { k_broad_rows<true><<<blocks, 256, 0, s>>>(B, N, top, ntop, nullptr, rowOff, candA, candB, candCap, topEnd); AM_LAUNCHED(1); }
     return 0;
 }
 
@@ -774,9 +781,65 @@ __device__ void narrow_pair(const DBodies& B, const DNodes& N, int b1, int b2, E
     }
 }
 
+// body-type class of a pair: 0 box-plane, 1 sphere tree on plane, 2 box-box,
+// 3 box-tree, 4 tree-tree (planes never pair with planes)
+__device__ __forceinline__ int pair_class(const DBodies& B, int b1, int b2) {
+    int t1 = B.type[b1], t2 = B.type[b2];
+    if (t1 == AM_PLANE || t2 == AM_PLANE) return (t1 == AM_BOX || t2 == AM_BOX) ? 0 : 1;
+    if (t1 == AM_BOX && t2 == AM_BOX) return 2;
+    return (t1 == AM_BOX || t2 == AM_BOX) ? 3 : 4;
+}
+
+// class counts (warp-aggregated atomics into cls[0..4])
+__global__ void k_pair_class_count(DBodies B, DPairs P, int n, int* cls) {
+    const unsigned FULL = 0xffffffffu;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        int i = base + threadIdx.x;
+        int c = i < n ? pair_class(B, P.a[i], P.b[i]) : -1;
+        for (int k = 0; k < 5; k++) {
+            unsigned m = __ballot_sync(FULL, c == k);
+            if (m && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&cls[k], __popc(m));
+        }
+    }
+}
+
+// positions: each class starts after the smaller classes; within a class the
+// order is arbitrary (every pair writes its own outputs)
+__global__ void k_pair_perm(DBodies B, DPairs P, int n, int* cls) {
+    const unsigned FULL = 0xffffffffu;
+    __shared__ int s_off[5];
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int k = 0; k < 5; k++) { s_off[k] = run; run += cls[k]; }
+    }
+    __syncthreads();
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        int i = base + threadIdx.x;
+        int c = i < n ? pair_class(B, P.a[i], P.b[i]) : -1;
+        const int lane = threadIdx.x & 31;
+        for (int k = 0; k < 5; k++) {
+            unsigned m = __ballot_sync(FULL, c == k);
+            if (!m) continue;
+            int leader = __ffs(m) - 1, pos = 0;
+            if (lane == leader) pos = atomicAdd(&cls[5 + k], __popc(m));
+            pos = __shfl_sync(FULL, pos, leader);
+            if (c == k) P.perm[s_off[k] + pos + __popc(m & ((1u << lane) - 1))] = i;
+        }
+    }
+}
+
+void launch_pair_order(const DBodies& B, DPairs& P, int n, int* cls, cudaStream_t s) {
+    cudaMemsetAsync(cls, 0, sizeof(int) * 16, s);
+    int blocks = std::min((n + 255) / 256, 4 * 152);
+    k_pair_class_count<<<blocks, 256, 0, s>>>(B, P, n, cls);
+    k_pair_perm<<<blocks, 256, 0, s>>>(B, P, n, cls);
+    AM_LAUNCHED(2);
+}
+
 __global__ void k_narrow_count(DBodies B, DNodes N, DPairs P, DCount* dc) {
     int n = dc->n_pairs;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int i = P.perm[j];
         CountEmit e{0};
         int err = 0;
         narrow_pair(B, N, P.a[i], P.b[i], e, &err);
@@ -787,7 +850,8 @@ __global__ void k_narrow_count(DBodies B, DNodes N, DPairs P, DCount* dc) {
 
 __global__ void k_narrow_emit(DBodies B, DNodes N, DPairs P, DContacts C, DCount* dc) {
     int n = dc->n_pairs;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int i = P.perm[j];
         WriteEmit e{&B, &C, P.off[i], 0, i, &dc->overflow};
         int err = 0;
         narrow_pair(B, N, P.a[i], P.b[i], e, &err);

@@ -358,7 +358,7 @@ int Ctx::ensurePairs(int need) {
     np.cap = cap;
     int r = 0;
     r |= alloc(&np.a, cap); r |= alloc(&np.b, cap); r |= alloc(&np.count, cap); r |= alloc(&np.off, cap + 1);
-    r |= alloc(&np.keep, cap);
+    r |= alloc(&np.keep, cap); r |= alloc(&np.perm, cap);
     r |= alloc(&colourOf, cap); r |= alloc(&groupOrder, cap);
     if (r) return AM_E_CUDA;
     PR = np;
@@ -606,6 +606,8 @@ int Ctx::collisionDetection() {
     cudaMemsetAsync(&dc->n_pairs, 0, sizeof(int), stream);
     cudaMemcpyAsync(&dc->n_pairs, &nPairs, sizeof(int), cudaMemcpyHostToDevice, stream);
     if (npairs > 0) {
+        if (!pairCls && alloc(&pairCls, 16)) return AM_E_CUDA;
+        launch_pair_order(B, PR, npairs, pairCls, stream);
         launch_narrow(B, N, PR, C[cur], SC, dc, false, stream);
         if ((r = ensureScratch(npairs + 1))) return r;
         launch_scan(PR.count, PR.off, npairs, SC, &dc->n_contacts, stream);
