@@ -137,7 +137,7 @@ void launch_bv_update(const DBodies& B, const DNodes& N, cudaStream_t s);
 void launch_pair_order(const DBodies& B, DPairs& P, int n, int* cls, cudaStream_t s);
 int launch_broadphase(const DBodies& B, const DNodes& N, const int* top, int ntop, int* candA, int* candB,
                       int candCap, int* rowCount, int* rowOff, Scratch& sc, DCount* dc, cudaStream_t s,
-                      const int* topEnd = nullptr);
+                      const int* topEnd = nullptr, unsigned* masks = nullptr, int mw = 0);
 void launch_expand_pairs(const DBodies& B, const int* sub_off, const int* sub_ids, const int* candA,
                          const int* candB, int ncand, DPairs& P, Scratch& sc, DCount* dc, cudaStream_t s);
 void launch_narrow(const DBodies& B, const DNodes& N, DPairs& P, DContacts& C, Scratch& sc, DCount* dc,

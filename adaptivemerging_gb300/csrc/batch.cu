@@ -1649,6 +1649,19 @@ int Ctx::batchAutotune(double dt) {
     }
     int nc = nContacts;
     int r0 = 0;
+    // With the size classes on, the one-CTA launch only gets scenes that fit
+    // no class and no cluster (streamed through its staging buffers).  When
+    // there are none at the largest capacity there is nothing to tune.
+    if (batchClasses && !fixedThreads) {
+        batchLayout(caps.back());
+        if ((r0 = batchSplit(caps.back(), clusterEnabled))) return r0;
+        if (hSmall.empty()) {
+            batchThreads = 256;
+            batchCap = caps.back();
+            batchTunedContacts = nc;
+            return syncErr();
+        }
+    }
     float* save = bLamL;   // the learned start is written only after tuning
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);

@@ -172,6 +172,8 @@ struct Ctx {
     int cur = 0;
     DPairs PR;
     int* pairCls = nullptr;      // narrow-phase order: per-class counters
+    unsigned* broadMask = nullptr;   // broad phase: hit mask per row and 32-pair chunk
+    size_t broadMaskCap = 0;
     DHash H;
     Scratch SC;
     DCount* dc = nullptr;

@@ -183,10 +183,13 @@ __device__ __forceinline__ bool far_apart32(float4 a, float4 b) {
     return d2 > T * T;
 }
 
-// one warp per row i of the top-level list; ballot + popc keeps row-major order
+// one warp per row i of the top-level list; ballot + popc keeps row-major order.
+// With `masks`, the count pass stores every 32-pair chunk's hit mask (row i,
+// chunk c at masks[i * mw + c]) and the emit pass reads them back instead of
+// testing the pairs again.
 template <bool WRITE>
 __global__ void k_broad_rows(DBodies B, DNodes N, const int* top, int ntop, int* rowCount, const int* rowOff,
-                             int* candA, int* candB, int cap, const int* topEnd) {
+                             int* candA, int* candB, int cap, const int* topEnd, unsigned* masks, int mw) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (warp >= ntop - 1) return;
@@ -195,10 +198,14 @@ __global__ void k_broad_rows(DBodies B, DNodes N, const int* top, int ntop, int*
     int run = WRITE ? rowOff[i] : 0;
     int end = topEnd ? topEnd[i] : ntop;   // batched scenes: pairs stay inside one scene
     const float4 ca = B.bc[a];
+    unsigned* mrow = masks ? masks + (size_t)i * mw : nullptr;
     for (int j0 = i + 1; j0 < end; j0 += 32) {
         int j = j0 + lane;
+        const int c = (j0 - i - 1) >> 5;
         bool hit = false;
-        if (j < end) {
+        if (WRITE && mrow) {
+            hit = (mrow[c] >> lane) & 1u;
+        } else if (j < end) {
             int b = top[j];
             float4 cb = B.bc[b];
             // the prefilter only removes pairs the exact test rejects as well
@@ -206,6 +213,7 @@ __global__ void k_broad_rows(DBodies B, DNodes N, const int* top, int ntop, int*
             hit = !far && pair_may_touch(B, N, a, b);
         }
         unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (!WRITE && mrow && lane == 0) mrow[c] = m;
         if (WRITE && hit) {
             int pos = run + __popc(m & ((1u << lane) - 1u));
             if (pos < cap) { candA[pos] = a; candB[pos] = top[j]; }
@@ -220,7 +228,7 @@ __global__ void k_broad_rows(DBodies B, DNodes N, const int* top, int ntop, int*
 // the rows' offsets from the count pass of the same step.
 int launch_broadphase(const DBodies& B, const DNodes& N, const int* top, int ntop, int* candA, int* candB,
                       int candCap, int* rowCount, int* rowOff, Scratch& sc, DCount* dc, cudaStream_t s,
-                      const int* topEnd) {
+                      const int* topEnd, unsigned* masks, int mw) {
     if (ntop < 2) {
         if (!candA) cudaMemsetAsync(&dc->n_cand, 0, sizeof(int), s);
         return 0;
@@ -230,12 +238,14 @@ int launch_broadphase(const DBodies& B, const DNodes& N, const int* top, int nto
     if (!candA) {
         k_broad_pack<<<(ntop + 127) / 128, 128, 0, s>>>(B, N, top, ntop);
         AM_LAUNCHED(1);
-        k_broad_rows<false><<<blocks, 256, 0, s>>>(B, N, top, ntop, rowCount, nullptr, nullptr, nullptr, 0, topEnd);
+        k_broad_rows<false><<<blocks, 256, 0, s>>>(B, N, top, ntop, rowCount, nullptr, nullptr, nullptr, 0, topEnd,
+                                                   masks, mw);
         AM_LAUNCHED(1);
         launch_scan(rowCount, rowOff, ntop - 1, sc, &dc->n_cand, s);
         return 0;
     }
-    k_broad_rows<true><<<blocks, 256, 0, s>>>(B, N, top, ntop, nullptr, rowOff, candA, candB, candCap, topEnd);
+    k_broad_rows<true><<<blocks, 256, 0, s>>>(B, N, top, ntop, nullptr, rowOff, candA, candB, candCap, topEnd,
+                                              masks, mw);
     AM_LAUNCHED(1);
     return 0;
 }

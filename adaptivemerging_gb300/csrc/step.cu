@@ -323,6 +323,26 @@ void Ctx::release() {
     }
     if (evFork) cudaEventDestroy(evFork);
     evFork = nullptr;
+    // every device buffer went with `allocs`: forget them and their capacities,
+    // so a context given a new scene allocates afresh
+    std::memset(&PR, 0, sizeof(PR));
+    std::memset(&H, 0, sizeof(H));
+    std::memset(&SC, 0, sizeof(SC));
+    candA = candB = nullptr;
+    candCap = 0;
+    Mj = invD = nullptr;
+    mjCap = 0;
+    levOrder = levOff = nullptr;
+    levCap = 0;
+    idxA = idxB = nullptr;
+    idxCap = 0;
+    metA = metB = metM = nullptr;
+    metOut = nullptr;
+    metCap = 0;
+    pairCls = nullptr;
+    broadMask = nullptr;
+    broadMaskCap = 0;
+    bCS = nullptr;
 }
 
 
@@ -587,12 +607,30 @@ int Ctx::collisionDetection() {
     launch_bv_update(B, N, stream);
     int r = ensureCand(1);
     if (r) return r;
-    launch_broadphase(B, N, top, ntop, nullptr, nullptr, 0, rowCount, rowOff, SC, dc, stream, topEnd);
+    // hit masks of the count pass, reused by the emit pass (when they fit 256 MB)
+    unsigned* masks = nullptr;
+    int mw = 0;
+    if (ntop >= 2) {
+        const int rowMax = nScenes > 0 ? maxSceneBodies : ntop;
+        mw = (rowMax + 31) / 32;
+        size_t need = (size_t)ntop * (size_t)mw;
+        if (need * sizeof(unsigned) <= (size_t)256 << 20) {
+            if (need > broadMaskCap) {
+                if (alloc(&broadMask, need)) return AM_E_CUDA;
+                broadMaskCap = need;
+            }
+            masks = broadMask;
+        } else {
+            mw = 0;
+        }
+    }
+    launch_broadphase(B, N, top, ntop, nullptr, nullptr, 0, rowCount, rowOff, SC, dc, stream, topEnd, masks, mw);
     if ((r = readCounts())) return r;
     int ncand = hc->n_cand;
     if ((r = ensureCand(ncand))) return r;
     if (ntop >= 2 && ncand > 0) {
-        launch_broadphase(B, N, top, ntop, candA, candB, candCap, rowCount, rowOff, SC, dc, stream, topEnd);
+        launch_broadphase(B, N, top, ntop, candA, candB, candCap, rowCount, rowOff, SC, dc, stream, topEnd, masks,
+                          mw);
     }
     if ((r = ensureScratch(ncand + 1))) return r;
     launch_expand_pairs(B, subOff, subIds, candA, candB, ncand, PR, SC, dc, stream);

@@ -152,3 +152,37 @@ def test_nonfinite_velocity_is_reported(gpu_lib):
     with pytest.raises(native.AmError) as e:
         g.step(DT)
     assert e.value.code == -3
+
+
+def test_context_reused_for_new_scenes(gpu_lib):
+    """One context given a second scene (and then a batch) steps it exactly
+    as a fresh context does: every device buffer of the first scene is
+    released and allocated anew."""
+    import ctypes as C
+    from adaptivemerging_gb300 import native
+    P = params(friction=0.6, iterations=40)
+    first = scenes.tower(6, seed=1)
+    second = scenes.random_pile(14, seed=3, kinds=("box", "sphere"))
+    g = native.System(first, P)
+    for _ in range(20):
+        g.step(0.01)
+    s2 = second.struct()
+    g._check(native.lib().am_set_scene(g.h, C.byref(s2)))
+    g._s, g.n, g.scene = s2, second.n, second
+    fresh = native.System(second, P)
+    for _ in range(30):
+        g.step(0.01)
+        fresh.step(0.01)
+    assert np.array_equal(g.bodies()["x"], fresh.bodies()["x"])
+    assert np.array_equal(g.contacts()["lambda"], fresh.contacts()["lambda"])
+    # the same context loaded with a batch afterwards
+    bins = [scenes.bin_scene(n, 70 + n, gap=-0.001) for n in (25, 60)]
+    arr = (native.abi.am_scene * len(bins))(*[b.struct() for b in bins])
+    g._check(native.lib().am_set_batch(g.h, arr, len(bins)))
+    g._check(native.lib().am_set_batch_options(g.h, 0, 1e-6, 10))
+    g.n = sum(b.n for b in bins)
+    ref = native.BatchSystem(bins, P, threads=0, residual_target=1e-6, check_every=10)
+    for _ in range(5):
+        g.step(0.005)
+        ref.step(0.005)
+    assert np.array_equal(g.bodies()["x"], ref.bodies()["x"])
