@@ -125,6 +125,7 @@ struct DCount {
     int n_prev;      // contacts in the previous buffer
     unsigned long long reschk[2];  // residual-target check of the coloured solve (double bits, by check parity)
     unsigned long long lamchk[2];
+    int stage_ovf;   // the staged narrow phase met a pair with more contacts than it keeps
 };
 
 // ---- kernels / launchers (defined in the .cu files) ----------------------
@@ -141,7 +142,8 @@ int launch_broadphase(const DBodies& B, const DNodes& N, const int* top, int nto
 void launch_expand_pairs(const DBodies& B, const int* sub_off, const int* sub_ids, const int* candA,
                          const int* candB, int ncand, DPairs& P, Scratch& sc, DCount* dc, cudaStream_t s);
 void launch_narrow(const DBodies& B, const DNodes& N, DPairs& P, DContacts& C, Scratch& sc, DCount* dc,
-                   bool emit, cudaStream_t s);
+                   bool emit, cudaStream_t s, double* sd = nullptr, int* si = nullptr, int* ovf = nullptr);
+int narrow_stage_slots();
 void launch_scan(const int* in, int* out, int n, Scratch& sc, int* total, cudaStream_t s);
 
 // solve.cu

@@ -174,6 +174,11 @@ struct Ctx {
     int* pairCls = nullptr;      // narrow-phase order: per-class counters
     unsigned* broadMask = nullptr;   // broad phase: hit mask per row and 32-pair chunk
     size_t broadMaskCap = 0;
+    // staged narrow phase: raw contacts per pair (7 doubles + 5 ints per slot)
+    bool narrowStageable = false;    // no body is a sphere tree of more than one node
+    double* stageD = nullptr;
+    int* stageI = nullptr;
+    size_t stageCap = 0;
     DHash H;
     Scratch SC;
     DCount* dc = nullptr;

@@ -869,11 +869,73 @@ __global__ void k_narrow_emit(DBodies B, DNodes N, DPairs P, DContacts C, DCount
     }
 }
 
+// Staged narrow phase (one collider pass): when no pair can yield more than
+// NSTAGE contacts (boxes, planes and single-sphere trees), the record pass
+// runs the colliders once, counting and keeping each pair's raw contacts
+// (point, normal, depth, BV ids, info, bodies) in emission order; after the
+// scan the set pass writes Contact.set for them at the pair's offset.  The
+// result is the two-pass result: the same emitter arguments in the same
+// order.  A pair that yields more than NSTAGE raises *stageOvf, and the step
+// falls back to the emit pass.
+static const int NSTAGE = 8;
+struct StageEmit {
+    double* sd;      // 7 doubles per staged contact: point, normal, depth
+    int* si;         // 5 ints: body1, body2, bv1, bv2, info
+    int base, n;
+    int* ovf;
+    __device__ void operator()(int b1, int b2, v3 pW, v3 nW, int bv1, int bv2, int info, double cv) {
+        if (n < NSTAGE) {
+            size_t q = (size_t)base * NSTAGE + n;
+            double* d = sd + 7 * q;
+            d[0] = pW.x; d[1] = pW.y; d[2] = pW.z; d[3] = nW.x; d[4] = nW.y; d[5] = nW.z; d[6] = cv;
+            int* e = si + 5 * q;
+            e[0] = b1; e[1] = b2; e[2] = bv1; e[3] = bv2; e[4] = info;
+        } else {
+            *ovf = 1;
+        }
+        n++;
+    }
+};
+
+__global__ void k_narrow_record(DBodies B, DNodes N, DPairs P, DCount* dc, double* sd, int* si, int* ovf) {
+    int n = dc->n_pairs;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int i = P.perm[j];
+        StageEmit e{sd, si, i, 0, ovf};
+        int err = 0;
+        narrow_pair(B, N, P.a[i], P.b[i], e, &err);
+        if (err) dc->error = err;
+        P.count[i] = e.n;
+    }
+}
+
+__global__ void k_narrow_set(DBodies B, DPairs P, DContacts C, DCount* dc, const double* sd, const int* si) {
+    int n = dc->n_pairs;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int i = P.perm[j];
+        WriteEmit e{&B, &C, P.off[i], 0, i, &dc->overflow};
+        const int cnt = P.count[i];
+        for (int k = 0; k < cnt; k++) {
+            size_t q = (size_t)i * NSTAGE + k;
+            const double* d = sd + 7 * q;
+            const int* x = si + 5 * q;
+            e(x[0], x[1], mk(d[0], d[1], d[2]), mk(d[3], d[4], d[5]), x[2], x[3], x[4], d[6]);
+        }
+    }
+}
+
+int narrow_stage_slots() { return NSTAGE; }
+
 void launch_narrow(const DBodies& B, const DNodes& N, DPairs& P, DContacts& C, Scratch& sc, DCount* dc,
-                   bool emit, cudaStream_t s) {
+                   bool emit, cudaStream_t s, double* sd, int* si, int* ovf) {
     (void)sc;
-    if (!emit) k_narrow_count<<<4 * 152, 128, 0, s>>>(B, N, P, dc);
-    else k_narrow_emit<<<4 * 152, 128, 0, s>>>(B, N, P, C, dc);
+    if (sd) {
+        if (!emit) k_narrow_record<<<4 * 152, 128, 0, s>>>(B, N, P, dc, sd, si, ovf);
+        else k_narrow_set<<<4 * 152, 128, 0, s>>>(B, P, C, dc, sd, si);
+    } else {
+        if (!emit) k_narrow_count<<<4 * 152, 128, 0, s>>>(B, N, P, dc);
+        else k_narrow_emit<<<4 * 152, 128, 0, s>>>(B, N, P, C, dc);
+    }
     AM_LAUNCHED(1);
 }
 

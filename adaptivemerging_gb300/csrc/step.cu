@@ -342,6 +342,9 @@ void Ctx::release() {
     pairCls = nullptr;
     broadMask = nullptr;
     broadMaskCap = 0;
+    stageD = nullptr;
+    stageI = nullptr;
+    stageCap = 0;
     bCS = nullptr;
 }
 
@@ -436,6 +439,9 @@ int Ctx::setScene(const am_scene& s) {
         cudaDeviceGetAttribute(&g_numSMs, cudaDevAttrMultiProcessorCount, dev);
     }
     nScene = s.n_bodies;
+    narrowStageable = true;   // boxes, planes and single spheres: at most 8 contacts per pair
+    for (int i = 0; i < s.n_bodies; i++)
+        if (s.body_root[i] >= 0 && s.node_nchild[s.body_root[i]] > 0) narrowStageable = false;
     host.init(s, P);
     int cap = host.cap;
     B.n = cap;
@@ -643,19 +649,40 @@ int Ctx::collisionDetection() {
     nPairs = npairs;
     cudaMemsetAsync(&dc->n_pairs, 0, sizeof(int), stream);
     cudaMemcpyAsync(&dc->n_pairs, &nPairs, sizeof(int), cudaMemcpyHostToDevice, stream);
+    // staged narrow phase (colliders run once) when no pair can exceed the
+    // staging slots and the staging fits 512 MB; otherwise count, then emit
+    double* sd = nullptr;
+    int* si = nullptr;
+    if (npairs > 0 && narrowStageable) {
+        size_t slots = (size_t)npairs * narrow_stage_slots();
+        if (slots * (7 * sizeof(double) + 5 * sizeof(int)) <= ((size_t)512 << 20)) {
+            if (slots > stageCap) {
+                size_t cap = slots + slots / 2;
+                if (alloc(&stageD, 7 * cap) || alloc(&stageI, 5 * cap)) return AM_E_CUDA;
+                stageCap = cap;
+            }
+            sd = stageD;
+            si = stageI;
+        }
+    }
     if (npairs > 0) {
         if (!pairCls && alloc(&pairCls, 16)) return AM_E_CUDA;
         launch_pair_order(B, PR, npairs, pairCls, stream);
-        launch_narrow(B, N, PR, C[cur], SC, dc, false, stream);
+        if (sd) cudaMemsetAsync(&dc->stage_ovf, 0, sizeof(int), stream);
+        launch_narrow(B, N, PR, C[cur], SC, dc, false, stream, sd, si, &dc->stage_ovf);
         if ((r = ensureScratch(npairs + 1))) return r;
         launch_scan(PR.count, PR.off, npairs, SC, &dc->n_contacts, stream);
         if ((r = readCounts())) return r;
         nContacts = hc->n_contacts;
+        if (sd && hc->stage_ovf) {   // a pair kept more contacts than staged: emit pass
+            sd = nullptr;
+            si = nullptr;
+        }
     } else {
         nContacts = 0;
     }
     if ((r = ensureContacts(nContacts))) return r;
-    if (nContacts > 0) launch_narrow(B, N, PR, C[cur], SC, dc, true, stream);
+    if (nContacts > 0) launch_narrow(B, N, PR, C[cur], SC, dc, true, stream, sd, si, nullptr);
     return AM_OK;
 }
 
