@@ -183,6 +183,25 @@ __device__ __forceinline__ bool far_apart32(float4 a, float4 b) {
     return d2 > T * T;
 }
 
+// True only when the FP32 distance proves the centres closer than the sum of
+// the radii, i.e. when the exact FP64 quick exit would accept the pair's
+// geometry too (the same margin as far_apart32, on the other side).
+__device__ __forceinline__ bool near32(float4 a, float4 b) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    float d2 = dx * dx + dy * dy + dz * dz;
+    float size = 1.f + fabsf(a.x) + fabsf(a.y) + fabsf(a.z) + fabsf(b.x) + fabsf(b.y) + fabsf(b.z);
+    float T = (a.w + b.w) * 0.99999f - 1e-6f * size;
+    return T > 0.f && d2 < T * T;
+}
+
+// the pair tests of pair_may_touch that come before the geometry
+__device__ __forceinline__ bool pair_flags_allow(const DBodies& B, int a, int b) {
+    int fa = B.flags[a], fb = B.flags[b];
+    bool pa = fa & F_PINNED, pb = fb & F_PINNED;
+    if (pa && pb) return false;
+    return !((pa && (fb & F_SLEEPING)) || (pb && (fa & F_SLEEPING)));
+}
+
 // one warp per row i of the top-level list; ballot + popc keeps row-major order.
 // With `masks`, the count pass stores every 32-pair chunk's hit mask (row i,
 // chunk c at masks[i * mw + c]) and the emit pass reads them back instead of
@@ -208,9 +227,13 @@ __global__ void k_broad_rows(DBodies B, DNodes N, const int* top, int ntop, int*
         } else if (j < end) {
             int b = top[j];
             float4 cb = B.bc[b];
-            // the prefilter only removes pairs the exact test rejects as well
-            bool far = ca.w >= 0.f && cb.w >= 0.f && far_apart32(ca, cb);
-            hit = !far && pair_may_touch(B, N, a, b);
+            // FP32 decides the geometry where its margin proves the FP64 quick
+            // exit's answer (far: rejected, near: accepted); the band between
+            // takes the exact test
+            const bool prim = ca.w >= 0.f && cb.w >= 0.f;
+            if (prim && far_apart32(ca, cb)) hit = false;
+            else if (prim && near32(ca, cb)) hit = pair_flags_allow(B, a, b);
+            else hit = pair_may_touch(B, N, a, b);
         }
         unsigned m = __ballot_sync(0xffffffffu, hit);
         if (!WRITE && mrow && lane == 0) mrow[c] = m;
