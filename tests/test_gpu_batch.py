@@ -210,3 +210,56 @@ def test_batch_rejects_oversized_scene(gpu_lib):
     with pytest.raises(native.AmError) as e:
         g.step(DT)
     assert e.value.code == -2
+
+
+def _mixed_scenes():
+    """Scenes of every body kind the batch takes: sphere-tree clumps resting
+    1 mm into a plane, boxes and spheres in a bin, a short tower."""
+    b = scenes.Builder()
+    b.plane((0, 0, 0), (0, 1, 0))
+    rng = np.random.default_rng(11)
+    for k in range(6):
+        cen = rng.uniform(-0.08, 0.08, (5, 3))
+        rad = rng.uniform(0.03, 0.06, 5)
+        low = float((cen[:, 1] - rad).min())
+        b.clump(cen, rad, (0.5 * k, -low - 0.001, 0.0), density=800.0)
+    b.box((0.3, 0.3, 0.3), (0.25, 0.149, 0.5), density=500.0)
+    clumps = b.build()
+    return [clumps, scenes.bin_scene(45, 77, gap=-0.001), scenes.tower(5, seed=3)]
+
+
+def test_batch_mixed_bodies_compliance_restitution(gpu_lib):
+    """Clumps, boxes and spheres with compliance and restitution on: the first
+    step's contacts (two-pass narrow phase, trees present) equal each scene's
+    oracle bit for bit, and the FP32 solve converges to the oracle's FP64
+    multipliers."""
+    from adaptivemerging_gb300 import native
+    sc = _mixed_scenes()
+    P = params(friction_override=0, iterations=4000, tolerance=0.0, enable_compliance=1, compliance=1e-3,
+               restitution=0.3)
+    g = native.BatchSystem(sc, P, threads=0, residual_target=0.0, check_every=0)
+    g.collision_detection(DT)
+    parts = _split(g.contacts(), sc)
+    for k, s in enumerate(sc):
+        o = Oracle(s, P)
+        o.begin_step()
+        o.collide()
+        msg = compare_contacts(parts[k], o.contacts(),
+                               fields=("body1", "body2", "bv1", "bv2", "info", "frame", "jac", "violation"))
+        assert msg is None, f"scene {k}: {msg}"
+    g2 = native.BatchSystem(sc, P, threads=0, residual_target=0.0, check_every=0)
+    g2.step(DT)
+    parts = _split(g2.contacts(), sc)
+    worst, n = 0.0, 0
+    for k, s in enumerate(sc):
+        o = Oracle(s, P)
+        o.step(DT)
+        co = o.contacts()
+        assert np.array_equal(parts[k]["body1"], co["body1"]) and np.array_equal(parts[k]["info"], co["info"])
+        if len(co["lambda"]):
+            scale = max(1.0, float(np.abs(co["lambda"]).max()))
+            worst = max(worst, float(np.abs(parts[k]["lambda"] - co["lambda"]).max()) / scale)
+            n += len(co["lambda"])
+    assert n > 50
+    print(f"mixed batch: {n} contacts, rel err {worst:.2e}")
+    assert worst <= 2e-4
