@@ -118,8 +118,7 @@ struct DCount {
     int error;       // AM_E_* raised on device
     unsigned long long maxchg[2];  // max |delta lambda| (bits of a non-negative double) per sweep parity
     int n_colours;
-    int bar_count;
-    int bar_gen;
+    int bar_count;   // grid-barrier arrivals of the running cooperative sweep (counts up)
     double res_abs;  // residual
     double lam_max;
     int n_prev;      // contacts in the previous buffer
@@ -161,8 +160,11 @@ void colour_groups(const DBodies& B, const DContacts& C, DPairs& P, int npairs, 
                    DCount* dc, Scratch& sc, cudaStream_t s);
 void launch_pgs_fast(const DBodies& B, DContacts& C, DPairs& P, const int* groupOrder, const int* colourOff,
                      int ncol, int nc, int iters, double omega, double comp, double tol, bool early, int fo,
-                     double fv, double slide, double* Mj, double* invD, int mcap, DCount* dc, int gridBlocks,
+                     double fv, double slide, double* Mj, double* K, int mcap, DCount* dc, int gridBlocks,
                      cudaStream_t s, double resTol = 0.0, int check = 0);
+// rows of the coloured solve's per-contact constant table (1/(D+c), A, q,
+// couplings, friction coefficient), each `mcap` doubles
+int pgs_fast_krows();
 void launch_residual(const DBodies& B, DContacts& C, int nc, double comp, int frictionOv, double frictionVal,
                      DCount* dc, cudaStream_t s);
 void launch_bpc_keep(const DContacts& C, DPairs& P, int npairs, cudaStream_t s);

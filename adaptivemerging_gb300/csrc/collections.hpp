@@ -203,7 +203,7 @@ struct Ctx {
     int coopBlocks = 0;
     std::vector<int> hColOff;    // colour offsets of the coloured full solve (host copy)
     double* Mj = nullptr;     // coloured sweep: M^-1 J^T per row and lane (36 per contact)
-    double* invD = nullptr;   // 1/(D + c) per row
+    double* invD = nullptr;   // coloured sweep constants per contact: 1/(D + c), A, q per row, couplings, mu
     int mjCap = 0;
     int nScene = 0, ntop = 0, nContacts = 0, nPrev = 0, nPairs = 0;
     int totalSteps = 0;

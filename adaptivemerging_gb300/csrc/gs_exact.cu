@@ -24,38 +24,10 @@
 #include "am_ctx.hpp"
 #include "am_dev.cuh"
 #include "collections.hpp"
+#include "grid_sync.cuh"
 
 namespace am {
 using namespace amd;
-
-__device__ __forceinline__ bool barrier_x(DCount* dc, int nblocks) {
-    if (nblocks == 1) {   // one block: the block barrier orders global memory too
-        __syncthreads();
-        return *(volatile int*)&dc->error == 0;
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile int* gen = &dc->bar_gen;
-        int g0 = *gen;
-        __threadfence();
-        int arrived = atomicAdd(&dc->bar_count, 1);
-        if (arrived == nblocks - 1) {
-            dc->bar_count = 0;
-            __threadfence();
-            atomicAdd(&dc->bar_gen, 1);
-        } else {
-            long long spins = 0;
-            while (*gen == g0) {
-                if (++spins > (1ll << 24)) { atomicExch(&dc->error, AM_E_TIMEOUT); break; }
-                __nanosleep(20);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return *(volatile int*)&dc->error == 0;
-}
 
 // J . dv in the reference's order; result valid in every lane
 __device__ __forceinline__ double jdv_exact(double p) {
@@ -94,6 +66,7 @@ __global__ void k_gs_levels(DBodies B, DContacts C, const int* order, const int*
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (nblocks * blockDim.x) >> 5;
     const int cap = C.cap;
+    unsigned target = 0;
     const bool act = lane < 12;
     const int q = lane / 3;                 // 0 a.v, 1 a.w, 2 b.v, 3 b.w
     const int side = lane / 6;
@@ -117,7 +90,7 @@ __global__ void k_gs_levels(DBodies B, DContacts C, const int* order, const int*
             }
             if (act) __stcg(B.dv + 6 * body + comp6, dv);
         }
-        if (!barrier_x(dc, nblocks)) return;
+        if (!grid_barrier_counted(dc, nblocks, target)) return;
     }
     int iter = iters, done = 0;
     double change = 0;
@@ -181,7 +154,7 @@ __global__ void k_gs_levels(DBodies B, DContacts C, const int* order, const int*
             }
             if (L == nLevels - 1 && lane == 0 && mx > 0)
                 atomicMax(&dc->maxchg[par], (unsigned long long)__double_as_longlong(mx));
-            if (!barrier_x(dc, nblocks)) return;
+            if (!grid_barrier_counted(dc, nblocks, target)) return;
         }
         iter--;
         done++;
@@ -231,7 +204,7 @@ void launch_gs_levels(const DBodies& B, DContacts& C, const int* order, const in
                       DCount* dc, int blocks, cudaStream_t s) {
     if (nLevels <= 0) return;
     cudaMemsetAsync(&dc->maxchg, 0, sizeof(unsigned long long) * 2, s);
-    cudaMemsetAsync(&dc->bar_count, 0, sizeof(int) * 2, s);
+    cudaMemsetAsync(&dc->bar_count, 0, sizeof(int), s);
     int earlyI = early ? 1 : 0;
     DBodies Bc = B;
     void* args[] = {&Bc, &C, (void*)&order, (void*)&levelOff, &nLevels, &iters, &omega, &comp, &tol, &earlyI,

@@ -395,39 +395,6 @@ void colour_groups(const DBodies& B, const DContacts& C, DPairs& P, int npairs, 
     AM_LAUNCHED(1);
 }
 
-// ---------------------------------------------------------------------------
-// bounded grid barrier for the cooperative sweep kernel.  Every wait has an
-// iteration limit; on expiry the kernel records AM_E_TIMEOUT and all blocks
-// leave at their next barrier check.
-__device__ __forceinline__ bool grid_barrier(DCount* dc, int nblocks) {
-    if (nblocks == 1) {   // one block: the block barrier orders global memory too
-        __syncthreads();
-        return *(volatile int*)&dc->error == 0;
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile int* gen = &dc->bar_gen;
-        int g0 = *gen;
-        __threadfence();
-        int arrived = atomicAdd(&dc->bar_count, 1);
-        if (arrived == nblocks - 1) {
-            dc->bar_count = 0;
-            __threadfence();
-            atomicAdd(&dc->bar_gen, 1);
-        } else {
-            long long spins = 0;
-            while (*gen == g0) {
-                if (++spins > (1ll << 24)) { atomicExch(&dc->error, AM_E_TIMEOUT); break; }
-                __nanosleep(32);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return *(volatile int*)&dc->error == 0;
-}
-
 __device__ __forceinline__ double warp_max(double v) {
     for (int o = 16; o > 0; o >>= 1) v = jmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;

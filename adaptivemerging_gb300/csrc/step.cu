@@ -738,7 +738,7 @@ int Ctx::runPGS(int nc, const int* order, int iters, bool inColl, double dt, boo
         }
         if (nc > mjCap) {
             int cap2 = std::max(nc + nc / 2, 1024);
-            if (alloc(&Mj, 36 * (size_t)cap2) || alloc(&invD, 3 * (size_t)cap2)) return AM_E_CUDA;
+            if (alloc(&Mj, 36 * (size_t)cap2) || alloc(&invD, (size_t)pgs_fast_krows() * cap2)) return AM_E_CUDA;
             mjCap = cap2;
         }
         // 8 half-warp groups per block; enough blocks for every group of the
