@@ -381,7 +381,7 @@ __global__ void k_colour_place(DPairs P, int npairs, const int* colourOf, const 
     groupOrder[pos] = g;
 }
 
-// host-side driver for the colouring (needs the contact buffer for solve bodies)
+// host-side launcher of the colouring (needs the contact buffer for solve bodies)
 void colour_groups(const DBodies& B, const DContacts& C, DPairs& P, int npairs, int* colourOf, int* colourCnt,
                    int* colourOff, int* fill, int* groupOrder, int maxC, unsigned long long* bodyMax, int nbodies,
                    DCount* dc, Scratch& sc, cudaStream_t s) {
