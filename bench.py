@@ -37,7 +37,7 @@ import numpy as np  # noqa: E402
 from adaptivemerging_gb300 import abi, scenes  # noqa: E402
 
 METRIC = "sim steps/s at LCP residual<=1e-6: warm-start+batched vs plain GPU PGS, 1 GB300"
-FP64_BYTES_PER_CONTACT_SWEEP = 728   # J 288 + M^-1 J^T 288 + b 24 + lambda r/w 48 + A, q, couplings, mu 80
+FP64_BYTES_PER_CONTACT_SWEEP = 736   # J 288 + b,D 48 + lambda r/w 48 + dv of 2 bodies r/w 192 + minv,jinv 160
 FP32_BYTES_PER_CONTACT_SWEEP = 368   # the same quantities in FP32
 BATCH_SCENES = 512
 BATCH_SAMPLE_STRIDE = 32             # CPU baseline: every 32nd scene, one core
