@@ -48,14 +48,40 @@ __device__ __forceinline__ double mu_exact(const DBodies& B, const DContacts& C,
     return (f1 + f2) / 2.;
 }
 
-// PGS.updateDeltaVwithLambdai for lane k: (minv * lambda) * J.v + dv, lambda * (jinv J.w) + dv
-__device__ __forceinline__ double dv_update(double dv, double lam, int lane, double m1, double m2, double j,
-                                            double ia) {
-    if (lane < 3) return (m1 * lam) * j + dv;
-    if (lane < 6) return lam * ia + dv;
-    if (lane < 9) return (m2 * lam) * j + dv;
-    if (lane < 12) return lam * ia + dv;
-    return dv;
+// PGS.updateDeltaVwithLambdai for lane k: (minv * lambda) * J.v + dv on the
+// linear lanes, lambda * (jinv J.w) + dv on the angular lanes.  One
+// branch-free form serves every lane, (s * lambda) * e + dv with s = minv and
+// e = J.v, or s = 1 and e = jinv J.w: 1 * lambda is lambda exactly, so the
+// angular lanes round as lambda * e + dv does.  GB300 issues each FP64 warp
+// instruction once for all lanes, so one form costs 3 instructions where
+// per-lane branches cost one set per branch.
+__device__ __forceinline__ double dv_update(double dv, double lam, bool act, double s, double e) {
+    return act ? (s * lam) * e + dv : dv;
+}
+
+// Math.max / Math.min (Java semantics: NaN propagates from either argument,
+// -0 < +0) on IEEE bit patterns in the integer pipe.  Non-NaN doubles compare
+// like their keys: the bits for a positive sign, the bits with the magnitude
+// inverted for a negative one.  Results are the same bits as jmax / jmin.
+__device__ __forceinline__ bool nan_bits(long long b) { return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll; }
+__device__ __forceinline__ long long order_key(long long b) { return b < 0 ? b ^ 0x7fffffffffffffffll : b; }
+__device__ __forceinline__ double jmax_i(double a, double b) {
+    long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    if (nan_bits(x)) return a;
+    if (nan_bits(y)) return b;
+    return order_key(x) >= order_key(y) ? a : b;
+}
+__device__ __forceinline__ double jmin_i(double a, double b) {
+    long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    if (nan_bits(x)) return a;
+    if (nan_bits(y)) return b;
+    return order_key(x) <= order_key(y) ? a : b;
+}
+__device__ __forceinline__ double abs_i(double a) {
+    return __longlong_as_double(__double_as_longlong(a) & 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ double neg_i(double a) {
+    return __longlong_as_double(__double_as_longlong(a) ^ (long long)0x8000000000000000ull);
 }
 
 __global__ void k_gs_levels(DBodies B, DContacts C, const int* order, const int* levelOff, int nLevels, int iters,
@@ -78,15 +104,15 @@ __global__ void k_gs_levels(DBodies B, DContacts C, const int* order, const int*
             int c = order[k];
             int s1 = C.sb1[c], s2 = C.sb2[c];
             int body = side == 0 ? s1 : s2;
-            double m1 = B.minv[s1], m2 = B.minv[s2];
+            double sc = (q == 0) ? B.minv[s1] : (q == 2) ? B.minv[s2] : 1.0;
             double dv = act ? __ldcg(B.dv + 6 * body + comp6) : 0.0;
             for (int r = 0; r < 3; r++) {
                 double lam = C.lam[r * cap + c];
-                double j = act ? C.J[(12 * r + lane) * cap + c] : 0.0;
-                double ia = 0.0;
-                if (q == 1) ia = C.Ia[(3 * r + comp6 - 3) * cap + c];
-                else if (q == 3) ia = C.Ib[(3 * r + comp6 - 3) * cap + c];
-                dv = dv_update(dv, lam, lane, m1, m2, j, ia);
+                double e = 0.0;
+                if (q == 0 || q == 2) e = C.J[(12 * r + lane) * cap + c];
+                else if (q == 1) e = C.Ia[(3 * r + comp6 - 3) * cap + c];
+                else if (q == 3) e = C.Ib[(3 * r + comp6 - 3) * cap + c];
+                dv = dv_update(dv, lam, act, sc, e);
             }
             if (act) __stcg(B.dv + 6 * body + comp6, dv);
         }
@@ -102,14 +128,14 @@ __global__ void k_gs_levels(DBodies B, DContacts C, const int* order, const int*
                 int c = order[k];
                 int s1 = C.sb1[c], s2 = C.sb2[c];
                 int body = side == 0 ? s1 : s2;
-                double m1 = B.minv[s1], m2 = B.minv[s2];
+                double sc = (q == 0) ? B.minv[s1] : (q == 2) ? B.minv[s2] : 1.0;
                 double dv = act ? __ldcg(B.dv + 6 * body + comp6) : 0.0;
-                double j[3], ia[3];
+                double j[3], e[3];
                 for (int r = 0; r < 3; r++) {
                     j[r] = act ? C.J[(12 * r + lane) * cap + c] : 0.0;
-                    ia[r] = 0.0;
-                    if (q == 1) ia[r] = C.Ia[(3 * r + comp6 - 3) * cap + c];
-                    else if (q == 3) ia[r] = C.Ib[(3 * r + comp6 - 3) * cap + c];
+                    e[r] = j[r];
+                    if (q == 1) e[r] = C.Ia[(3 * r + comp6 - 3) * cap + c];
+                    else if (q == 3) e[r] = C.Ib[(3 * r + comp6 - 3) * cap + c];
                 }
                 // normal direction
                 double Jd = jdv_exact(j[0] * dv);
@@ -117,10 +143,10 @@ __global__ void k_gs_levels(DBodies B, DContacts C, const int* order, const int*
                 double prev = l0;
                 double D = C.bD[3 * cap + c];
                 l0 = (D * l0 - omega * (C.bD[c] + Jd)) / (D + comp);
-                l0 = jmax(0.0, l0);
+                l0 = jmax_i(0.0, l0);
                 double diff = l0 - prev;
-                dv = dv_update(dv, diff, lane, m1, m2, j[0], ia[0]);
-                mx = jmax(mx, fabs(diff));
+                dv = dv_update(dv, diff, act, sc, e[0]);
+                mx = jmax_i(mx, abs_i(diff));
                 double mu = mu_exact(B, C, c, fo, fv);
                 double lr[3];
                 lr[0] = l0;
@@ -131,11 +157,11 @@ __global__ void k_gs_levels(DBodies B, DContacts C, const int* order, const int*
                     double Dr = C.bD[(3 + r) * cap + c];
                     l = (Dr * l - omega * (C.bD[r * cap + c] + Jd)) / (Dr + comp);
                     double lim = mu * l0;
-                    l = jmax(l, -lim);
-                    l = jmin(l, lim);
+                    l = jmax_i(l, neg_i(lim));
+                    l = jmin_i(l, lim);
                     diff = l - prev;
-                    dv = dv_update(dv, diff, lane, m1, m2, j[r], ia[r]);
-                    mx = jmax(mx, fabs(diff));
+                    dv = dv_update(dv, diff, act, sc, e[r]);
+                    mx = jmax_i(mx, abs_i(diff));
                     lr[r] = l;
                 }
                 if (iter == 1) {   // Contact.updateContactState (Contact.java:385-398)
