@@ -9,6 +9,7 @@
 // reference arithmetic.
 #pragma once
 #include <cstdint>
+#include <cstring>
 
 namespace amd {
 
@@ -187,6 +188,52 @@ __host__ __device__ __forceinline__ double jmin(double a, double b) {
     if (a != a) return a;
     if (a == 0.0 && b == 0.0 && signbit(b)) return b;
     return (a <= b) ? a : b;
+}
+
+// The same Math.max / Math.min on IEEE bit patterns, for the sweeps where
+// every FP64 instruction costs a full pass of the FP64 pipe: a NaN test on
+// the bits, then an integer comparison of keys that order non-NaN doubles as
+// their values do (the bits for a positive sign, the bits with the magnitude
+// inverted for a negative one, so -0 < +0).  The results are the same bits as
+// jmax / jmin for every pair of arguments.
+__host__ __device__ __forceinline__ long long dbits(double x) {
+#ifdef __CUDA_ARCH__
+    return __double_as_longlong(x);
+#else
+    long long b;
+    std::memcpy(&b, &x, sizeof b);
+    return b;
+#endif
+}
+__host__ __device__ __forceinline__ double dfrombits(long long b) {
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double(b);
+#else
+    double x;
+    std::memcpy(&x, &b, sizeof x);
+    return x;
+#endif
+}
+__host__ __device__ __forceinline__ bool nan_bits(long long b) {
+    return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+__host__ __device__ __forceinline__ long long order_key(long long b) { return b < 0 ? b ^ 0x7fffffffffffffffll : b; }
+__host__ __device__ __forceinline__ double jmax_i(double a, double b) {
+    const long long x = dbits(a), y = dbits(b);
+    if (nan_bits(x)) return a;
+    if (nan_bits(y)) return b;
+    return order_key(x) >= order_key(y) ? a : b;
+}
+__host__ __device__ __forceinline__ double jmin_i(double a, double b) {
+    const long long x = dbits(a), y = dbits(b);
+    if (nan_bits(x)) return a;
+    if (nan_bits(y)) return b;
+    return order_key(x) <= order_key(y) ? a : b;
+}
+// |a| and -a by the sign bit (the same bits as fabs and unary minus)
+__host__ __device__ __forceinline__ double abs_i(double a) { return dfrombits(dbits(a) & 0x7fffffffffffffffll); }
+__host__ __device__ __forceinline__ double neg_i(double a) {
+    return dfrombits(dbits(a) ^ (long long)0x8000000000000000ull);
 }
 
 // Deterministic sine/cosine for the Rodrigues rotation update: Cody-Waite

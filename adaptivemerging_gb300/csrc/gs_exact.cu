@@ -59,31 +59,6 @@ __device__ __forceinline__ double dv_update(double dv, double lam, bool act, dou
     return act ? (s * lam) * e + dv : dv;
 }
 
-// Math.max / Math.min (Java semantics: NaN propagates from either argument,
-// -0 < +0) on IEEE bit patterns in the integer pipe.  Non-NaN doubles compare
-// like their keys: the bits for a positive sign, the bits with the magnitude
-// inverted for a negative one.  Results are the same bits as jmax / jmin.
-__device__ __forceinline__ bool nan_bits(long long b) { return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll; }
-__device__ __forceinline__ long long order_key(long long b) { return b < 0 ? b ^ 0x7fffffffffffffffll : b; }
-__device__ __forceinline__ double jmax_i(double a, double b) {
-    long long x = __double_as_longlong(a), y = __double_as_longlong(b);
-    if (nan_bits(x)) return a;
-    if (nan_bits(y)) return b;
-    return order_key(x) >= order_key(y) ? a : b;
-}
-__device__ __forceinline__ double jmin_i(double a, double b) {
-    long long x = __double_as_longlong(a), y = __double_as_longlong(b);
-    if (nan_bits(x)) return a;
-    if (nan_bits(y)) return b;
-    return order_key(x) <= order_key(y) ? a : b;
-}
-__device__ __forceinline__ double abs_i(double a) {
-    return __longlong_as_double(__double_as_longlong(a) & 0x7fffffffffffffffll);
-}
-__device__ __forceinline__ double neg_i(double a) {
-    return __longlong_as_double(__double_as_longlong(a) ^ (long long)0x8000000000000000ull);
-}
-
 __global__ void k_gs_levels(DBodies B, DContacts C, const int* order, const int* levelOff, int nLevels, int iters,
                             double omega, double comp, double tol, int early, int fo, double fv, double slide,
                             DCount* dc) {
