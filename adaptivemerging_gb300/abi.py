@@ -22,6 +22,8 @@ AM_E_STATE = -6
 AM_BOX, AM_SPHERE, AM_PLANE, AM_TREE = 0, 1, 2, 3
 AM_STATE_BROKEN, AM_STATE_ONEDGE, AM_STATE_CLEAR = 0, 1, 2
 AM_BV_NULL = -1
+# device phases of a batched step (am_get_step_phases)
+STEP_PHASES = ("detection", "warm_start", "solve_setup", "sweeps", "integration", "statistics")
 AM_ORDER_REFERENCE, AM_ORDER_COLOURED = 0, 1
 # am_get_phase_times order: the reference's CSV time columns
 # (RigidBodySystem.exportDataToFile, RigidBodySystem.java:495-542)

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libam.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["collide.cu", "solve.cu", "step.cu", "capi.cu", "pgs_fast.cu", "merging.cu", "gs_exact.cu", "batch.cu", "learned.cu"]
+SOURCES = ["collide.cu", "solve.cu", "step.cu", "capi.cu", "pgs_fast.cu", "merging.cu", "gs_exact.cu", "batch.cu", "learned.cu", "state.cu"]
 # translation units that may contract a*b+c (the coloured FP64 solve and the
 # FP32 batched and learned paths; none of them is part of the bit-exact path)
 FMA_OK = {"pgs_fast.cu", "batch.cu", "learned.cu"}

@@ -125,6 +125,7 @@ struct DCount {
     unsigned long long reschk[2];  // residual-target check of the coloured solve (double bits, by check parity)
     unsigned long long lamchk[2];
     int stage_ovf;   // the staged narrow phase met a pair with more contacts than it keeps
+    int spin_log2;   // grid barriers give up after 2^spin_log2 polls (0: 2^24)
 };
 
 // ---- kernels / launchers (defined in the .cu files) ----------------------
@@ -168,5 +169,9 @@ int pgs_fast_krows();
 void launch_residual(const DBodies& B, DContacts& C, int nc, double comp, int frictionOv, double frictionVal,
                      DCount* dc, cudaStream_t s);
 void launch_bpc_keep(const DContacts& C, DPairs& P, int npairs, cudaStream_t s);
+// a grid barrier that can never complete (its target counts one block more
+// than the grid holds), bounded by 2^spin_log2 polls: every block must give
+// up with AM_E_TIMEOUT in the status word and return
+void launch_barrier_timeout_check(DCount* dc, int spin_log2, cudaStream_t s);
 
 }  // namespace am

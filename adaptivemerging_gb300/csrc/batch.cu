@@ -489,7 +489,7 @@ __device__ __forceinline__ void pair_impulse(Pair& P, const Rec& c, const float*
 // evaluated as lam - (c lam + w) / (D + c), and the relaxation factor (1:
 // plain) scales 1 / (D + c).
 __device__ __forceinline__ void sweep_contact(Pair& P, const float* R, int slot, float* lp, float omega,
-                                              float comp, float relax) {
+                                              float comp, float relax, float* dOut) {
     Rec c;
     load_rec(R, slot, c);
     const float4 l = sld4(lp);
@@ -514,6 +514,9 @@ __device__ __forceinline__ void sweep_contact(Pair& P, const float* R, int slot,
     const float d1 = n1 - l.y;
     const float n2 = fminf(fmaxf(fmaf(c21, d1, fmaf(c20, d0, base[2])), -lim), lim);
     const float d2 = n2 - l.z;
+    dOut[0] = d0;
+    dOut[1] = d1;
+    dOut[2] = d2;
     *reinterpret_cast<float4*>(lp) = make_float4(n0, n1, n2, l.w);
     float F[3];
 #pragma unroll
@@ -543,10 +546,12 @@ __device__ __forceinline__ void res_contact(const Pair& P, const float* R, int s
     const float lq[3] = {l.x, l.y, l.z};
     float rv[3];
     rel_vel(P, c, rv);
+    // explicit roundings: every kernel that inlines this evaluates the same
+    // operations, so a scene stops at the same check whichever kernel solves it
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-        float w = c.bq[q] + fdot(c.f[q], rv) + comp * lq[q];
-        float z = lq[q] - w * c.iq[q];
+        float w = __fmaf_rn(comp, lq[q], __fadd_rn(c.bq[q], fdot(c.f[q], rv)));
+        float z = __fmaf_rn(-w, c.iq[q], lq[q]);
         if (q == 0) z = fmaxf(z, 0.f);
         else { float lim = l.w * l.x; z = fminf(fmaxf(z, -lim), lim); }
         rmax = fmaxf(rmax, fabsf(lq[q] - z));
@@ -561,24 +566,130 @@ __device__ __forceinline__ int final_state(const Pair& P, const float* R, int sl
     load_rec(R, slot, c);
     float rv[3];
     rel_vel(P, c, rv);
-    const float w1 = c.bq[1] + fdot(c.f[1], rv), w2 = c.bq[2] + fdot(c.f[2], rv);
+    const float w1 = __fadd_rn(c.bq[1], fdot(c.f[1], rv)), w2 = __fadd_rn(c.bq[2], fdot(c.f[2], rv));
     if (fabsf(lp[0]) <= 1e-14f) return AM_STATE_BROKEN;
     if (fabsf(w1) > slide || fabsf(w2) > slide) return AM_STATE_ONEDGE;
     return AM_STATE_CLEAR;
 }
 
+// ---------------------------------------------------------------------------
+// Nonsmooth nonlinear conjugate gradient (NNCG; Silcowitz, Niebe and Erleben,
+// 2010) around the projected Gauss-Seidel sweep.  With g the change of the
+// multipliers over one sweep and beta = |g_k|^2 / |g_k-1|^2: beta > 1
+// restarts (p = 0); otherwise lambda += beta p and p = beta p + g.  The
+// fixed point is that of PGS, so the residual stopping rule is unchanged.
+// The momentum's effect on delta-v, beta M^-1 J^T p, is kept per body as
+// q = M^-1 J^T p, which follows q = beta q + (the sweep's own delta-v
+// change); the momentum step is then one pass over slots and one over bodies,
+// with no colour order.
+//
+// |g|^2 must come out bit-identical whatever CTA size, size class, staging
+// or cluster solves the scene, and whatever order the groups of a colour
+// take (the colouring places them by atomic arrival).  So it is summed
+// exactly, in integers: each group's squared change (a float, summed over
+// its contacts in slot order) is scaled by 2^E and rounded to a 64-bit
+// integer, and integer sums do not depend on their order.  Four scales
+// E0 + 16j run side by side (E0 from the previous sweep's |g|^2, or a fixed
+// one on the first sweep); the finest whose total stays below 2^50 (so no
+// group was clamped) gives |g|^2.
+static const int NNCG_SCALES = 4;
+static const unsigned long long NNCG_CLAMP = 1ull << 50;
+
+// E0 of the sweep after one whose |g|^2 was gg (the first sweep: -10)
+__device__ __forceinline__ int nncg_e0(int it, float gg) {
+    if (it == 0) return -10;
+    const float x = fmaxf(gg, 0x1p-100f);
+    return 10 - ilogbf(x);
+}
+// one group's squared change at the four scales, added to acc
+__device__ __forceinline__ void nncg_acc(float gsq, int e0, unsigned long long* acc) {
+#pragma unroll
+    for (int j = 0; j < NNCG_SCALES; j++) {
+        const float y = ldexpf(gsq, e0 + 16 * j);
+        acc[j] += (y >= 0x1p50f) ? NNCG_CLAMP : (unsigned long long)__float2ull_rn(y);
+    }
+}
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+// a warp's accumulators into the CTA's shared totals (integer: any order)
+__device__ __forceinline__ void nncg_flush(unsigned long long* acc, unsigned long long* tot) {
+#pragma unroll
+    for (int j = 0; j < NNCG_SCALES; j++) {
+        const unsigned long long v = warp_sum_u64(acc[j]);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(tot + j, v);
+        acc[j] = 0ull;
+    }
+}
+// |g|^2 from the totals of the four scales
+__device__ __forceinline__ float nncg_gg(const unsigned long long* tot, int e0) {
+    int j = NNCG_SCALES - 1;
+    while (j > 0 && tot[j] >= NNCG_CLAMP) j--;
+    return ldexpf(__ull2float_rn(tot[j]), -(e0 + 16 * j));
+}
+// the sweep's squared change of one contact, accumulated in a fixed order
+__device__ __forceinline__ float sq3_acc(const float* d, float acc) {
+    return __fmaf_rn(d[2], d[2], __fmaf_rn(d[1], d[1], __fmaf_rn(d[0], d[0], acc)));
+}
+// beta of iteration `it` (0: the first sweep, no momentum); < 0 means restart
+__device__ __forceinline__ float nncg_beta(int it, float gg, float ggPrev) {
+    if (it == 0) return 0.f;
+    const float b = __fdiv_rn(gg, ggPrev);
+    return (b <= 1.f) ? b : -1.f;   // also restarts on 0 / 0 and overflow
+}
+// one slot: lambda (3 of l), g and p (gp[0..2], gp[4..6])
+__device__ __forceinline__ void nncg_slot(float* l, float* gp, int it, float beta) {
+    for (int q = 0; q < 3; q++) {
+        const float g = gp[q], p = gp[4 + q];
+        if (it == 0) {
+            gp[4 + q] = g;
+        } else if (beta < 0.f) {
+            gp[4 + q] = 0.f;
+        } else {
+            l[q] = __fmaf_rn(beta, p, l[q]);
+            gp[4 + q] = __fmaf_rn(beta, p, g);
+        }
+    }
+}
+// one body: delta-v (6), and dq = delta-v at the sweep's start (6), then q (6)
+__device__ __forceinline__ void nncg_body(float* dv, float* dq, int it, float beta) {
+    for (int k = 0; k < 6; k++) {
+        const float d = __fsub_rn(dv[k], dq[k]);
+        float v = dv[k], q = dq[6 + k];
+        if (it == 0) {
+            q = d;
+        } else if (beta < 0.f) {
+            q = 0.f;
+        } else {
+            v = __fmaf_rn(beta, q, v);
+            q = __fmaf_rn(beta, q, d);
+        }
+        dv[k] = v;
+        dq[k] = v;
+        dq[6 + k] = q;
+    }
+}
+
 // shared-memory layout of the sweep kernel (floats).  The staging arrays
 // hold two buffers of `cap` slots each (double buffering of chunks); a
 // resident scene uses both as one buffer of 2 cap slots.
+// With the conjugate-gradient acceleration on, a resident scene also keeps
+// per body delta-v at the sweep's start and q (12 floats) and per slot g and
+// p (8 floats, at the multipliers' permuted position); a streamed scene keeps
+// these in global memory.
 struct SweepSmem {
-    int dv, mv, ji, rec, lam, gi, gl, total;
-    __host__ __device__ SweepSmem(int nbMax, int cap) {
+    int dv, mv, ji, dq, rec, lam, gp, gi, gl, total;
+    __host__ __device__ SweepSmem(int nbMax, int cap, int accel = 0) {
         dv = 0;                // 6 floats per body (even offsets: 8-byte aligned)
         ji = 6 * nbMax;        // symmetric inverse inertia, 6 floats per body
-        mv = 12 * nbMax;
-        rec = (13 * nbMax + 3) & ~3;
+        dq = 12 * nbMax;       // accel: delta-v at sweep start and q, 12 floats per body
+        mv = dq + (accel ? 12 * nbMax : 0);
+        rec = (mv + nbMax + 3) & ~3;
         lam = rec + 2 * cap * RECS;
-        gi = lam + 8 * cap;
+        gp = lam + 8 * cap;
+        gi = gp + (accel ? 16 * cap : 0);
         gl = gi + 4 * cap;
         total = gl + 4 * cap;
     }
@@ -604,9 +715,10 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     const int* chunkK, const int* nChunks, const int* contactOf, const float* __restrict__ rec, float* lamS, int cap,
     int nbMax, int iters, float omega, float comp, float tolRel, int check, float slide, int* sceneSweeps,
     float* sceneRes, const float* lamAlt, int* sceneFall, int writeBack, int inner, float relax, int sym,
-    long long* trace, const int* lidOf, const int* bodyOf, const int* sceneActive) {
+    long long* trace, const int* lidOf, const int* bodyOf, const int* sceneActive, int accel, float* gpG,
+    float* dqG) {
     extern __shared__ float sm[];
-    const SweepSmem L(nbMax, cap);
+    const SweepSmem L(nbMax, cap, accel);
     const long long tStart = gtimer();
     float* dv = sm + L.dv;
     float* mv = sm + L.mv;
@@ -653,6 +765,14 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     const int2 lastG = gInfo[kS1 - 1];
     const int nslots = lastG.x + lastG.y - slotS0;
     const bool resident = nslots <= 2 * cap;
+    // conjugate-gradient state: shared memory for a resident scene, global
+    // memory (slot and body arrays of the whole batch) for a streamed one;
+    // |g|^2 totals by sweep parity
+    __shared__ unsigned long long s_tot[2][NNCG_SCALES];
+    float* sgp = sm + L.gp;
+    float* dqB = resident ? sm + L.dq : dqG + 12 * (size_t)b0;
+    unsigned long long acc[NNCG_SCALES] = {0ull, 0ull, 0ull, 0ull};
+    int e0 = 0, par = 0;
 
     // issue the asynchronous copy of groups [k0, k1) (and their slots) into
     // staging buffer `buf` (one commit group per call)
@@ -705,6 +825,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         // sweeps may pass over a group's contacts `inner` times: Gauss-Seidel
         // on the body pair's own block before the sweep moves on
         const int reps = op == OP_SWEEP ? inner : 1;
+        float gsq = 0.f;
         for (int rep = 0; rep < reps; rep++)
         for (int j = 0; j < cnt; j++) {
             const int slot = sl0 + j;
@@ -713,7 +834,17 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
             if (op == OP_WARM) {
                 warm_contact(P, R, slot, lp);
             } else if (op == OP_SWEEP) {
-                sweep_contact(P, R, slot, lp, omega, comp, relax);
+                float d[3];
+                sweep_contact(P, R, slot, lp, omega, comp, relax, d);
+                if (accel) {
+                    float* g = resident ? sgp + 8 * lam_pos(slot) : gpG + 8 * ((size_t)slA + j);
+                    if (rep > 0)
+                        for (int q = 0; q < 3; q++) d[q] = __fadd_rn(g[q], d[q]);
+                    g[0] = d[0];
+                    g[1] = d[1];
+                    g[2] = d[2];
+                    if (rep == reps - 1) gsq = sq3_acc(d, gsq);
+                }
             } else if (op == OP_RES) {
                 res_contact(P, R, slot, lp, comp, rmax, lmax);
             } else {
@@ -728,6 +859,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
             if (P.ma != 0.f) for (int q = 0; q < 3; q++) da[q] = make_float2(P.a[2 * q], P.a[2 * q + 1]);
             if (P.mb != 0.f) for (int q = 0; q < 3; q++) db[q] = make_float2(P.b[2 * q], P.b[2 * q + 1]);
         }
+        if (op == OP_SWEEP && accel) nncg_acc(gsq, e0, acc);
     };
     // one pass of `op` over the scene, colour by colour.  Resident: the whole
     // scene sits in the buffers and the chunks of one colour run together.
@@ -758,6 +890,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
                     int2 gi = sgi[k - kS0];
                     group(op, gi.x - slotS0, gi.x, gi.y, sgl[k - kS0]);
                 }
+                if (op == OP_SWEEP && accel && hh == nhead - 1) nncg_flush(acc, s_tot[par]);
                 __syncthreads();
             }
             return;
@@ -786,6 +919,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
                 int2 gi = gi0[k - k0];
                 group(op, buf * cap + gi.x - ss, gi.x, gi.y, gl0[k - k0]);
             }
+            if (op == OP_SWEEP && accel && m == nch - 1) nncg_flush(acc, s_tot[par]);
             __syncthreads();
             if (op == OP_SWEEP) {
                 unstage(buf, k0, k1);
@@ -819,10 +953,35 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
             sceneFall[s] = 0;
         }
         pass(OP_WARM, false);
+        float ggPrev = 0.f;
+        if (accel) {   // delta-v at the first sweep's start
+            for (int b = t; b < nbA; b += T)
+                for (int k = 0; k < 6; k++) dqB[12 * b + k] = dv[6 * b + k];
+            if (t < 2 * NNCG_SCALES) s_tot[t / NNCG_SCALES][t % NNCG_SCALES] = 0ull;
+            e0 = nncg_e0(0, 0.f);
+            __syncthreads();
+        }
         int done = 0;
         for (int it = 0; it < iters; it++) {
             pass(OP_SWEEP, sym && (it & 1));
             done = it + 1;
+            if (accel) {
+                // |g|^2 from the exact totals, then the momentum step on every
+                // slot and every body (no colour order needed)
+                const float gg = nncg_gg(s_tot[par], e0);
+                const float beta = nncg_beta(it, gg, ggPrev);
+                ggPrev = gg;
+                if (t < NNCG_SCALES) s_tot[par ^ 1][t] = 0ull;   // the next sweep's totals
+                e0 = nncg_e0(1, gg);
+                par ^= 1;
+                for (int i = t; i < nslots; i += T) {
+                    float* lp = resident ? slam + 4 * lam_pos(i) : lamS + 4 * ((size_t)slotS0 + i);
+                    float* gp = resident ? sgp + 8 * lam_pos(i) : gpG + 8 * ((size_t)slotS0 + i);
+                    nncg_slot(lp, gp, it, beta);
+                }
+                for (int b = t; b < nbA; b += T) nncg_body(dv + 6 * b, dqB + 12 * b, it, beta);
+                __syncthreads();
+            }
             // the same check points as the cluster kernel, so a scene stops at
             // the same sweep whichever kernel solves it
             if (check > 0 && (done % check == 0 || done == iters)) {
@@ -906,19 +1065,29 @@ __device__ __forceinline__ int dsm_ld_s32(unsigned a) {
 __device__ __forceinline__ void dsm_st_s32(unsigned a, int v) {
     asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
+__device__ __forceinline__ unsigned long long dsm_ld_u64(unsigned a) {
+    unsigned long long v;
+    asm volatile("ld.shared::cluster.u64 %0, [%1];" : "=l"(v) : "r"(a) : "memory");
+    return v;
+}
 __device__ __forceinline__ void dsm_max_s32(unsigned a, int v) {
     asm volatile("red.shared::cluster.max.s32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
 
+// With the conjugate-gradient acceleration on, a CTA also keeps per owned
+// body delta-v at the sweep's start and q (12 floats) and per staged slot g
+// and p (8 floats).
 struct ClusterSmem {
-    int dv, mv, rec, lam, gi, gl, total;
-    __host__ __device__ ClusterSmem(int nbMax, int K, int cap) {
+    int dv, dq, mv, rec, lam, gp, gi, gl, total;
+    __host__ __device__ ClusterSmem(int nbMax, int K, int cap, int accel = 0) {
         int own = (nbMax + K - 1) / K;
         dv = 0;               // 12 floats per owned body: delta-v, then symmetric jinv
-        mv = 12 * own;
-        rec = (12 * own + nbMax + 3) & ~3;
+        dq = 12 * own;
+        mv = dq + (accel ? 12 * own : 0);
+        rec = (mv + nbMax + 3) & ~3;
         lam = rec + cap * RECS;
-        gi = lam + 4 * cap;
+        gp = lam + 4 * cap;
+        gi = gp + (accel ? 8 * cap : 0);
         gl = gi + 2 * cap;
         total = gl + 2 * cap;
     }
@@ -929,9 +1098,9 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
     const int2* glid, const int* contactOf, const float* __restrict__ rec, const float* lamS, int cap, int nbMax,
     int K, int iters, float omega, float comp, float tolRel, int check, float slide, int* sceneSweeps,
     float* sceneRes, int inner, int writeBack, float relax, int sym, long long* trace, const int* lidOf,
-    const int* bodyOf, const int* sceneActive) {
+    const int* bodyOf, const int* sceneActive, int accel) {
     extern __shared__ float sm[];
-    const ClusterSmem L(nbMax, K, cap);
+    const ClusterSmem L(nbMax, K, cap, accel);
     const long long tStart = gtimer();
     float* dvOwn = sm + L.dv;
     float* mv = sm + L.mv;
@@ -1033,6 +1202,13 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
     cp_async_wait_all();
     __syncthreads();
 
+    float* dq = sm + L.dq;
+    float* sgp = sm + L.gp;
+    // |g|^2 totals of this CTA's groups by sweep parity, and the cluster's
+    // totals gathered from every CTA
+    __shared__ unsigned long long s_tot[2][NNCG_SCALES], s_all[8 * NNCG_SCALES];
+    unsigned long long acc[NNCG_SCALES] = {0ull, 0ull, 0ull, 0ull};
+    int e0 = 0, par = 0;
     float rmax = 0.f, lmax = 0.f;
     auto group = [&](int op, int col, int kk) {
         int2 gi = sgi[kk];
@@ -1054,6 +1230,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
         P.mb = mv[id.y];
         const int cnt = gi.y;
         const int reps = op == OP_SWEEP ? inner : 1;
+        float gsq = 0.f;
         for (int jj = 0; jj < reps * cnt; jj++) {
             const int j = reps == 1 ? jj : jj % cnt;
             const int slot = sl0 + j;
@@ -1062,7 +1239,17 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
             if (op == OP_WARM) {
                 warm_contact(P, R, slot, lp);
             } else if (op == OP_SWEEP) {
-                sweep_contact(P, R, slot, lp, omega, comp, relax);
+                float d[3];
+                sweep_contact(P, R, slot, lp, omega, comp, relax, d);
+                if (accel) {
+                    float* g = sgp + 8 * lam_pos(slot);
+                    if (jj >= cnt)
+                        for (int q = 0; q < 3; q++) d[q] = __fadd_rn(g[q], d[q]);
+                    g[0] = d[0];
+                    g[1] = d[1];
+                    g[2] = d[2];
+                    if (jj >= (reps - 1) * cnt) gsq = sq3_acc(d, gsq);
+                }
             } else if (op == OP_RES) {
                 res_contact(P, R, slot, lp, comp, rmax, lmax);
             } else {
@@ -1075,23 +1262,58 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
             if (P.ma != 0.f) { dsm_st4(pa, P.a[0], P.a[1], P.a[2], P.a[3]); dsm_st2(pa + 16, P.a[4], P.a[5]); }
             if (P.mb != 0.f) { dsm_st4(pb, P.b[0], P.b[1], P.b[2], P.b[3]); dsm_st2(pb + 16, P.b[4], P.b[5]); }
         }
+        if (op == OP_SWEEP && accel) nncg_acc(gsq, e0, acc);
     };
     // colours in order, a cluster barrier after each one that writes delta-v
     auto pass = [&](int op, bool rev) {
         for (int cc = 0; cc < ncol; cc++) {
             int col = rev ? ncol - 1 - cc : cc;
             for (int kk = s_kb[col] + t; kk < s_kb[col + 1]; kk += T) group(op, col, kk);
+            if (op == OP_SWEEP && accel && cc == ncol - 1) nncg_flush(acc, s_tot[par]);
             if (op == OP_WARM || op == OP_SWEEP) cluster_sync_all();
         }
     };
 
     cluster_sync_all();   // zeroed delta-v of every CTA visible before any remote access
     pass(OP_WARM, false);
+    if (accel) {   // delta-v of the owned bodies at the first sweep's start
+        for (int i = t; i < own; i += T)
+            for (int k = 0; k < 6; k++) dq[12 * i + k] = dvOwn[12 * i + k];
+        if (t < 2 * NNCG_SCALES) s_tot[t / NNCG_SCALES][t % NNCG_SCALES] = 0ull;
+        e0 = nncg_e0(0, 0.f);
+        // every CTA has copied its bodies (and cleared its totals) before any
+        // CTA's first sweep writes them
+        cluster_sync_all();
+    }
     int done = 0;
     float res = 0.f;
+    float ggPrev = 0.f;
     for (int it = 0; it < iters; it++) {
         pass(OP_SWEEP, sym && (it & 1));
         done = it + 1;
+        if (accel) {
+            // every CTA gathers the totals of all CTAs (complete at the last
+            // colour's barrier) and adds them in integers, so all get the same
+            // beta; then each updates its own slots and bodies
+            if (t < K * NNCG_SCALES) s_all[t] = dsm_ld_u64(dsm_map(&s_tot[par][t % NNCG_SCALES], t / NNCG_SCALES));
+            __syncthreads();
+            unsigned long long tot[NNCG_SCALES];
+            for (int j = 0; j < NNCG_SCALES; j++) {
+                tot[j] = 0ull;
+                for (int r = 0; r < K; r++) tot[j] += s_all[r * NNCG_SCALES + j];
+            }
+            const float gg = nncg_gg(tot, e0);
+            const float beta = nncg_beta(it, gg, ggPrev);
+            ggPrev = gg;
+            if (t < NNCG_SCALES) s_tot[par ^ 1][t] = 0ull;   // the next sweep's totals
+            e0 = nncg_e0(1, gg);
+            par ^= 1;
+            for (int i = t; i < s_sb[ncol]; i += T) nncg_slot(slam + 4 * lam_pos(i), sgp + 8 * lam_pos(i), it, beta);
+            for (int i = t; i < own; i += T) nncg_body(dvOwn + 12 * i, dq + 12 * i, it, beta);
+            // delta-v of every CTA updated before the next sweep reads it, and
+            // every CTA done reading the squared changes before they are rewritten
+            cluster_sync_all();
+        }
         if (check > 0 && (done % check == 0 || done == iters)) {
             if (t == 0) { s_res = 0; s_lam = 0; }
             rmax = 0.f;
@@ -1138,22 +1360,24 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
     cluster_sync_all();   // no CTA leaves while another may still read its shared memory
 }
 
-size_t batch_cluster_smem(int nbMax, int K, int cap) { return sizeof(float) * (size_t)ClusterSmem(nbMax, K, cap).total; }
+size_t batch_cluster_smem(int nbMax, int K, int cap, int accel) {
+    return sizeof(float) * (size_t)ClusterSmem(nbMax, K, cap, accel).total;
+}
 
 const void* batch_sweep_kernel() { return (const void*)k_batch_sweep; }
 
-size_t batch_sweep_smem(int nbMax, int cap) { return sizeof(float) * (size_t)SweepSmem(nbMax, cap).total; }
+size_t batch_sweep_smem(int nbMax, int cap, int accel) { return sizeof(float) * (size_t)SweepSmem(nbMax, cap, accel).total; }
 
 int Ctx::batchLaunchSweep(int threads, int cap, int iters, float tol, int check, float* lamStart, const float* lamAlt,
                           int* fall, int writeBack, int nGrid, const int* order, int nbMax, cudaStream_t strm) {
     double comp = P.enable_compliance ? P.compliance : 0.;
-    size_t ssm = batch_sweep_smem(nbMax, cap);
+    size_t ssm = batch_sweep_smem(nbMax, cap, batchAccel);
     if (nGrid <= 0) return AM_OK;
     k_batch_sweep<<<nGrid, threads, ssm, strm>>>(
         B, C[cur], sceneBodyOffDev, order, bGInfo, bLid, bChunkK, bNChunks, bContactOf, bRec, lamStart, cap,
         nbMax, iters, (float)P.omega, (float)comp, tol, check, (float)P.sliding_threshold, bSweeps, bRes,
         lamAlt, fall, writeBack, batchInner, (float)batchRelax, batchSym, writeBack ? bTrace : nullptr, bLidOf, bBodyOf,
-        bSceneActive);
+        bSceneActive, batchAccel, bGP, bDQ);
     AM_LAUNCHED(1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { err = std::string("sweep launch: ") + cudaGetErrorString(e); return AM_E_CUDA; }
@@ -1204,7 +1428,7 @@ int Ctx::batchSplit(int cap, bool useCluster) {
         if (batchClasses)
             for (int q = 0; q < NCLASS && c < 0; q++)
                 if (slots == 0 || (slots <= 2 * CLASS_CAP[q] && nb <= 4 * CLASS_CAP[q] &&
-                                   batch_sweep_smem(nb, CLASS_CAP[q]) <= batchSmemLimit))
+                                   batch_sweep_smem(nb, CLASS_CAP[q], batchAccel) <= batchSmemLimit))
                     c = q;
         if (c >= 0) {
             hClass[c].push_back(sc);
@@ -1224,7 +1448,7 @@ int Ctx::batchSplit(int cap, bool useCluster) {
             for (int q = 0; q < 3; q++) {
                 int K = CLUSTER_K[q];
                 int per = ((slots + K - 1) / K + sz[sc].y + 31) & ~31;
-                if (per <= capK && batch_cluster_smem(std::max(bigNb[q], nb), K, std::max(bigCap[q], per)) <=
+                if (per <= capK && batch_cluster_smem(std::max(bigNb[q], nb), K, std::max(bigCap[q], per), batchAccel) <=
                                              clusterSmemLimit) {
                     need = q;
                     hBigK[q].push_back(sc);
@@ -1270,6 +1494,14 @@ int Ctx::batchClusterMaxK() const {
     return k;
 }
 
+// CTAs that solved each scene in the last split: 1 for the one-CTA launch
+// and the size classes, K for a cluster of K
+void Ctx::batchSceneCtas(int* out) const {
+    for (int s = 0; s < nScenes; s++) out[s] = 1;
+    for (int q = 0; q < 3; q++)
+        for (int s : hBigK[q]) out[s] = CLUSTER_K[q];
+}
+
 // the cluster launch of cluster size CLUSTER_K[q] over `list`
 int Ctx::batchLaunchCluster(int q, const int* list, int nBig, cudaStream_t strm, int iters, float tol, int check,
                             int writeBack) {
@@ -1278,7 +1510,7 @@ int Ctx::batchLaunchCluster(int q, const int* list, int nBig, cudaStream_t strm,
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nBig * K);
     cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = batch_cluster_smem(bigNb[q], K, bigCap[q]);
+    cfg.dynamicSmemBytes = batch_cluster_smem(bigNb[q], K, bigCap[q], batchAccel);
     cfg.stream = strm;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1293,7 +1525,7 @@ int Ctx::batchLaunchCluster(int q, const int* list, int nBig, cudaStream_t strm,
                                        bigNb[q], K, iters, (float)P.omega, (float)comp, tol, check,
                                        (float)P.sliding_threshold, bSweeps, bRes, batchInner, writeBack,
                                        (float)batchRelax, batchSym, writeBack ? bTrace : nullptr, (const int*)bLidOf,
-                                       (const int*)bBodyOf, (const int*)bSceneActive);
+                                       (const int*)bBodyOf, (const int*)bSceneActive, batchAccel);
     AM_LAUNCHED(1);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) { err = std::string("cluster sweep launch: ") + cudaGetErrorString(e); return AM_E_CUDA; }
@@ -1378,7 +1610,7 @@ int Ctx::batchSolve(double dt) {
     if (nc > bRecCap) {
         int cap = std::max(nc + nc / 2, 4096);
         if (alloc(&bRec, (size_t)REC * cap) || alloc(&bLam, 4 * (size_t)cap) || alloc(&bLamL, 4 * (size_t)cap) ||
-            alloc(&bSlotOf, cap) || alloc(&bContactOf, cap))
+            alloc(&bSlotOf, cap) || alloc(&bContactOf, cap) || alloc(&bGP, 8 * (size_t)cap))
             return AM_E_CUDA;
         bRecCap = cap;
     }
@@ -1437,6 +1669,36 @@ __global__ void k_scene_cs(DPairs P, int npairs, int nc, const int* pairOff, con
     int a = pairOff[s] < npairs ? P.off[pairOff[s]] : nc;
     int b = pairOff[s + 1] < npairs ? P.off[pairOff[s + 1]] : nc;
     out[s] = (long long)(b - a) * sweeps[s];
+}
+
+// critical path of one sweep of each scene, in contacts: the sum over its
+// colours of the longest group (a group's contacts update one after another,
+// and a colour ends when its longest group does); one warp per scene
+__global__ void k_scene_chain(const int2* gInfo, const int* colOff, int nScenes, int* chain) {
+    const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (s >= nScenes) return;
+    const int* co = colOff + s * (MAXCB + 1);
+    const int ncol = scene_colours(co);
+    int sum = 0;
+    for (int c = 0; c < ncol; c++) {
+        int m = 0;
+        for (int k = co[c] + lane; k < co[c + 1]; k += 32) m = max(m, gInfo[k].y);
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        sum += m;
+    }
+    if (lane == 0) chain[s] = sum;
+}
+
+int Ctx::batchChain(int* out) {
+    if (!bChain && alloc(&bChain, nScenes)) return AM_E_CUDA;
+    if (nContacts <= 0 || !bGInfo) {
+        for (int s = 0; s < nScenes; s++) out[s] = 0;
+        return AM_OK;
+    }
+    k_scene_chain<<<(nScenes + 7) / 8, 256, 0, stream>>>(bGInfo, bColOff, nScenes, bChain);
+    AM_LAUNCHED(1);
+    cudaMemcpyAsync(out, bChain, sizeof(int) * nScenes, cudaMemcpyDeviceToHost, stream);
+    return syncErr();
 }
 
 // colours per scene of the last colouring (colours are contiguous from 0)
@@ -1552,7 +1814,8 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     if (alloc(&sceneOfDev, cap) || alloc(&sceneBodyOffDev, n + 1) || alloc(&topEnd, all.n_bodies) ||
         alloc(&bPairOff, n + 1) || alloc(&bColOff, (size_t)n * (MAXCB + 1)) || alloc(&bSweeps, n) || alloc(&bRes, n) ||
         alloc(&bFall, n) || alloc(&bTrace, 3 * (size_t)n) || alloc(&bSceneActive, n) ||
-        alloc(&bLidOf, (size_t)bodyOff[n] + 1) || alloc(&bBodyOf, (size_t)bodyOff[n] + 1))
+        alloc(&bLidOf, (size_t)bodyOff[n] + 1) || alloc(&bBodyOf, (size_t)bodyOff[n] + 1) ||
+        alloc(&bDQ, 12 * ((size_t)bodyOff[n] + 1)))
         return AM_E_CUDA;
     cudaMemsetAsync(bFall, 0, sizeof(int) * n, stream);
     cudaMemsetAsync(bTrace, 0, sizeof(long long) * 3 * n, stream);
@@ -1605,8 +1868,8 @@ int Ctx::setBatch(const am_scene* sc, int n) {
         // the most records a CTA of a cluster may hold (a scene's part; its
         // bodies are checked when the scenes are split)
         clusterCap = clusterCapUser > 0 ? clusterCapUser : 2048;
-        while (clusterCap > 64 && batch_cluster_smem(64, 2, clusterCap) > lim) clusterCap -= 32;
-        if (batch_cluster_smem(64, 2, clusterCap) <= lim &&
+        while (clusterCap > 64 && batch_cluster_smem(64, 2, clusterCap, 0) > lim) clusterCap -= 32;
+        if (batch_cluster_smem(64, 2, clusterCap, 0) <= lim &&
             cudaFuncSetAttribute((const void*)k_batch_sweep_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)lim) == cudaSuccess)
             clusterUsable = true;
@@ -1639,9 +1902,9 @@ int Ctx::batchAutotune(double dt) {
     std::vector<int> thr = fixedThreads > 0 ? std::vector<int>{fixedThreads} : std::vector<int>{128, 256, 512};
     std::vector<int> caps;
     for (int c : {64, 128, 192, 256})
-        if (batch_sweep_smem(maxSceneBodies, c) <= batchSmemLimit && (!batchCapUser || c == batchCapUser))
+        if (batch_sweep_smem(maxSceneBodies, c, batchAccel) <= batchSmemLimit && (!batchCapUser || c == batchCapUser))
             caps.push_back(c);
-    if (batchCapUser && caps.empty() && batch_sweep_smem(maxSceneBodies, batchCapUser) <= batchSmemLimit)
+    if (batchCapUser && caps.empty() && batch_sweep_smem(maxSceneBodies, batchCapUser, batchAccel) <= batchSmemLimit)
         caps.push_back(batchCapUser);
     if (caps.empty()) {
         err = "a scene has too many bodies for the batched solve's shared memory";
@@ -1697,19 +1960,35 @@ int Ctx::batchAutotune(double dt) {
 // RigidBodySystem.advanceTime for every scene of the batch (merging off)
 int Ctx::stepBatch(double dt) {
     int r;
+    if (!evPh[0])
+        for (auto& e : evPh) cudaEventCreate(&e);
+    if (evA != evPh[3]) {   // the sweep's timing events are phase boundaries 3 and 4
+        if (evA) { cudaEventDestroy(evA); cudaEventDestroy(evB); }
+        evA = evPh[3];
+        evB = evPh[4];
+    }
+    cudaEventRecord(evPh[0], stream);
     if ((r = beginStep(0))) return r;
     double t = phaseNow();
     if ((r = collisionDetection())) return r;
     phaseAdd(AM_PHASE_DETECTION, t);
+    cudaEventRecord(evPh[1], stream);
     t = phaseNow();
     if ((r = warmStart())) return r;
     phaseAdd(AM_PHASE_WARMSTART, t);
     if ((r = wake())) return r;
-    if (!evA) { cudaEventCreate(&evA); cudaEventCreate(&evB); }
+    cudaEventRecord(evPh[2], stream);
     t = phaseNow();
+    // the solve records evA (= evPh[3]) before its sweep launches and evB
+    // (= evPh[4]) after them; a step without contacts records both here
     if ((r = batchSolve(dt))) return r;
     phaseAdd(AM_PHASE_LCP_SOLVE, t);
+    if (!pgsPending) {
+        cudaEventRecord(evPh[3], stream);
+        cudaEventRecord(evPh[4], stream);
+    }
     if ((r = finishStep(dt))) return r;
+    cudaEventRecord(evPh[5], stream);
     if ((r = readCounts())) return r;
     if (pgsPending) {
         float ms = 0;
@@ -1720,6 +1999,12 @@ int Ctx::stepBatch(double dt) {
         pgsPending = false;
     }
     if ((r = batchStats())) return r;
+    cudaEventRecord(evPh[6], stream);
+    cudaEventSynchronize(evPh[6]);
+    for (int k = 0; k < AM_STEP_PHASES; k++) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, evPh[k], evPh[k + 1]) == cudaSuccess) phaseDevMs[k] += ms;
+    }
     perf.contact_sweeps += batchContactSweepsLast;
     perf.steps++;
     stats.n_contacts = nContacts;

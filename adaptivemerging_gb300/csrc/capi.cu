@@ -252,6 +252,15 @@ int32_t am_set_batch_relaxation(void* ctx, double relax, int32_t symmetric) {
     return AM_OK;
 }
 
+int32_t am_set_batch_accel(void* ctx, int32_t mode) {
+    if (!ctx || mode < 0 || mode > 1) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    c->batchAccel = mode;
+    c->batchThreads = c->batchThreadsUser;   // shared-memory layouts change: tune again
+    c->batchCap = c->batchCapUser;
+    return AM_OK;
+}
+
 int32_t am_set_residual_target(void* ctx, double residual_target, int32_t check_every) {
     if (!ctx || check_every < 0 || !(residual_target >= 0)) return AM_E_ARG;
     Ctx* c = (Ctx*)ctx;
@@ -270,6 +279,21 @@ int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, in
     if (fell_back) cudaMemcpyAsync(fell_back, c->bFall, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream);
     if (colours) return c->batchColours(colours);
     return c->syncErr();
+}
+
+int32_t am_get_batch_scene_chain(void* ctx, int32_t* chain) {
+    if (!ctx || !chain) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->nScenes) return AM_E_STATE;
+    return c->batchChain(chain);
+}
+
+int32_t am_get_batch_scene_ctas(void* ctx, int32_t* ctas) {
+    if (!ctx || !ctas) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->nScenes) return AM_E_STATE;
+    c->batchSceneCtas(ctas);
+    return AM_OK;
 }
 
 int32_t am_get_batch_scene_times(void* ctx, int64_t* start_ns, int64_t* end_ns, int32_t* sm) {
@@ -316,7 +340,10 @@ int32_t am_learned_use(void* ctx, int32_t mode) {
     if (!c->stream) return AM_E_STATE;
     int r = c->learnedInit();
     if (r) return r;
-    if (mode && (r = c->learnedPackInference())) return r;
+    if (mode) {
+        if ((r = c->learnedPackInference())) return r;
+        c->lReady = true;
+    }
     c->lUse = mode;
     return AM_OK;
 }
@@ -475,6 +502,45 @@ int32_t am_get_topology(void* ctx, int32_t* items, int32_t* item_off, int32_t ca
 int32_t am_reset_perf(void* ctx) {
     if (!ctx) return AM_E_ARG;
     std::memset(&((Ctx*)ctx)->perf, 0, sizeof(am_perf));
+    for (double& v : ((Ctx*)ctx)->phaseDevMs) v = 0.0;
+    return AM_OK;
+}
+
+int32_t am_check_barrier_timeout(void* ctx, int32_t spin_log2, int32_t* status) {
+    if (!ctx || !status || spin_log2 < 1 || spin_log2 > 24) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->dc || !c->stream) return AM_E_STATE;
+    launch_barrier_timeout_check(c->dc, spin_log2, c->stream);
+    int e = 0;
+    cudaMemcpyAsync(&e, &c->dc->error, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    const int zero = 0;
+    cudaMemcpyAsync(&c->dc->error, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return AM_E_CUDA;
+    *status = e;
+    return AM_OK;
+}
+
+int32_t am_get_state(void* ctx, void* buf, int64_t capacity, int64_t* size) {
+    if (!ctx || !size || capacity < 0 || (capacity > 0 && !buf)) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    std::vector<uint8_t> blob;
+    int r = c->getState(blob);
+    if (r) return r;
+    *size = (int64_t)blob.size();
+    if (capacity < (int64_t)blob.size()) return AM_E_CAPACITY;
+    std::memcpy(buf, blob.data(), blob.size());
+    return AM_OK;
+}
+
+int32_t am_put_state(void* ctx, const void* buf, int64_t size) {
+    if (!ctx || !buf || size <= 0) return AM_E_ARG;
+    return ((Ctx*)ctx)->putState((const uint8_t*)buf, (size_t)size);
+}
+
+int32_t am_get_step_phases(void* ctx, double* ms) {
+    if (!ctx || !ms) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    for (int k = 0; k < AM_STEP_PHASES; k++) ms[k] = c->phaseDevMs[k];
     return AM_OK;
 }
 

@@ -163,6 +163,7 @@ struct HostMerge {
 // The step context behind the C ABI.
 struct Ctx {
     am_params P;
+    int device = -1;             // the CUDA device current when the context was created
     std::string err;
     HostWorld host;
     cudaStream_t stream = nullptr;
@@ -211,6 +212,11 @@ struct Ctx {
     am_solve_stats stats{};
     am_perf perf{};
     cudaEvent_t evA = nullptr, evB = nullptr;
+    // batched step: device events at the phase boundaries (detection, warm
+    // start, solve set-up, sweeps, integration, statistics); per-phase sums
+    // since the last am_reset_perf
+    cudaEvent_t evPh[7] = {};
+    double phaseDevMs[AM_STEP_PHASES] = {};
     bool pgsPending = false;
     std::vector<void*> allocs;
     // merging state
@@ -271,6 +277,9 @@ struct Ctx {
     void phaseAdd(int k, double t0) { if (phaseOn) phase[k] += phaseNow() - t0; }
     double batchRelax = 1.0;     // over-relaxation of the batched sweep (1: plain projected Gauss-Seidel)
     int batchSym = 0;            // 1: odd sweeps walk the colours backwards
+    int batchAccel = 0;          // 1: nonsmooth nonlinear conjugate gradient around each sweep
+    float* bGP = nullptr;        // per slot: g and p of the conjugate-gradient step (streamed scenes)
+    float* bDQ = nullptr;        // per body: delta-v at sweep start and q (streamed scenes)
     // scenes larger than one CTA's shared memory: thread-block clusters
     int2* bSceneSize = nullptr;  // per scene: slots, one group per colour (split overhead)
     long long* bTrace = nullptr; // per scene, last solve: start and end (device timer, ns), SM of the (first) CTA
@@ -315,6 +324,7 @@ struct Ctx {
     float *lW = nullptr, *lG = nullptr, *lM = nullptr, *lV = nullptr, *lNorm = nullptr, *lBias = nullptr,
           *lLoss = nullptr;
     __nv_bfloat16* lWb = nullptr;
+    bool lReady = false;         // weights set by am_learned_use / _weights / _train, BF16 copy current
     float *lX = nullptr, *lY = nullptr, *lDX = nullptr, *lDY = nullptr, *lZ1 = nullptr, *lZ2 = nullptr,
           *lYh = nullptr, *lXN = nullptr, *lA1 = nullptr, *lA2 = nullptr, *lD1 = nullptr, *lD2 = nullptr,
           *lDYb = nullptr;
@@ -418,6 +428,10 @@ struct Ctx {
     int batchStats();
     int batchAutotune(double dt);
     int batchColours(int* out);
+    int getState(std::vector<uint8_t>& out);
+    int putState(const uint8_t* in, size_t size);
+    int batchChain(int* out);
+    int* bChain = nullptr;
     int batchLayout(int cap);
     int batchLaunchSweep(int threads, int cap, int iters, float tol, int check, float* lamStart, const float* lamAlt,
                          int* fall, int writeBack, int nGrid, const int* order, int nbMax, cudaStream_t strm);
@@ -428,6 +442,7 @@ struct Ctx {
                        int writeBack);
     int batchClusterScenes() const;
     int batchClusterMaxK() const;
+    void batchSceneCtas(int* out) const;
     int learnedInit();
     int ensureFeat(int nc);
     int learnedFeatures(double dt);

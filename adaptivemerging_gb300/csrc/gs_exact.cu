@@ -214,4 +214,22 @@ void launch_gs_levels(const DBodies& B, DContacts& C, const int* order, const in
     AM_LAUNCHED(1);
 }
 
+// Two blocks wait at a barrier whose target counts three: no arrival can
+// complete it, so each block's wait must expire (or see the other's expiry).
+__global__ void k_barrier_timeout_check(DCount* dc) {
+    unsigned target = 0;
+    grid_barrier_counted(dc, gridDim.x + 1, target);   // every block expects one arrival too many
+}
+
+void launch_barrier_timeout_check(DCount* dc, int spin_log2, cudaStream_t s) {
+    cudaMemsetAsync(&dc->bar_count, 0, sizeof(int), s);
+    cudaMemsetAsync(&dc->error, 0, sizeof(int), s);
+    cudaMemcpyAsync(&dc->spin_log2, &spin_log2, sizeof(int), cudaMemcpyHostToDevice, s);
+    k_barrier_timeout_check<<<2, 64, 0, s>>>(dc);
+    AM_LAUNCHED(1);
+    const int zero = 0;
+    cudaMemcpyAsync(&dc->spin_log2, &zero, sizeof(int), cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);
+}
+
 }  // namespace am

@@ -537,6 +537,7 @@ int Ctx::learnedNormalise() {
 
 // mini-batch Adam on the recorded set; returns the mean loss of the last epoch
 int Ctx::learnedTrain(int epochs, int batch, float lr, float* lastLoss, int normalise) {
+    lReady = false;   // set again once the trained weights are packed
     int r = learnedInit();
     if (r) return r;
     int n = lDn;
@@ -585,7 +586,9 @@ int Ctx::learnedTrain(int epochs, int batch, float lr, float* lastLoss, int norm
         el = ls / (float)nb;
     }
     if (lastLoss) *lastLoss = el;
-    return learnedPackInference();
+    if ((r = learnedPackInference())) return r;
+    lReady = true;
+    return AM_OK;
 }
 
 // loss and gradients of the current weights on host samples (test hook)
@@ -635,7 +638,11 @@ int Ctx::learnedWeights(float* w, const float* in, float* norm, const float* nor
     if (w) cudaMemcpyAsync(w, lW, sizeof(float) * NPAR, cudaMemcpyDeviceToHost, stream);
     if (norm) cudaMemcpyAsync(norm, lNorm, sizeof(float) * 2 * NIN, cudaMemcpyDeviceToHost, stream);
     if ((r = syncErr())) return r;
-    return in ? learnedPackInference() : AM_OK;
+    if (!in) return AM_OK;
+    lReady = false;
+    if ((r = learnedPackInference())) return r;
+    lReady = true;
+    return AM_OK;
 }
 
 int Ctx::learnedCollect(int enable, int capacity) {
@@ -683,9 +690,10 @@ static __device__ __align__(256) float g_noalloc_scratch[(size_t)NOALLOC_ROWS * 
 static float* g_noalloc_ptr[NOALLOC_MAX_DEVICES];
 static std::mutex g_noalloc_mu;
 
-static float* noalloc_scratch() {
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) return nullptr;
+// the scratch of device `dev`, which must be the current device (the symbol
+// lookup resolves against the current device)
+static float* noalloc_scratch(int dev) {
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return nullptr;
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     if (!g_noalloc_ptr[dev]) {
         void* p = nullptr;
@@ -699,17 +707,20 @@ static float* noalloc_scratch() {
 // touched, so a rejected call allocates nothing either).
 int Ctx::learnedInferNoAlloc(const float* X, int n, float* out, int tensorCores) {
     if (n > NOALLOC_ROWS) return AM_E_CAPACITY;
-    if (!lW || !lWb) return AM_E_STATE;   // weights are set up by am_learned_use / _weights / _train
-    float* base = noalloc_scratch();
+    if (!lReady) return AM_E_STATE;   // weights are set up (and packed) by am_learned_use / _weights / _train
+    // the scratch and the kernels belong to the context's device, which must
+    // be the current one
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != device) return AM_E_STATE;
+    float* base = noalloc_scratch(device);
     if (!base) return AM_E_CUDA;
     float* dX = base;
     float* dO = base + (size_t)NOALLOC_ROWS * NIN;
     if (cudaMemcpyAsync(dX, X, sizeof(float) * NIN * (size_t)n, cudaMemcpyHostToDevice, stream) != cudaSuccess)
         return AM_E_CUDA;
-    k_pack_bf16<<<(NH * NH + 255) / 256, 256, 0, stream>>>(lW, lWb, lBias);
     if (tensorCores) k_infer_bf16<<<(n + 63) / 64, 128, 0, stream>>>(dX, lNorm, lWb, lBias, n, dO);
     else k_infer_f32<<<(n + 127) / 128, 128, 0, stream>>>(dX, lNorm, lW, n, dO);
-    AM_LAUNCHED(2);
+    AM_LAUNCHED(1);
     if (cudaGetLastError() != cudaSuccess) return AM_E_CUDA;
     if (cudaMemcpyAsync(out, dO, sizeof(float) * NOUT * (size_t)n, cudaMemcpyDeviceToHost, stream) != cudaSuccess)
         return AM_E_CUDA;

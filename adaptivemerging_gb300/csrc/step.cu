@@ -293,6 +293,7 @@ static int g_numSMs = 0;
 
 
 Ctx::Ctx(const am_params& p) : P(p) {
+    cudaGetDevice(&device);
     std::memset(&B, 0, sizeof(B));
     std::memset(&N, 0, sizeof(N));
     std::memset(&C[0], 0, sizeof(DContacts) * 2);
@@ -323,6 +324,12 @@ void Ctx::release() {
     }
     if (evFork) cudaEventDestroy(evFork);
     evFork = nullptr;
+    if (evA && evA != evPh[3]) { cudaEventDestroy(evA); cudaEventDestroy(evB); }
+    evA = evB = nullptr;
+    for (auto& e : evPh) {
+        if (e) cudaEventDestroy(e);
+        e = nullptr;
+    }
     // every device buffer went with `allocs`: forget them and their capacities,
     // so a context given a new scene allocates afresh
     std::memset(&PR, 0, sizeof(PR));

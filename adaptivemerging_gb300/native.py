@@ -19,8 +19,8 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libam.so")
 EXPORTS = [
     "am_params_default", "am_create", "am_destroy", "am_last_error", "am_set_params", "am_set_scene",
     "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
-    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats", "am_get_batch_scene_times", "am_set_residual_target",
-    "am_set_batch_local_sweeps", "am_set_batch_clusters", "am_set_batch_stage", "am_set_batch_relaxation",
+    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_get_step_phases", "am_get_state", "am_put_state", "am_check_barrier_timeout", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats", "am_get_batch_scene_times", "am_get_batch_scene_ctas", "am_get_batch_scene_chain", "am_set_residual_target",
+    "am_set_batch_local_sweeps", "am_set_batch_accel", "am_set_batch_clusters", "am_set_batch_stage", "am_set_batch_relaxation",
     "am_set_batch_cluster_stage", "am_set_batch_size_classes", "am_set_phase_timing", "am_get_phase_times",
     "am_learned_collect", "am_learned_train", "am_learned_use", "am_learned_scope", "am_learned_weights", "am_learned_info",
     "am_learned_grad", "am_learned_infer", "am_learned_infer_noalloc",
@@ -68,8 +68,11 @@ def lib():
         ip = C.POINTER(C.c_int32)
         L.am_get_batch_scene_stats.argtypes = [vp, ip, fp, ip, ip]
         L.am_get_batch_scene_times.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), ip]
+        L.am_get_batch_scene_ctas.argtypes = [vp, ip]
+        L.am_get_batch_scene_chain.argtypes = [vp, ip]
         L.am_set_residual_target.argtypes = [vp, C.c_double, C.c_int32]
         L.am_set_batch_local_sweeps.argtypes = [vp, C.c_int32]
+        L.am_set_batch_accel.argtypes = [vp, C.c_int32]
         L.am_set_batch_clusters.argtypes = [vp, C.c_int32]
         L.am_set_batch_size_classes.argtypes = [vp, C.c_int32]
         L.am_set_batch_stage.argtypes = [vp, C.c_int32]
@@ -90,6 +93,10 @@ def lib():
         L.am_set_phase_timing.argtypes = [vp, C.c_int32]
         L.am_get_phase_times.argtypes = [vp, C.POINTER(C.c_double)]
         L.am_get_stream.argtypes = [vp, C.POINTER(vp)]
+        L.am_get_step_phases.argtypes = [vp, C.POINTER(C.c_double)]
+        L.am_get_state.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
+        L.am_put_state.argtypes = [vp, vp, C.c_int64]
+        L.am_check_barrier_timeout.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
         for f in EXPORTS:
             if f not in ("am_params_default", "am_last_error"):
                 getattr(L, f).restype = C.c_int32
@@ -135,6 +142,10 @@ class BatchSystem:
     def set_size_classes(self, enable=True):
         self._check(lib().am_set_batch_size_classes(self.h, int(enable)))
 
+    def set_accel(self, mode=1):
+        """1: conjugate-gradient (NNCG) acceleration of the batched sweep; 0: plain PGS."""
+        self._check(lib().am_set_batch_accel(self.h, int(mode)))
+
     def set_local_sweeps(self, passes):
         self._check(lib().am_set_batch_local_sweeps(self.h, passes))
 
@@ -160,6 +171,18 @@ class BatchSystem:
         self._check(lib().am_get_batch_scene_times(self.h, t0.ctypes.data_as(i64), t1.ctypes.data_as(i64),
                                                    sm.ctypes.data_as(C.POINTER(C.c_int32))))
         return {"start_ns": t0, "end_ns": t1, "sm": sm}
+
+    def scene_ctas(self):
+        """Per scene, last solve: CTAs that solved it (1, or the cluster size)."""
+        out = np.zeros(len(self.scenes), np.int32)
+        self._check(lib().am_get_batch_scene_ctas(self.h, out.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out
+
+    def scene_chain(self):
+        """Per scene, last solve: contacts on one sweep's critical path."""
+        out = np.zeros(len(self.scenes), np.int32)
+        self._check(lib().am_get_batch_scene_chain(self.h, out.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out
 
     # learned warm start
     def learned_collect(self, enable=True, capacity=2_000_000):
@@ -285,6 +308,27 @@ class System:
         self._check(lib().am_get_phase_times(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
         return out
 
+    def step_phases(self):
+        """Batched steps: device ms per phase (abi.STEP_PHASES order) summed
+        since reset_perf."""
+        out = np.zeros(len(abi.STEP_PHASES), np.float64)
+        self._check(lib().am_get_step_phases(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return dict(zip(abi.STEP_PHASES, out.tolist()))
+
+    def get_state(self):
+        """Snapshot of the simulation state (bytes) for put_state."""
+        n = C.c_int64(0)
+        r = lib().am_get_state(self.h, None, 0, C.byref(n))
+        if r not in (0, -2):
+            self._check(r)
+        buf = C.create_string_buffer(max(1, n.value))
+        self._check(lib().am_get_state(self.h, buf, n.value, C.byref(n)))
+        return buf.raw[:n.value]
+
+    def put_state(self, blob):
+        buf = C.create_string_buffer(bytes(blob), len(blob))
+        self._check(lib().am_put_state(self.h, buf, len(blob)))
+
     def stream_handle(self):
         s = C.c_void_p()
         self._check(lib().am_get_stream(self.h, C.byref(s)))
@@ -340,7 +384,7 @@ class System:
 
 
 for _name in ("_check", "close", "__del__", "step", "advance_time", "stats", "num_contacts", "contacts", "bodies",
-              "perf", "reset_perf", "set_phase_timing", "phase_times", "stream_handle", "set_params", "topology",
+              "perf", "reset_perf", "set_phase_timing", "phase_times", "step_phases", "get_state", "put_state", "stream_handle", "set_params", "topology",
               "put_bodies_struct",
               "get_bodies_struct", "collision_detection", "warm_start", "solve_lcp", "integrate"):
     setattr(BatchSystem, _name, getattr(System, _name))

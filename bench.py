@@ -7,17 +7,25 @@
 A step is one RigidBodySystem.advanceTime of every scene of the workload:
 collision detection, contact setup, warm start, the projected Gauss-Seidel
 solve, integration and sleeping.  The default workload is the batched one
-(512 independent bins, FP32 solve, each scene iterated until its relative LCP
-residual <= 1e-6, cap 5000 sweeps); `value` is simulated scene-steps per
-second with the state resident in HBM (device time of K steps measured with
-CUDA events on the library's stream); `e2e` runs the same steps through the C
-ABI with the body state pushed from and read back into pinned host buffers
-every step.  `plain_gpu_pgs` times the FP64 drop-in stepping a sample of the
-same scenes one at a time to the same residual.  `--impl reference` times the
-CPU restatement of the reference path (the oracle) on the same workload, over
-all host cores.  Scenes are independent, so several
-GPUs each run their own batch ("weak" scaling, no collective): value = all
-ranks' scene-steps / max time.
+(512 independent bins).  Every scene of every arm is iterated until its
+relative LCP residual is <= 1e-6 (checked every 10 sweeps, cap SWEEP_CAP).
+
+- `value`: the batched FP32 solve with previous-frame warm start and the
+  conjugate-gradient (NNCG) acceleration of each sweep, simulated scene-steps
+  per second with the state resident in HBM (device time of K steps, CUDA
+  events on the library's stream).  `e2e`: the same steps through the C ABI
+  with the body state pushed from and read back into pinned host buffers.
+- `plain_gpu_pgs`: the same batched FP32 kernels, same scenes, steps and
+  residual rule, plain projected Gauss-Seidel (no acceleration).
+- `plain_gpu_pgs_one_scene_at_a_time`: plain FP32 PGS on the same kernels,
+  one scene per launch sequence (a sample of the scenes).
+- `fp64_drop_in_one_scene_at_a_time`: the FP64 drop-in's coloured solve, one
+  scene at a time (a sample).
+- `--impl reference`: the CPU restatement of the reference path (the oracle,
+  FP64 Gauss-Seidel in list order with the same stopping rule) on all 512
+  scenes over all host cores, timed by wall clock.
+Scenes are independent, so several GPUs each run their own batch ("weak"
+scaling, no collective): value = all ranks' scene-steps / max time.
 """
 import argparse
 import ctypes as C
@@ -38,13 +46,23 @@ from adaptivemerging_gb300 import abi, scenes  # noqa: E402
 
 METRIC = "sim steps/s at LCP residual<=1e-6: warm-start+batched vs plain GPU PGS, 1 GB300"
 FP64_BYTES_PER_CONTACT_SWEEP = 736   # J 288 + b,D 48 + lambda r/w 48 + dv of 2 bodies r/w 192 + minv,jinv 160
-FP32_BYTES_PER_CONTACT_SWEEP = 368   # the same quantities in FP32
+# compulsory HBM traffic of the batched sweep launches per step: per contact the
+# 96 B record and the 16 B multiplier slot read once, the FP64 multipliers
+# (24 B) and the contact state (4 B) written once; per body in contact its
+# inverse mass and inertia (8 + 72 B), flags and compact id (8 B) read and its
+# FP64 delta-v (48 B) written.  Everything else the sweeps touch stays in shared
+# memory for the whole solve.
+SWEEP_HBM_BYTES_PER_CONTACT = 96 + 16 + 24 + 4
+SWEEP_HBM_BYTES_PER_BODY = 8 + 72 + 8 + 48
+# cycles of one contact update on the sweep's dependent chain (arithmetic
+# only, record in registers; measured with clock64 on one GB300)
+CHAIN_CYCLES_PER_CONTACT = 170
 BATCH_SCENES = 512
 BATCH_SAMPLE_STRIDE = 32             # CPU baseline: every 32nd scene, one core
-REFERENCE_SAMPLE_STRIDE = 4          # reference arm: every 4th scene, all host cores
-PLAIN_SAMPLE_STRIDE = 32             # plain GPU PGS arm: every 32nd scene, one scene at a time
-SWEEP_CAP = 5000                     # sweep cap of the residual-targeted solves
+PLAIN_SAMPLE_STRIDE = 32             # one-scene-at-a-time arms: every 32nd scene
+SWEEP_CAP = 20000                    # sweep cap of the residual-targeted solves
 RESIDUAL_TARGET = 1e-6
+STEADY = (20, 40)                    # the steady window: steps 21..60
 
 
 def workload(name, n_scenes=BATCH_SCENES):
@@ -59,9 +77,10 @@ def workload(name, n_scenes=BATCH_SCENES):
             "workload": f"{n_scenes} independent bins, body counts log-uniform 20..2000, boxes U(0.1,1.0) m and "
                         "spheres U(0.05,0.5) m, density U(500,2000), per-scene mu U(0.3,0.8), 4 pinned walls + plane",
             "scenes": n_scenes, "bodies": int(sum(x.n for x in sc)), "dt": 0.005,
-            "pgs": f"FP32, one CTA per scene (size-class launches) or a 2-8 CTA cluster for the largest, "
-                   f"previous-frame warm start, each scene swept until its relative "
-                   f"LCP residual <= {RESIDUAL_TARGET:g} (checked every 10 sweeps, cap {SWEEP_CAP})",
+            "pgs": f"FP32 projected Gauss-Seidel with box friction, previous-frame warm start, each sweep wrapped "
+                   f"in a nonsmooth nonlinear conjugate-gradient step; one CTA per scene (size-class launches) or "
+                   f"a 2-8 CTA cluster for the largest; each scene swept until its relative LCP residual <= "
+                   f"{RESIDUAL_TARGET:g} (checked every 10 sweeps, cap {SWEEP_CAP})",
             "merging": "off", "precision": "fp32 solve, fp64 collision/contact setup/integration"}
     if name in ("wall", "wall_nomerge"):
         merging = name == "wall"
@@ -186,31 +205,31 @@ def _oracle_scene_time(job):
     return time.perf_counter() - t0
 
 
-def oracle_batch_sample(sc_list, P, dt, warmup, steps, stride=BATCH_SAMPLE_STRIDE, workers=1):
-    """Oracle on every `stride`-th scene from the initial state: `warmup`
-    untimed steps, then `steps` timed steps, the scenes spread over `workers`
-    processes.  Returns scene-steps/s of `workers` cores (sum of the scenes'
-    timed steps / sum of their timed seconds x workers)."""
+def _reference_params(P):
+    """The oracle's parameters for the batched workload: the reference's
+    Gauss-Seidel in list order, stopped by the same residual rule as the GPU
+    arms (the reference's own max-change test switched off)."""
     P.solver_order = abi.AM_ORDER_REFERENCE
-    P.iterations = SWEEP_CAP      # the reference's Gauss-Seidel, stopped by the same residual rule as the GPU
+    P.iterations = SWEEP_CAP
     P.tolerance = 0.0
+    return P
+
+
+def oracle_batch_sample(sc_list, P, dt, warmup, steps, stride=BATCH_SAMPLE_STRIDE):
+    """Oracle on every `stride`-th scene from the initial state, one core:
+    `warmup` untimed steps, then `steps` timed steps.  Returns scene-steps/s
+    of one core and a description of the sample."""
+    P = _reference_params(P)
     sample = sc_list[::stride]
-    jobs = [(s, P, dt, warmup, steps) for s in sample]
-    if workers > 1:
-        import multiprocessing as mp
-        with mp.get_context("spawn").Pool(workers) as pool:
-            ts = pool.map(_oracle_scene_time, jobs, chunksize=1)
-    else:
-        ts = [_oracle_scene_time(j) for j in jobs]
+    ts = [_oracle_scene_time((s, P, dt, warmup, steps)) for s in sample]
     t = sum(ts)
-    return workers * steps * len(sample) / t, (
-        f"{len(sample)} of {len(sc_list)} scenes (every {stride}th), {steps} timed steps after {warmup} from the "
-        f"initial state, {t:.1f} s of scene time on {workers} concurrent worker process(es); the reference's FP64 "
-        f"Gauss-Seidel in list order, stopped at relative LCP residual <= {RESIDUAL_TARGET:g} (checked every 10 "
-        f"sweeps, cap {SWEEP_CAP}) like the GPU arm")
+    return steps * len(sample) / t, (
+        f"{len(sample)} of {len(sc_list)} scenes (every {stride}th), steps {warmup + 1}..{warmup + steps} from the "
+        f"initial state, {t:.1f} s on one core; the reference's FP64 Gauss-Seidel in list order, stopped at "
+        f"relative LCP residual <= {RESIDUAL_TARGET:g} (checked every 10 sweeps, cap {SWEEP_CAP}) like the GPU arms")
 
 
-def cpu_baseline(name, max_seconds=15.0, max_steps=400, warmup=20, steps=10, n_scenes=BATCH_SCENES):
+def cpu_baseline(name, max_seconds=15.0, warmup=20, steps=10, n_scenes=BATCH_SCENES):
     """Oracle (single-threaded CPU restatement of the reference path) on the
     same workload: steps/s over a bounded sample."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -233,6 +252,61 @@ def cpu_baseline(name, max_seconds=15.0, max_steps=400, warmup=20, steps=10, n_s
                       f"{warmup + 1}..{warmup + steps}), {el:.1f} s, single thread, reference order"}
 
 
+_BARRIER = None
+
+
+def _ref_init(barrier):
+    global _BARRIER
+    _BARRIER = barrier
+
+
+def _ref_worker(job):
+    """A share of the scenes on one core: warm-up steps, then (after every
+    worker is ready) the timed steps.  Returns the monotonic clock at the start
+    and end of the timed steps."""
+    scenes_, P, dt, warmup, steps = job
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_binding import Oracle
+    ors = []
+    for s in scenes_:
+        o = Oracle(s, P)
+        o.set_residual_target(RESIDUAL_TARGET, 10)
+        o.step(dt, warmup)
+        ors.append(o)
+    _BARRIER.wait()
+    t0 = time.monotonic()
+    for _ in range(steps):
+        for o in ors:
+            o.step(dt)
+    return t0, time.monotonic()
+
+
+def oracle_batch_wall(sc_list, P, dt, warmup, steps, workers):
+    """Every scene of the batch on the oracle, spread over `workers` processes
+    (largest scenes first, each to the least loaded worker).  All workers warm
+    up, meet at a barrier, and step their scenes; the timed region is the wall
+    clock from the first start to the last end."""
+    import multiprocessing as mp
+    P = _reference_params(P)
+    workers = max(1, min(workers, len(sc_list)))
+    order = sorted(range(len(sc_list)), key=lambda k: -sc_list[k].n)
+    load = [0.0] * workers
+    share = [[] for _ in range(workers)]
+    for k in order:
+        w = min(range(workers), key=lambda i: load[i])
+        share[w].append(sc_list[k])
+        load[w] += sc_list[k].n ** 1.6
+    ctx = mp.get_context("spawn")
+    bar = ctx.Barrier(workers)
+    with ctx.Pool(workers, initializer=_ref_init, initargs=(bar,)) as pool:
+        res = pool.map(_ref_worker, [(sh, P, dt, warmup, steps) for sh in share], chunksize=1)
+    wall = max(t1 for _, t1 in res) - min(t0 for t0, _ in res)
+    return wall, (f"all {len(sc_list)} scenes, steps {warmup + 1}..{warmup + steps} from the initial state, on "
+                  f"{workers} worker processes (one core each), wall clock from the first timed step to the last; "
+                  f"the reference's FP64 Gauss-Seidel in list order, stopped at relative LCP residual <= "
+                  f"{RESIDUAL_TARGET:g} (checked every 10 sweeps, cap {SWEEP_CAP}) like the GPU arms")
+
+
 def run_reference(args):
     ws, rank, _ = dist_init()
     if rank != 0:
@@ -245,10 +319,15 @@ def run_reference(args):
     cores = 1
     if args.workload == "batch":
         cores = max(1, len(os.sched_getaffinity(0)))
-        v, desc = oracle_batch_sample(sc, P, dt, args.warmup, args.steps, stride=REFERENCE_SAMPLE_STRIDE,
-                                      workers=cores)
-        el = args.steps * len(sc) / v
+        el, desc = oracle_batch_wall(sc, P, dt, args.warmup, args.steps, cores)
+        cores = min(cores, len(sc))
+        v = args.steps * len(sc) / el
         unit = "scene-steps/s"
+        cfg = dict(cfg, pgs=f"FP64 projected Gauss-Seidel with box friction in the reference's list order "
+                            f"(PGS.java:73-194), previous-frame warm start, stopped at relative LCP residual <= "
+                            f"{RESIDUAL_TARGET:g} (checked every 10 sweeps, cap {SWEEP_CAP})",
+                   precision="fp64 throughout (the oracle, a C++ restatement of the reference path)",
+                   parallelism=f"scenes spread over {cores} host cores")
     else:
         o = Oracle(sc, P)
         o.step(dt, args.warmup)
@@ -257,6 +336,7 @@ def run_reference(args):
         el = time.perf_counter() - t0
         v = args.steps / el
         desc = f"{args.steps} steps after {args.warmup} warm-up steps, single thread"
+        cfg = dict(cfg, pgs_order="reference list order")
     out = {"metric": METRIC, "value": v, "unit": unit, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
@@ -266,10 +346,10 @@ def run_reference(args):
     print(json.dumps(out))
 
 
-def plain_gpu_pgs(sc_list, dt, warmup, steps, flush):
-    """The plain GPU PGS: the FP64 drop-in, one scene per context and launch
-    sequence (coloured full solve, stop at the same relative residual), on
-    every PLAIN_SAMPLE_STRIDE-th scene.  CUDA-event time per scene-step."""
+def fp64_drop_in_one_scene_at_a_time(sc_list, dt, warmup, steps, flush):
+    """The FP64 drop-in, one scene per context and launch sequence (coloured
+    full solve, stop at the same relative residual), on every
+    PLAIN_SAMPLE_STRIDE-th scene.  CUDA-event time per scene-step."""
     import torch
     from adaptivemerging_gb300 import native
     P = abi.default_params(gravity_amount=9.81, friction_override=0, restitution_override=1, restitution=0.0,
@@ -300,9 +380,105 @@ def plain_gpu_pgs(sc_list, dt, warmup, steps, flush):
         g.close()
     return {"value": 1e3 * n / tot_ms, "unit": "scene-steps/s",
             "sample": f"{len(sample)} of {len(sc_list)} scenes (every {PLAIN_SAMPLE_STRIDE}th) stepped one at a "
-                      f"time, {steps} timed steps each after {warmup}, FP64 coloured PGS to relative residual <= "
+                      f"time, steps {warmup + 1}..{warmup + steps}, FP64 coloured PGS to relative residual <= "
                       f"{RESIDUAL_TARGET:g} (cap {SWEEP_CAP})",
             "frac_scene_steps_residual_le_1e-6": conv / max(1, n), "pgs_sweeps_mean": float(np.mean(sweeps))}
+
+
+def _batch_system(sc, P, threads, accel, stage=0):
+    from adaptivemerging_gb300 import native
+    g = native.BatchSystem(sc, P, threads=threads, residual_target=RESIDUAL_TARGET, check_every=10)
+    g.set_accel(accel)
+    if stage:
+        g.set_stage(stage)
+    return g
+
+
+def time_batch_window(g, dt, steps, flush, stream, pin=None, n_units=None):
+    """K timed steps of a BatchSystem (device time on its stream, L2 flushed
+    between steps).  With `pin` (pinned host body state), every step also
+    pushes the state before and reads it back after (the end-to-end figure).
+    Per step: sweeps and residual of every scene and the critical path."""
+    import torch
+    g.reset_perf()
+    p0 = g.perf()
+    out = {"ms": 0.0, "e2e_s": 0.0, "put_get_s": [0.0, 0.0], "contacts": [], "sweeps_mean": [], "conv": [],
+           "res_max": [], "floor_cycles": 0, "sweeps_total": 0}
+    for _ in range(steps):
+        flush.fill_(1.0)                     # L2 flush between timed steps
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        ta = time.perf_counter()
+        if pin is not None:
+            g.put_bodies_struct(pin)         # H2D of the host-owned state
+        tb = time.perf_counter()
+        e0.record(stream)
+        g.step(dt)
+        e1.record(stream)
+        tc = time.perf_counter()
+        if pin is not None:
+            g.get_bodies_struct(pin)         # D2H of the new state
+        td = time.perf_counter()
+        e1.synchronize()
+        out["ms"] += e0.elapsed_time(e1)
+        out["e2e_s"] += td - ta
+        out["put_get_s"][0] += tb - ta
+        out["put_get_s"][1] += td - tc
+        st = g.stats()
+        bs = g.batch_stats()
+        ss = g.scene_stats()
+        chain = g.scene_chain()
+        out["contacts"].append(st.n_contacts)
+        out["sweeps_mean"].append(bs.sweeps_sum / max(1, bs.n_scenes))
+        out["conv"].append(float(np.mean(ss["residual"] <= RESIDUAL_TARGET)))
+        out["res_max"].append(float(ss["residual"].max()))
+        out["floor_cycles"] += int((ss["sweeps"].astype(np.int64) * chain).max()) * CHAIN_CYCLES_PER_CONTACT
+        out["sweeps_total"] += int(ss["sweeps"].sum())
+    torch.cuda.synchronize()
+    p1 = g.perf()
+    out["launches"] = int(p1.launches - p0.launches)
+    out["pgs_ms"] = p1.pgs_ms - p0.pgs_ms
+    out["contact_sweeps"] = int(p1.contact_sweeps - p0.contact_sweeps)
+    out["phases_ms"] = g.step_phases()
+    bst = g.batch_stats()
+    out["last"] = {"cta_threads": int(bst.threads), "stage_slots": int(bst.stage_slots),
+                   "resident_scenes": int(bst.resident_scenes), "cluster_scenes": int(bst.cluster_scenes),
+                   "cluster_size": int(bst.cluster_size)}
+    return out
+
+
+def summarise_window(w, steps, n_units, first, label):
+    ms = w["ms"] / steps
+    return {"value": 1e3 * n_units / ms, "unit": "scene-steps/s", "ms_per_step": ms,
+            "window": f"steps {first + 1}..{first + steps} from the initial state ({label})",
+            "frac_scene_steps_residual_le_1e-6": float(np.mean(w["conv"])),
+            "residual_rel_max": float(np.max(w["res_max"])), "pgs_sweeps_mean": float(np.mean(w["sweeps_mean"])),
+            "contacts_mean": float(np.mean(w["contacts"])),
+            "phases_ms_per_step": {k: v / steps for k, v in w["phases_ms"].items()}}
+
+
+def plain_fp32_one_scene_at_a_time(sc_list, P, dt, warmup, steps, flush):
+    """Plain FP32 PGS on the batched kernels, one scene per context and
+    launch sequence, on every PLAIN_SAMPLE_STRIDE-th scene."""
+    import torch
+    sample = sc_list[::PLAIN_SAMPLE_STRIDE]
+    tot_ms, n, conv = 0.0, 0, []
+    for s in sample:
+        g = _batch_system([s], P, 0, 0)
+        stream = torch.cuda.ExternalStream(g.stream_handle())
+        for _ in range(warmup):
+            g.step(dt)
+        w = time_batch_window(g, dt, steps, flush, stream)
+        tot_ms += w["ms"]
+        n += steps
+        conv += w["conv"]
+        g.close()
+    return {"value": 1e3 * n / tot_ms, "unit": "scene-steps/s",
+            "sample": f"{len(sample)} of {len(sc_list)} scenes (every {PLAIN_SAMPLE_STRIDE}th), each alone in its "
+                      f"own context, steps {warmup + 1}..{warmup + steps}, plain FP32 PGS on the batched kernels "
+                      f"to relative residual <= {RESIDUAL_TARGET:g} (cap {SWEEP_CAP})",
+            "frac_scene_steps_residual_le_1e-6": float(np.mean(conv))}
 
 
 def learned_protocol(sc_list, P, dt, collect_steps=100, compare_steps=30, stride=4):
@@ -357,16 +533,14 @@ def run_ours(args):
     barrier(ws)
     sc, P, dt, cfg = workload(args.workload, args.scenes)
     batch = args.workload == "batch"
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     if batch:
-        sysm = native.BatchSystem(sc, P, threads=args.threads, residual_target=RESIDUAL_TARGET, check_every=10)
-        if args.stage:
-            sysm.set_stage(args.stage)
+        sysm = _batch_system(sc, P, args.threads, 1, args.stage)
         n_units = len(sc)
     else:
         sysm = native.System(sc, P)
         n_units = 1
     stream = torch.cuda.ExternalStream(sysm.stream_handle())
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     # host-owned body state in pinned memory: every timed step pushes it to the
     # device, steps, and reads it back (the end-to-end figure); the device
     # time of the step alone is the `value` figure, on the same steps
@@ -384,107 +558,145 @@ def run_ours(args):
     for _ in range(args.warmup):
         sysm.step(dt)
     sysm.get_bodies_struct(st_s)
-    sysm.reset_perf()
-    p0 = sysm.perf()
     barrier(ws)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
     if args.profile:
         torch.cuda.profiler.start()
-    total_ms = 0.0
-    e2e_s = 0.0
-    split = [0.0, 0.0]
-    sweeps, contacts, res = [], [], []
-    conv = []
-    for _ in range(args.steps):
-        flush.fill_(1.0)                     # L2 flush between timed steps
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        ta = time.perf_counter()
-        sysm.put_bodies_struct(st_s)         # H2D of the host-owned state
-        tb = time.perf_counter()
-        e0.record(stream)
-        sysm.step(dt)
-        e1.record(stream)
-        tc = time.perf_counter()
-        sysm.get_bodies_struct(st_s)         # D2H of the new state
-        td = time.perf_counter()
-        e1.synchronize()
-        total_ms += e0.elapsed_time(e1)
-        e2e_s += td - ta
-        split[0] += tb - ta
-        split[1] += td - tc
-        st = sysm.stats()
-        contacts.append(st.n_contacts)
-        if batch:
-            bs = sysm.batch_stats()
-            sweeps.append(bs.sweeps_sum / max(1, bs.n_scenes)); res.append(bs.residual_max)
-            conv.append(bs.converged / max(1, bs.n_scenes))
-        else:
-            sweeps.append(st.sweeps); res.append(st.residual_rel)
+    if batch:
+        w = time_batch_window(sysm, dt, args.steps, flush, stream, pin=st_s)
+        total_ms, e2e_s, split = w["ms"], w["e2e_s"], w["put_get_s"]
+        launches = w["launches"]
+        pgs_ms = w["pgs_ms"]
+    else:
+        sysm.reset_perf()
+        p0 = sysm.perf()
+        total_ms = e2e_s = 0.0
+        split = [0.0, 0.0]
+        res = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            ta = time.perf_counter()
+            sysm.put_bodies_struct(st_s)
+            tb = time.perf_counter()
+            e0.record(stream)
+            sysm.step(dt)
+            e1.record(stream)
+            tc = time.perf_counter()
+            sysm.get_bodies_struct(st_s)
+            td = time.perf_counter()
+            e1.synchronize()
+            total_ms += e0.elapsed_time(e1)
+            e2e_s += td - ta
+            split[0] += tb - ta
+            split[1] += td - tc
+            res.append(sysm.stats().residual_rel)
+        p1 = sysm.perf()
+        launches = int(p1.launches - p0.launches)
+        pgs_ms = p1.pgs_ms - p0.pgs_ms
     torch.cuda.synchronize()
     if args.profile:
         torch.cuda.profiler.stop()
     clk = clocks.stop()
     barrier(ws)
-    p1 = sysm.perf()
     t_max = max_over_ranks(ws, total_ms / 1e3, "cuda")
     value = ws * args.steps * n_units / t_max
     e2e_t = max_over_ranks(ws, e2e_s, "cuda")
     e2e = ws * args.steps * n_units / e2e_t
-
-    pgs_l = p1.pgs_launches - p0.pgs_launches
-    pgs_ms = p1.pgs_ms - p0.pgs_ms
-    cs = p1.contact_sweeps - p0.contact_sweeps
-    peak, peak_kind = measured_peak()
-    bpcs = FP32_BYTES_PER_CONTACT_SWEEP if batch else FP64_BYTES_PER_CONTACT_SWEEP
-    achieved = (cs * bpcs / pgs_l) / (pgs_ms / pgs_l / 1e3) / 1e9 if pgs_l and pgs_ms else 0.0
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "pgs_traffic.json")
-    if os.path.exists(tf):
-        with open(tf) as f:
-            traffic = json.load(f).get(args.workload)
     if rank != 0:
         return
-    cfg.update({"contacts_mean": float(np.mean(contacts)), "pgs_sweeps_mean": float(np.mean(sweeps)),
-                "residual_rel_mean": float(np.mean(res)), "residual_rel_max": float(np.max(res)),
-                "l2": "flushed between timed steps (256 MB write)",
+    peak, peak_kind = measured_peak()
+    unit = "scene-steps/s" if batch else "steps/s"
+    cfg.update({"l2": "flushed between timed steps (256 MB write)",
                 "parallelism": "independent scenes per GPU" if batch else "replicas only",
                 "timed_window": f"steps {args.warmup + 1}..{args.warmup + args.steps} from the initial state"})
-    if batch:
-        cfg["frac_scene_steps_residual_le_1e-6"] = float(np.mean(conv))
-        bst = sysm.batch_stats()
-        cfg["cta_threads"] = int(bst.threads)
-        cfg["stage_slots"] = int(bst.stage_slots)
-        cfg["resident_scenes_last_step"] = int(bst.resident_scenes)
-        cfg["cluster_scenes_last_step"] = int(bst.cluster_scenes)
-        cfg["cluster_size"] = int(bst.cluster_size)
-    else:
-        cfg["frac_steps_residual_le_1e-6"] = float(np.mean(np.array(res) <= 1e-6))
-    unit = "scene-steps/s" if batch else "steps/s"
     out = {"metric": METRIC, "value": value, "unit": unit, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if batch else "f64", "data": "synthetic",
            "config": cfg,
            "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                    "ms_per_step_put_get": [1e3 * x / args.steps for x in split],
-                   "note": "same steps as value; wall time of push + step + read back"},
-           "gpu_launches": int(p1.launches - p0.launches),
-           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak if peak else None, "traffic": traffic,
-                        "kernel": "k_batch_sweep" if batch else "k_pgs_fast", "peak_source": peak_kind,
-                        "bytes_per_contact_sweep": bpcs,
-                        "pgs_ms_per_launch": pgs_ms / pgs_l if pgs_l else None},
-           "clocks": clk}
-    if batch and not args.no_plain:
+                   "note": "same steps as value; wall time of push + step + read back through the C ABI"},
+           "gpu_launches": launches, "clocks": clk}
+    if batch:
+        sm_mhz = clk.get("sm_mhz") or 2070.0
+        head = summarise_window(w, args.steps, n_units, args.warmup, "the timed steps")
+        cfg.update({k: head[k] for k in ("frac_scene_steps_residual_le_1e-6", "residual_rel_max",
+                                         "pgs_sweeps_mean", "contacts_mean")})
+        cfg.update(w["last"])
+        sweep_ms = pgs_ms / args.steps
+        bytes_step = head["contacts_mean"] * SWEEP_HBM_BYTES_PER_CONTACT + cfg["bodies"] * SWEEP_HBM_BYTES_PER_BODY
+        achieved = bytes_step / (sweep_ms / 1e3) / 1e9 if sweep_ms > 0 else 0.0
+        traffic = None
+        tf = os.path.join(ROOT, "profiles", "k_batch_sweep_traffic.json")
+        if os.path.exists(tf):
+            with open(tf) as f:
+                tj = json.load(f)
+            if tj.get("warmup") == args.warmup and tj.get("steps") == args.steps:
+                traffic = tj.get("dram_bytes_per_step")
+        floor_ms = w["floor_cycles"] / (sm_mhz * 1e3) / args.steps
+        out["roofline"] = {
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if peak else None, "traffic": traffic, "peak_source": peak_kind,
+            "kernel": "k_batch_sweep + k_batch_sweep_cluster (all sweep launches of a step)",
+            "sweep_ms_per_step": sweep_ms,
+            "algorithmic_bytes_per_step": bytes_step,
+            "note": "compulsory HBM bytes of the sweep launches (records and multipliers in once, results out "
+                    "once); every sweep after the first reads shared memory, so the sweep is not HBM-bound: "
+                    "see critical_path"}
+        out["critical_path"] = {
+            "bound": "dependent-chain latency", "unit": "ms per step",
+            "floor_ms_per_step": floor_ms, "sweep_ms_per_step": sweep_ms,
+            "frac": floor_ms / sweep_ms if sweep_ms > 0 else None,
+            "cycles_per_contact": CHAIN_CYCLES_PER_CONTACT, "sm_mhz": sm_mhz,
+            "definition": "per step, max over scenes of sweeps x (sum over colours of the longest body-pair group "
+                          "in contacts) x cycles of one contact update's arithmetic chain, at the sampled SM clock; "
+                          "the scenes run concurrently, so the slowest chain bounds the sweep launches"}
+        out["phases_ms_per_step"] = head["phases_ms_per_step"]
+        out["phases_note"] = ("device time between consecutive CUDA events on the library stream; the phases add up "
+                              "to the step, host waits included")
         sysm.close()
-        pl = plain_gpu_pgs(sc, dt, args.warmup, min(args.steps, 10), flush)
-        pl["batched_over_plain"] = value / pl["value"]
-        out["plain_gpu_pgs"] = pl
-    if batch and args.learned:
-        out["learned_warm_start"] = learned_protocol(sc, P, dt)
+        # the same kernels and scenes, plain projected Gauss-Seidel
+        pg = _batch_system(sc, P, args.threads, 0, args.stage)
+        pstream = torch.cuda.ExternalStream(pg.stream_handle())
+        for _ in range(args.warmup):
+            pg.step(dt)
+        pw = time_batch_window(pg, dt, args.steps, flush, pstream)
+        plain = summarise_window(pw, args.steps, n_units, args.warmup, "the timed steps")
+        plain["pgs"] = "FP32 projected Gauss-Seidel, no acceleration, previous-frame warm start, same kernels"
+        out["plain_gpu_pgs"] = plain
+        out["accelerated_over_plain"] = value / plain["value"]
+        # the steady window (steps 21..60) beside the timed one, both arms
+        if (args.warmup, args.steps) != STEADY and not args.no_steady:
+            steady = {}
+            for name, acc in (("accelerated", 1), ("plain", 0)):
+                g = _batch_system(sc, P, args.threads, acc, args.stage)
+                gs = torch.cuda.ExternalStream(g.stream_handle())
+                for _ in range(STEADY[0]):
+                    g.step(dt)
+                sw = time_batch_window(g, dt, STEADY[1], flush, gs)
+                steady[name] = summarise_window(sw, STEADY[1], n_units, STEADY[0], "steady window")
+                g.close()
+            steady["accelerated_over_plain"] = steady["accelerated"]["value"] / steady["plain"]["value"]
+            out["steady_window"] = steady
+        pg.close()
+        if not args.no_plain:
+            k1 = min(args.steps, 10)
+            one = plain_fp32_one_scene_at_a_time(sc, P, dt, args.warmup, k1, flush)
+            one["batched_accelerated_over_this"] = value / one["value"]
+            out["plain_gpu_pgs_one_scene_at_a_time"] = one
+            f64 = fp64_drop_in_one_scene_at_a_time(sc, dt, args.warmup, k1, flush)
+            f64["batched_accelerated_over_this"] = value / f64["value"]
+            out["fp64_drop_in_one_scene_at_a_time"] = f64
+        if args.learned:
+            out["learned_warm_start"] = learned_protocol(sc, P, dt)
+    else:
+        cfg["frac_steps_residual_le_1e-6"] = float(np.mean(np.array(res) <= 1e-6))
+        out["pgs_ms_per_step"] = pgs_ms / args.steps
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.workload, warmup=args.warmup,
                                            steps=min(args.steps, 10) if batch else args.steps, n_scenes=args.scenes)
@@ -499,7 +711,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-plain", action="store_true", help="skip the plain GPU PGS comparison arm")
+    ap.add_argument("--no-plain", action="store_true", help="skip the one-scene-at-a-time comparison arms")
+    ap.add_argument("--no-steady", action="store_true", help="skip the steady-window (steps 21..60) figures")
     ap.add_argument("--learned", action="store_true", help="also run the learned warm-start protocol")
     ap.add_argument("--threads", type=int, default=0, help="batched solve: CTA size (0: autotuned)")
     ap.add_argument("--scenes", type=int, default=BATCH_SCENES, help="bins in the batch (profiling runs only)")

@@ -207,6 +207,25 @@ int32_t am_solve(void* ctx, double dt, am_solve_stats* stats);
 /* RigidBody.advanceVelocities + advancePositions for all bodies (RigidBody.java:409-441). */
 int32_t am_integrate(void* ctx, double dt);
 
+/*
+ * Snapshot and restore between steps.  The reference rebuilds its state from
+ * Java objects (RigidBodySystem.reset, RigidBodySystem.java:390-426; the
+ * contact pool, ContactPool.java:23-73; body-pair contacts with their
+ * motion-metric and contact-state histories, BodyPairContact.java:83-145;
+ * collections, RigidCollection.java).  am_get_state writes all of the
+ * context's state into one byte blob: bodies (with collections and sleeping
+ * histories), the last step's contacts with multipliers and warm-start copies,
+ * contacts inside collections, body-pair contacts and their histories, the
+ * step counter.  With capacity too small (or 0) it returns AM_E_CAPACITY and
+ * the size needed in *size.  am_put_state restores a blob into a context
+ * loaded with the same scene (am_set_scene / am_set_batch with the same
+ * bodies; AM_E_STATE otherwise, AM_E_ARG for a malformed blob): the steps that
+ * follow are bit-identical to those that followed the snapshot.  The blob is
+ * for this library build only.
+ */
+int32_t am_get_state(void* ctx, void* buf, int64_t capacity, int64_t* size);
+int32_t am_put_state(void* ctx, const void* buf, int64_t size);
+
 /* Read back. */
 int32_t am_get_bodies(void* ctx, am_body_state* out);
 /* Write x / R / v / omega of the free scene bodies (a caller that owns the
@@ -271,6 +290,15 @@ int32_t am_set_batch_cluster_stage(void* ctx, int32_t slots);
  * over-relaxation factor in (0, 2) applied before the projection (1 = plain
  * PGS), and symmetric = 1 to walk the colours backwards on odd sweeps */
 int32_t am_set_batch_relaxation(void* ctx, double relax, int32_t symmetric);
+/* 1: every batched sweep is wrapped in a nonsmooth nonlinear conjugate-
+ * gradient step (Silcowitz, Niebe and Erleben 2010): with g the sweep's change
+ * of the multipliers and beta = |g_k|^2 / |g_k-1|^2, lambda += beta p and
+ * p = beta p + g, restarting (p = 0) when beta > 1.  Same fixed point as
+ * projected Gauss-Seidel, so the residual stopping rule is unchanged; results
+ * stay independent of CTA size, size classes, staging and clusters.  0 (default): plain
+ * projected Gauss-Seidel, PGS.java:73-194.  Wraps the reference's sweep; no
+ * reference counterpart. */
+int32_t am_set_batch_accel(void* ctx, int32_t mode);
 /* coloured full solve of a single scene (AM_ORDER_COLOURED): stop once the
  * relative natural-map residual is <= residual_target, tested every
  * check_every sweeps (0 disables; the reference's max-change tolerance still
@@ -283,6 +311,16 @@ int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, in
  * relative to the earliest start) and the SM it ran on (a cluster: its first
  * CTA).  Any pointer may be null.  No reference counterpart. */
 int32_t am_get_batch_scene_times(void* ctx, int64_t* start_ns, int64_t* end_ns, int32_t* sm);
+/* per scene, last batched solve: CTAs that solved it (1: one CTA, a size
+ * class or the streaming launch; 2, 4 or 8: a thread-block cluster).  No
+ * reference counterpart. */
+int32_t am_get_batch_scene_ctas(void* ctx, int32_t* ctas);
+/* per scene, last batched solve: the critical path of one sweep in contacts,
+ * the sum over the scene's colours of its longest body-pair group (the
+ * contacts of a group update one after another; a colour ends with its
+ * longest group).  Sweeps x this x the cycles of one contact update bound the
+ * scene's solve time from below.  No reference counterpart. */
+int32_t am_get_batch_scene_chain(void* ctx, int32_t* chain);
 
 /*
  * Learned warm start for the batched solve (no reference counterpart).  An
@@ -319,8 +357,11 @@ int32_t am_learned_infer(void* ctx, const float* X, int32_t n, float* out, int32
  * thread, where cudaMalloc / cudaFree can stall on device-wide
  * synchronisation, and hosts that reserve the device memory for their own
  * pool up front and leave the library none to take mid-run.
- *   - needs the context's weights set up first (am_learned_use,
- *     am_learned_weights or am_learned_train), else AM_E_STATE;
+ *   - needs the context's weights set up first (am_learned_use with a
+ *     mode > 0, am_learned_weights with weights to set, or
+ *     am_learned_train), else AM_E_STATE;
+ *   - the context's device (current at am_create) must be the current
+ *     device, else AM_E_STATE;
  *   - n > AM_NOALLOC_MAX_ROWS returns AM_E_CAPACITY, n <= 0 AM_E_ARG;
  *   - errors are reported by the status alone (am_last_error is not updated);
  *   - the first call on a device, made with that device current, looks up
@@ -365,6 +406,21 @@ enum {
 };
 int32_t am_set_phase_timing(void* ctx, int32_t enable);
 int32_t am_get_phase_times(void* ctx, double* seconds /* [AM_NUM_PHASES] */);
+/* Device time of the phases of the batched am_step, in milliseconds summed
+ * over the steps since am_reset_perf, measured with CUDA events at the phase
+ * boundaries on the context stream: detection, warm start, solve set-up
+ * (contact setup, colouring, record packing, launch planning), the sweep
+ * launches, integration, statistics.  Boundaries are consecutive, so the
+ * phases add up to the device time of the steps, including the time the
+ * device waits on the host between phases.  No reference counterpart. */
+#define AM_STEP_PHASES 6
+int32_t am_get_step_phases(void* ctx, double* ms /* [AM_STEP_PHASES] */);
+/* Self-check of the bounded grid barrier of the FP64 sweeps: two blocks wait
+ * at a barrier that cannot complete, each giving up after 2^spin_log2 polls
+ * (1..24).  *status receives the device status word (AM_E_TIMEOUT when the
+ * bound works), which is then cleared; the context stays usable.  No
+ * reference counterpart. */
+int32_t am_check_barrier_timeout(void* ctx, int32_t spin_log2, int32_t* status);
 /* the context's cudaStream_t, for callers that order their own work after a step */
 int32_t am_get_stream(void* ctx, void** stream);
 

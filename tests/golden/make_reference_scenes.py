@@ -1,0 +1,46 @@
+"""Regenerates tests/golden/reference_scenes.json from the reference's own
+scene files.
+
+    python tests/golden/make_reference_scenes.py [reference project root]
+
+Two of the reference's XML scenes, `scenes3D/tower30.xml` (135 boxes in a
+ring tower on a plane) and `scenes3D/denseTower25.xml` (78 boxes), are parsed
+by this repository's loader (adaptivemerging_gb300.scene_xml) and stored as
+the loader's output: the am_scene arrays, the am_params fields the scene sets,
+and the body names.  The reference tree is not present where the GPU tests
+run, so the tests read this fixture instead of the XML files.  The first rows
+(#bodies, #contacts) of the reference's recorded metrics for tower30
+(`scenes3D/csv/conditional_acceptance_revisions/tower30_merged.csv`) are kept
+beside them as recorded.
+"""
+import csv
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from adaptivemerging_gb300 import abi, scene_xml  # noqa: E402
+
+SCENES = ("tower30", "denseTower25")
+CSV = "scenes3D/csv/conditional_acceptance_revisions/tower30_merged.csv"
+
+
+def main():
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    out = {"source": "reference scenes3D/*.xml parsed by adaptivemerging_gb300.scene_xml", "scenes": {}}
+    for name in SCENES:
+        sc, P, names = scene_xml.load(os.path.join(root, "scenes3D", name + ".xml"))
+        arrays = {k: v.tolist() for k, v in sc.a.items()}
+        prm = {f: getattr(P, f) for f, _ in abi.am_params._fields_}
+        out["scenes"][name] = {"arrays": arrays, "params": prm, "names": names}
+    with open(os.path.join(root, CSV)) as f:
+        rows = list(csv.reader(f))[1:]
+    out["tower30_csv_bodies_contacts"] = [[int(r[0]), int(r[1])] for r in rows[:60] if len(r) > 2]
+    with open(os.path.join(HERE, "reference_scenes.json"), "w") as f:
+        json.dump(out, f, separators=(",", ":"))
+
+
+if __name__ == "__main__":
+    main()

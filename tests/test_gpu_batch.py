@@ -101,15 +101,19 @@ def test_batch_residual_target_stops_early(gpu_lib):
     assert st.converged == len(sc) and st.sweeps_max < 2000 and st.residual_max <= 1e-5
 
 
-def test_cluster_path_converges_to_oracle(gpu_lib):
+@pytest.mark.parametrize("accel", [0, 1])
+def test_cluster_path_converges_to_oracle(gpu_lib, accel):
     """A bin too large for one CTA's shared memory is solved by a thread-block
     cluster; its converged multipliers match the FP64 oracle like the one-CTA
-    path's, and the streaming one-CTA path (clusters off) agrees."""
+    path's, and the streaming one-CTA path (clusters off) agrees, with and
+    without the conjugate-gradient acceleration."""
     from adaptivemerging_gb300 import native
     sc = [scenes.bin_scene(1400, 77, gap=-0.001), scenes.bin_scene(40, 78, gap=-0.001)]
-    P = params(friction_override=0, iterations=20000, tolerance=0.0)
+    P = params(friction_override=0, iterations=20000 if not accel else 6000, tolerance=0.0)
     g = native.BatchSystem(sc, P, threads=256, residual_target=0.0, check_every=0)
     h = native.BatchSystem(sc, P, threads=256, residual_target=0.0, check_every=0)
+    g.set_accel(accel)
+    h.set_accel(accel)
     h.set_clusters(False)
     g.step(DT)
     h.step(DT)
@@ -132,18 +136,23 @@ def test_cluster_path_converges_to_oracle(gpu_lib):
     assert np.array_equal(part["lambda"], parth["lambda"])
 
 
-def test_results_do_not_depend_on_kernel_shape(gpu_lib):
+@pytest.mark.parametrize("accel", [0, 1])
+def test_results_do_not_depend_on_kernel_shape(gpu_lib, accel):
     """A batch stepped with the residual target gives bit-identical states
     whatever CTA size, staging capacity, size classes and cluster use it runs
     with (the scenes stop at the same check and the per-group arithmetic is
-    shared)."""
+    shared).  With the conjugate-gradient acceleration on, its |g|^2 sum runs
+    in one fixed order in every kernel, so the same holds; the last
+    configuration repeats the first, so two runs of one shape agree too."""
     from adaptivemerging_gb300 import native
     sc = [scenes.bin_scene(n, 500 + n, gap=0.01) for n in (25, 40, 120, 300, 900, 1500)]
     P = params(friction_override=0, iterations=3000)
     runs = []
     for threads, stage, clusters, classes in ((128, 64, True, True), (256, 256, True, False),
-                                              (512, 128, False, True), (256, 256, True, True)):
+                                              (512, 128, False, True), (256, 256, True, True),
+                                              (128, 64, True, True)):
         g = native.BatchSystem(sc, P, threads=threads, residual_target=1e-6, check_every=10)
+        g.set_accel(accel)
         g.set_stage(stage)
         g.set_clusters(clusters)
         g.set_size_classes(classes)
@@ -263,3 +272,55 @@ def test_batch_mixed_bodies_compliance_restitution(gpu_lib):
     assert n > 50
     print(f"mixed batch: {n} contacts, rel err {worst:.2e}")
     assert worst <= 2e-4
+
+
+def test_nncg_fewer_sweeps_same_fixed_point(gpu_lib):
+    """The conjugate-gradient acceleration keeps the PGS fixed point: after the
+    same plain steps, one step solved to the residual target with and without
+    it takes at least 1.5 times fewer sweeps summed over the bins, with
+    multipliers within FP32 tolerance of each other; run to its fixed point
+    (a fixed 20000 sweeps) it gives the FP64 oracle's multipliers from the
+    same state within 2e-4."""
+    from adaptivemerging_gb300 import native
+    sc = [scenes.bin_scene(n, 600 + n, gap=0.01) for n in (60, 150, 300, 700, 1200)]
+    P = params(friction_override=0, iterations=30000)
+    a = native.BatchSystem(sc, P, threads=0, residual_target=1e-6, check_every=10)
+    b = native.BatchSystem(sc, P, threads=0, residual_target=1e-6, check_every=10)
+    for _ in range(30):
+        a.step(DT)
+        b.step(DT)
+    assert np.array_equal(a.bodies()["x"], b.bodies()["x"])
+    bod = a.bodies()
+    b.set_accel(1)
+    a.step(DT)
+    b.step(DT)
+    sa, sb = a.scene_stats(), b.scene_stats()
+    assert (sa["residual"] <= 1e-6).all() and (sb["residual"] <= 1e-6).all(), (sa["residual"], sb["residual"])
+    ratio = sa["sweeps"].sum() / max(1, sb["sweeps"].sum())
+    print("sweeps plain", sa["sweeps"], "nncg", sb["sweeps"], f"ratio {ratio:.2f}")
+    assert ratio >= 1.5
+    la, lb = a.contacts()["lambda"], b.contacts()["lambda"]
+    scale = max(1.0, float(np.abs(la).max()))
+    assert float(np.abs(la - lb).max()) / scale <= 2e-4
+    # the largest bin against the oracle from the same state (no warm start there)
+    k = len(sc) - 1
+    lo, hi = a.offsets[k], a.offsets[k + 1]
+    arr = {q: np.array(v, copy=True) for q, v in sc[k].a.items()}
+    body = arr["type"] != abi.AM_PLANE
+    for key, m in (("x", 3), ("R", 9), ("v", 3), ("omega", 3)):
+        t = arr[key].reshape(-1, m)
+        t[body] = bod[key][lo:hi][body]
+        arr[key] = t.reshape(-1)
+    o = Oracle(abi.SceneArrays(**arr), params(friction_override=0, iterations=400000, tolerance=0.0))
+    o.set_residual_target(1e-10, 10)
+    o.step(DT)
+    co = o.contacts()
+    c = native.BatchSystem([abi.SceneArrays(**arr)], params(friction_override=0, iterations=20000), threads=0,
+                           residual_target=0.0, check_every=0)
+    c.set_accel(1)
+    c.step(DT)
+    part = _split(c.contacts(), [sc[k]])[0]
+    assert np.array_equal(part["body1"], co["body1"]) and np.array_equal(part["info"], co["info"])
+    err = float(np.abs(part["lambda"] - co["lambda"]).max()) / max(1.0, float(np.abs(co["lambda"]).max()))
+    print(f"nncg vs oracle: {len(co['body1'])} contacts, rel err {err:.2e}")
+    assert err <= 2e-4

@@ -2,6 +2,8 @@
 PyTorch restatement of the same network, BF16 tensor-core inference against
 FP32, and what the learned start gains over the plain previous-frame start on
 batched scenes solved to a relative LCP residual of 1e-6."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -161,3 +163,16 @@ def test_learned_start_meets_residual_target_and_reports_gain(gpu_lib):
           f"fallback scene-steps {falls}")
     assert cs_learned > 0
     assert conv_learned >= conv_plain - 8   # the trajectories differ within the residual target
+
+
+def test_grid_barrier_wait_gives_up(gpu_lib):
+    """The bounded grid barrier of the FP64 sweeps: a barrier that cannot
+    complete (one arrival short) ends every block's wait after the poll limit
+    with AM_E_TIMEOUT in the status word, and the context keeps working."""
+    from adaptivemerging_gb300 import native
+    g = native.System(scenes.tower(4, seed=1), params(iterations=20))
+    st = C.c_int32(0)
+    g._check(native.lib().am_check_barrier_timeout(g.h, 12, C.byref(st)))
+    assert st.value == -4                          # AM_E_TIMEOUT
+    g.step(0.01)                                   # the context still steps
+    assert g.num_contacts() > 0

@@ -1,0 +1,91 @@
+"""The reference's own scene files (scenes3D/tower30.xml, denseTower25.xml),
+as parsed by this repository's loader and stored in
+tests/golden/reference_scenes.json by make_reference_scenes.py.
+
+- CPU: the oracle runs both scenes; its top-level body count matches the
+  reference's recorded metrics for tower30 (136 in every early row).  The
+  recorded contact counts are not reproduced: the metrics file holds about
+  534 contacts at the second step where the oracle (and the reference's
+  BoxBox.java in this tree, which keeps every clipped point) gives 1548, six
+  per box-box pair.  The run that wrote the file used a scene or code state
+  that is not in the tree, so the counts pin nothing and are only reported.
+- GPU: the device path in reference order reproduces the oracle bit for bit
+  on both scenes with the scenes' own parameters and merging on (every 10
+  steps for 400 steps: topology, contacts, bodies, merge / unmerge counts).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from adaptivemerging_gb300 import abi
+from helpers import compare_bodies, compare_contacts
+from oracle_binding import Oracle
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _load(name):
+    with open(os.path.join(HERE, "golden", "reference_scenes.json")) as f:
+        d = json.load(f)
+    s = d["scenes"][name]
+    sc = abi.SceneArrays(**s["arrays"])
+    P = abi.am_params()
+    for k, v in s["params"].items():
+        setattr(P, k, v)
+    return sc, P, d
+
+
+def test_tower30_oracle_against_recorded_metrics():
+    sc, P, d = _load("tower30")
+    rows = d["tower30_csv_bodies_contacts"]
+    assert sc.n == 136 and len(rows) >= 20
+    o = Oracle(sc, P)
+    ours = []
+    for k in range(12):
+        o.step(0.01)
+        ours.append((o.counters()["top"], o.num_contacts()))
+    # row r of the metrics file is written by step r + 2 (the first call writes the header)
+    for r in range(8):
+        assert ours[r + 1][0] == rows[r][0] == 136
+    print("step, recorded contacts, oracle contacts:",
+          [(r + 2, rows[r][1], ours[r + 1][1]) for r in range(8)])
+
+
+@pytest.mark.parametrize("name", ["tower30", "denseTower25"])
+def test_reference_scene_runs_on_oracle(name):
+    sc, P, _ = _load(name)
+    o = Oracle(sc, P)
+    o.step(0.01, 150)
+    c = o.counters()
+    assert o.num_contacts() >= 0 and np.isfinite(o.bodies()["x"]).all()
+    assert c["merges"] > 0, c
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["tower30", "denseTower25"])
+def test_reference_scene_device_bit_exact(gpu_lib, name):
+    from adaptivemerging_gb300 import native
+    sc, P, _ = _load(name)
+    assert P.enable_merging == 1 and P.solver_order == abi.AM_ORDER_REFERENCE
+    g = native.System(sc, P)
+    o = Oracle(sc, P)
+    seen = 0
+    for s in range(400):
+        g.step(0.01)
+        o.step(0.01)
+        if s % 10 == 9:
+            assert g.topology() == o.topology(), f"step {s}: topology"
+            cg, co = g.contacts(), o.contacts()
+            seen += len(co["body1"])
+            assert len(cg["body1"]) == len(co["body1"]), f"step {s}"
+            msg = compare_contacts(cg, co)
+            assert msg is None, f"step {s}: {msg}"
+            msg = compare_bodies(g.bodies(), o.bodies())
+            assert msg is None, f"step {s}: {msg}"
+            c, pg = o.counters(), g.perf()
+            assert (pg.merge_events, pg.unmerge_events) == (c["merges"], c["unmerges"]), f"step {s}"
+    c = o.counters()
+    print(f"{name}: {c['merges']} merges, {c['unmerges']} unmerges, {seen} contacts checked")
+    assert seen > 0 and c["merges"] > 0

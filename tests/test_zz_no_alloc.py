@@ -64,7 +64,34 @@ def test_noalloc_inference_matches_allocating_call(gpu_lib):
     assert r == -1                                 # AM_E_ARG
 
 
+def test_noalloc_inference_takes_no_device_memory(gpu_lib):
+    """After the first call, calls of several sizes leave the device's free
+    memory where it was: nothing is allocated per call."""
+    import torch
+    L = gpu_lib
+    g = _system()
+    rng = np.random.default_rng(5)
+    n_par = g.learned_info()["n_params"]
+    g.learned_weights(set_w=(rng.standard_normal(n_par) * 0.3).astype(np.float32))
+    X = rng.standard_normal((_max_rows(), NIN)).astype(np.float32)
+    assert _noalloc(L, g, X[:10], 1)[0] == 0       # first call: looks up the scratch
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for n in (1, 777, 4096, 30000, _max_rows()):
+        for tc in (1, 0):
+            assert _noalloc(L, g, X[:n], tc)[0] == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
 def test_noalloc_inference_needs_weights(gpu_lib):
     g = _system()
     r, _ = _noalloc(gpu_lib, g, np.zeros((4, NIN), np.float32), 1)
     assert r == -6                                 # AM_E_STATE: no weights set up yet
+    # recording samples initialises the network but sets up no weights either
+    g.learned_collect(True, 1000)
+    r, _ = _noalloc(gpu_lib, g, np.zeros((4, NIN), np.float32), 1)
+    assert r == -6
+    g.learned_use(1)                               # the default weights, packed for inference
+    r, out = _noalloc(gpu_lib, g, np.zeros((4, NIN), np.float32), 1)
+    assert r == 0 and np.isfinite(out).all()
