@@ -22,6 +22,8 @@ AM_E_STATE = -6
 AM_BOX, AM_SPHERE, AM_PLANE, AM_TREE = 0, 1, 2, 3
 AM_STATE_BROKEN, AM_STATE_ONEDGE, AM_STATE_CLEAR = 0, 1, 2
 AM_BV_NULL = -1
+# phases of the merging step (am_step_phase, AM_MPHASE_*)
+MPHASES = ("collide", "warm_start", "single_sweep", "unmerge", "solve", "advance", "merge", "finish")
 # device phases of a batched step (am_get_step_phases)
 STEP_PHASES = ("detection", "warm_start", "solve_setup", "sweeps", "integration", "statistics")
 AM_ORDER_REFERENCE, AM_ORDER_COLOURED = 0, 1
@@ -158,6 +160,11 @@ class SceneArrays:
         for k, v in self.a.items():
             setattr(s, k, ptr(v, _i32 if k in self.FIELDS_I else _f64))
         return s
+
+
+class am_bpc_tests(C.Structure):
+    _fields_ = [("body1", _P(_i32)), ("body2", _P(_i32)), ("kind", _P(_i32)), ("result", _P(_i32)),
+                ("metric", _P(_f64))]
 
 
 class Contacts:

@@ -332,8 +332,9 @@ __global__ void k_batch_slots(DContacts C, DPairs P, const int* pairOff, const i
         __syncthreads();
     }
     // slots of the scene, and the most a split of every colour into equal
-    // slot windows can add to one part (one group per colour)
-    if (t == 0) sceneSize[s] = make_int2(nslots, ncol * maxc);
+    // slot windows can add to one part: one group per colour, plus one slot
+    // per colour for rounding the window bounds
+    if (t == 0) sceneSize[s] = make_int2(nslots, ncol * (maxc + 1));
     int win = cap - maxc;
     if (win < maxc || win <= 0) {   // a group larger than half the staging buffer
         if (t == 0) { dc->error = AM_E_CAPACITY; nChunks[s] = 0; }
@@ -598,16 +599,33 @@ static const unsigned long long NNCG_CLAMP = 1ull << 50;
 // E0 of the sweep after one whose |g|^2 was gg (the first sweep: -10)
 __device__ __forceinline__ int nncg_e0(int it, float gg) {
     if (it == 0) return -10;
-    const float x = fmaxf(gg, 0x1p-100f);
-    return 10 - ilogbf(x);
+    const float x = fminf(fmaxf(gg, 0x1p-100f), 0x1p100f);
+    return 10 - (((int)(__float_as_uint(x) >> 23) & 255) - 127);   // 10 - floor(log2 x)
 }
+// x * 2^E rounded (half up) to an integer, clamped to 2^50; x >= 0 and
+// finite (zero and subnormal x lie below every scale used)
+__device__ __forceinline__ unsigned long long nncg_fixed(float x, int E) {
+    const unsigned b = __float_as_uint(x);
+    const int e = (int)(b >> 23) & 255;
+    if (e == 0) return 0ull;
+    const unsigned long long m = (b & 0x7FFFFFu) | 0x800000u;   // x = m 2^(e - 150)
+    const int sh = e - 150 + E;
+    if (sh >= 27) return NNCG_CLAMP;                               // m 2^sh >= 2^50
+    if (sh >= 0) return min(m << sh, NNCG_CLAMP);
+    if (sh < -25) return 0ull;
+    return (m + (1ull << (-sh - 1))) >> (-sh);
+}
+// a thread's |g|^2 accumulators at the four scales (named fields, so they
+// stay in registers inside the kernels' lambdas)
+struct Acc4 {
+    unsigned long long a0 = 0ull, a1 = 0ull, a2 = 0ull, a3 = 0ull;
+};
 // one group's squared change at the four scales, added to acc
-__device__ __forceinline__ void nncg_acc(float gsq, int e0, unsigned long long* acc) {
-#pragma unroll
-    for (int j = 0; j < NNCG_SCALES; j++) {
-        const float y = ldexpf(gsq, e0 + 16 * j);
-        acc[j] += (y >= 0x1p50f) ? NNCG_CLAMP : (unsigned long long)__float2ull_rn(y);
-    }
+__device__ __forceinline__ void nncg_acc(float gsq, int e0, Acc4& acc) {
+    acc.a0 += nncg_fixed(gsq, e0);
+    acc.a1 += nncg_fixed(gsq, e0 + 16);
+    acc.a2 += nncg_fixed(gsq, e0 + 32);
+    acc.a3 += nncg_fixed(gsq, e0 + 48);
 }
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
 #pragma unroll
@@ -615,19 +633,29 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     return v;
 }
 // a warp's accumulators into the CTA's shared totals (integer: any order)
-__device__ __forceinline__ void nncg_flush(unsigned long long* acc, unsigned long long* tot) {
-#pragma unroll
-    for (int j = 0; j < NNCG_SCALES; j++) {
-        const unsigned long long v = warp_sum_u64(acc[j]);
-        if ((threadIdx.x & 31) == 0 && v) atomicAdd(tot + j, v);
-        acc[j] = 0ull;
+__device__ __forceinline__ void nncg_flush(Acc4& acc, unsigned long long* tot) {
+    const unsigned long long v0 = warp_sum_u64(acc.a0), v1 = warp_sum_u64(acc.a1), v2 = warp_sum_u64(acc.a2),
+                             v3 = warp_sum_u64(acc.a3);
+    if ((threadIdx.x & 31) == 0) {
+        if (v0) atomicAdd(tot + 0, v0);
+        if (v1) atomicAdd(tot + 1, v1);
+        if (v2) atomicAdd(tot + 2, v2);
+        if (v3) atomicAdd(tot + 3, v3);
     }
+    acc = Acc4();
 }
 // |g|^2 from the totals of the four scales
 __device__ __forceinline__ float nncg_gg(const unsigned long long* tot, int e0) {
-    int j = NNCG_SCALES - 1;
-    while (j > 0 && tot[j] >= NNCG_CLAMP) j--;
-    return ldexpf(__ull2float_rn(tot[j]), -(e0 + 16 * j));
+    // the finest scale below the clamp (no dynamic index: tot may be registers)
+    const unsigned long long t0 = tot[0], t1 = tot[1], t2 = tot[2], t3 = tot[3];
+    const int j = t3 < NNCG_CLAMP ? 3 : (t2 < NNCG_CLAMP ? 2 : (t1 < NNCG_CLAMP ? 1 : 0));
+    const unsigned long long tj = j == 3 ? t3 : (j == 2 ? t2 : (j == 1 ? t1 : t0));
+    // the power-of-two scale 2^-E is applied in two exact steps, each a float
+    // built from its exponent bits
+    const int E = e0 + 16 * j;
+    const int h1 = -E / 2, h2 = -E - h1;   // both within the normal exponent range
+    return __fmul_rn(__fmul_rn(__ull2float_rn(tj), __int_as_float((h1 + 127) << 23)),
+                     __int_as_float((h2 + 127) << 23));
 }
 // the sweep's squared change of one contact, accumulated in a fixed order
 __device__ __forceinline__ float sq3_acc(const float* d, float acc) {
@@ -639,37 +667,59 @@ __device__ __forceinline__ float nncg_beta(int it, float gg, float ggPrev) {
     const float b = __fdiv_rn(gg, ggPrev);
     return (b <= 1.f) ? b : -1.f;   // also restarts on 0 / 0 and overflow
 }
-// one slot: lambda (3 of l), g and p (gp[0..2], gp[4..6])
+// one slot: lambda (xyz of the 16-byte multiplier slot, w = mu), g and p
+// (gp[0..2] and gp[4..6]; both 16-byte aligned, read and written as float4
+// so the 32-byte stride between slots costs few shared-memory wavefronts)
 __device__ __forceinline__ void nncg_slot(float* l, float* gp, int it, float beta) {
-    for (int q = 0; q < 3; q++) {
-        const float g = gp[q], p = gp[4 + q];
-        if (it == 0) {
-            gp[4 + q] = g;
-        } else if (beta < 0.f) {
-            gp[4 + q] = 0.f;
-        } else {
-            l[q] = __fmaf_rn(beta, p, l[q]);
-            gp[4 + q] = __fmaf_rn(beta, p, g);
-        }
+    float4 L = *reinterpret_cast<float4*>(l);
+    const float4 g = *reinterpret_cast<const float4*>(gp);
+    float4 p = *reinterpret_cast<const float4*>(gp + 4);
+    if (it == 0) {
+        p = g;
+    } else if (beta < 0.f) {
+        p = make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+        L.x = __fmaf_rn(beta, p.x, L.x);
+        L.y = __fmaf_rn(beta, p.y, L.y);
+        L.z = __fmaf_rn(beta, p.z, L.z);
+        p = make_float4(__fmaf_rn(beta, p.x, g.x), __fmaf_rn(beta, p.y, g.y), __fmaf_rn(beta, p.z, g.z), 0.f);
+        *reinterpret_cast<float4*>(l) = L;
     }
+    *reinterpret_cast<float4*>(gp + 4) = p;
 }
-// one body: delta-v (6), and dq = delta-v at the sweep's start (6), then q (6)
+// one body: delta-v (6 floats, 8-byte aligned), and dq (12 floats, 16-byte
+// aligned): delta-v at the sweep's start, then q
 __device__ __forceinline__ void nncg_body(float* dv, float* dq, int it, float beta) {
-    for (int k = 0; k < 6; k++) {
-        const float d = __fsub_rn(dv[k], dq[k]);
-        float v = dv[k], q = dq[6 + k];
-        if (it == 0) {
-            q = d;
-        } else if (beta < 0.f) {
-            q = 0.f;
-        } else {
-            v = __fmaf_rn(beta, q, v);
-            q = __fmaf_rn(beta, q, d);
-        }
-        dv[k] = v;
-        dq[k] = v;
-        dq[6 + k] = q;
+    float v[6], d0[6], q[6];
+    const float2* v2 = reinterpret_cast<const float2*>(dv);
+    const float4* q4 = reinterpret_cast<const float4*>(dq);
+#pragma unroll
+    for (int k = 0; k < 3; k++) { const float2 a = v2[k]; v[2 * k] = a.x; v[2 * k + 1] = a.y; }
+    {
+        const float4 a = q4[0], b = q4[1], c = q4[2];
+        d0[0] = a.x; d0[1] = a.y; d0[2] = a.z; d0[3] = a.w;
+        d0[4] = b.x; d0[5] = b.y; q[0] = b.z; q[1] = b.w;
+        q[2] = c.x; q[3] = c.y; q[4] = c.z; q[5] = c.w;
     }
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const float d = __fsub_rn(v[k], d0[k]);
+        if (it == 0) {
+            q[k] = d;
+        } else if (beta < 0.f) {
+            q[k] = 0.f;
+        } else {
+            v[k] = __fmaf_rn(beta, q[k], v[k]);
+            q[k] = __fmaf_rn(beta, q[k], d);
+        }
+    }
+    float2* w2 = reinterpret_cast<float2*>(dv);
+    float4* w4 = reinterpret_cast<float4*>(dq);
+#pragma unroll
+    for (int k = 0; k < 3; k++) w2[k] = make_float2(v[2 * k], v[2 * k + 1]);
+    w4[0] = make_float4(v[0], v[1], v[2], v[3]);
+    w4[1] = make_float4(v[4], v[5], q[0], q[1]);
+    w4[2] = make_float4(q[2], q[3], q[4], q[5]);
 }
 
 // shared-memory layout of the sweep kernel (floats).  The staging arrays
@@ -771,7 +821,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     __shared__ unsigned long long s_tot[2][NNCG_SCALES];
     float* sgp = sm + L.gp;
     float* dqB = resident ? sm + L.dq : dqG + 12 * (size_t)b0;
-    unsigned long long acc[NNCG_SCALES] = {0ull, 0ull, 0ull, 0ull};
+    Acc4 acc;
     int e0 = 0, par = 0;
 
     // issue the asynchronous copy of groups [k0, k1) (and their slots) into
@@ -1207,7 +1257,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
     // |g|^2 totals of this CTA's groups by sweep parity, and the cluster's
     // totals gathered from every CTA
     __shared__ unsigned long long s_tot[2][NNCG_SCALES], s_all[8 * NNCG_SCALES];
-    unsigned long long acc[NNCG_SCALES] = {0ull, 0ull, 0ull, 0ull};
+    Acc4 acc;
     int e0 = 0, par = 0;
     float rmax = 0.f, lmax = 0.f;
     auto group = [&](int op, int col, int kk) {
@@ -1298,6 +1348,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
             if (t < K * NNCG_SCALES) s_all[t] = dsm_ld_u64(dsm_map(&s_tot[par][t % NNCG_SCALES], t / NNCG_SCALES));
             __syncthreads();
             unsigned long long tot[NNCG_SCALES];
+#pragma unroll
             for (int j = 0; j < NNCG_SCALES; j++) {
                 tot[j] = 0ull;
                 for (int r = 0; r < K; r++) tot[j] += s_all[r * NNCG_SCALES + j];
@@ -1443,8 +1494,8 @@ int Ctx::batchSplit(int cap, bool useCluster) {
             // step (cost at least 3/4 of the largest) holds at most 640
             // records per CTA: a sweep takes less time the fewer records each
             // CTA holds, and these scenes bound the whole solve.
-            const bool critical = costTop > 0 && costOf(sc) * 4 >= costTop * 3;
-            const int capK = critical ? std::min(clusterCap, 640) : clusterCap;
+            const bool critical = costTop > 0 && (double)costOf(sc) >= batchCriticalFrac * (double)costTop;
+            const int capK = critical ? std::min(clusterCap, batchCriticalCap) : clusterCap;
             for (int q = 0; q < 3; q++) {
                 int K = CLUSTER_K[q];
                 int per = ((slots + K - 1) / K + sz[sc].y + 31) & ~31;

@@ -252,6 +252,14 @@ int32_t am_set_batch_relaxation(void* ctx, double relax, int32_t symmetric) {
     return AM_OK;
 }
 
+int32_t am_set_batch_critical(void* ctx, double frac, int32_t cap) {
+    if (!ctx || !(frac >= 0.0 && frac <= 1.0) || cap < 64 || cap % 32) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    c->batchCriticalFrac = frac;
+    c->batchCriticalCap = cap;
+    return AM_OK;
+}
+
 int32_t am_set_batch_accel(void* ctx, int32_t mode) {
     if (!ctx || mode < 0 || mode > 1) return AM_E_ARG;
     Ctx* c = (Ctx*)ctx;
@@ -517,6 +525,72 @@ int32_t am_check_barrier_timeout(void* ctx, int32_t spin_log2, int32_t* status) 
     cudaMemcpyAsync(&c->dc->error, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return AM_E_CUDA;
     *status = e;
+    return AM_OK;
+}
+
+static int merging_ctx(Ctx* c) {
+    if (!c->stream || !c->host.cap) { c->err = "no scene loaded"; return AM_E_STATE; }
+    if (c->nScenes > 0 || !c->host.anyMerging()) {
+        c->err = "phase calls of the merging step need a single scene with merging on";
+        return AM_E_STATE;
+    }
+    return AM_OK;
+}
+
+int32_t am_step_phase(void* ctx, int32_t phase, double dt) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    int r = merging_ctx(c);
+    if (r) return r;
+    if (phase < AM_MPHASE_COLLIDE || phase > AM_MPHASE_FINISH) { c->err = "unknown step phase"; return AM_E_ARG; }
+    if (phase == AM_MPHASE_COLLIDE) {
+        c->totalSteps++;
+        for (double& v : c->phase) v = 0.;
+    }
+    r = c->mergingPhase(phase, dt);
+    return r ? r : c->syncErr();
+}
+
+int32_t am_single_sweep_order(void* ctx, int32_t* refs, int32_t capacity, int32_t* n) {
+    if (!ctx || !n || capacity < 0) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    int r = merging_ctx(c);
+    if (r) return r;
+    std::vector<int> v;
+    if (c->P.update_contacts_in_collections && c->anyCollection() && (r = c->singleSweepOrder(v))) return r;
+    *n = (int32_t)v.size();
+    if (capacity < (int32_t)v.size()) return AM_E_CAPACITY;
+    if (!v.empty() && !refs) return AM_E_ARG;
+    for (size_t i = 0; i < v.size(); i++) refs[i] = v[i];
+    return AM_OK;
+}
+
+int32_t am_single_sweep(void* ctx, const int32_t* refs, int32_t n, double dt) {
+    if (!ctx || n < 0 || (n > 0 && !refs)) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    int r = merging_ctx(c);
+    if (r) return r;
+    std::vector<int> v(refs, refs + n);
+    return c->singleSweepRefs(v, dt);
+}
+
+int32_t am_merge_tests(void* ctx, am_bpc_tests* out, int32_t capacity, int32_t* n) {
+    if (!ctx || !n || capacity < 0) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    std::vector<int> a, b, k, res;
+    std::vector<double> m;
+    int r = c->mergeTests(a, b, k, res, m);
+    if (r) return r;
+    *n = (int32_t)a.size();
+    if (capacity < (int32_t)a.size()) return AM_E_CAPACITY;
+    if (!out) return a.empty() ? AM_OK : AM_E_ARG;
+    for (size_t i = 0; i < a.size(); i++) {
+        if (out->body1) out->body1[i] = a[i];
+        if (out->body2) out->body2[i] = b[i];
+        if (out->kind) out->kind[i] = k[i];
+        if (out->result) out->result[i] = res[i];
+        if (out->metric) out->metric[i] = m[i];
+    }
     return AM_OK;
 }
 

@@ -278,6 +278,8 @@ struct Ctx {
     double batchRelax = 1.0;     // over-relaxation of the batched sweep (1: plain projected Gauss-Seidel)
     int batchSym = 0;            // 1: odd sweeps walk the colours backwards
     int batchAccel = 0;          // 1: nonsmooth nonlinear conjugate gradient around each sweep
+    double batchCriticalFrac = 0.75;   // scenes within this fraction of the costliest solve are critical
+    int batchCriticalCap = 640;        // records per CTA of a critical scene's cluster
     float* bGP = nullptr;        // per slot: g and p of the conjugate-gradient step (streamed scenes)
     float* bDQ = nullptr;        // per body: delta-v at sweep start and q (streamed scenes)
     // scenes larger than one CTA's shared memory: thread-block clusters
@@ -429,6 +431,12 @@ struct Ctx {
     int batchAutotune(double dt);
     int batchColours(int* out);
     int getState(std::vector<uint8_t>& out);
+    int mergeTests(std::vector<int>& a, std::vector<int>& b, std::vector<int>& kind, std::vector<int>& result,
+                   std::vector<double>& metric);
+    int mergingPhase(int ph, double dt);
+    int singleSweepOrder(std::vector<int>& refs);
+    int singleSweepRefs(const std::vector<int>& refs, double dt);
+    bool anyCollection() const;
     int putState(const uint8_t* in, size_t size);
     int batchChain(int* out);
     int* bChain = nullptr;

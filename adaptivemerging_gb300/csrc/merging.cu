@@ -383,11 +383,18 @@ void Ctx::nextLayer(std::vector<int>& layer, std::vector<int>& ordered) {
     }
 }
 
-int Ctx::singleSweep(double dt) {
-    if (!P.update_contacts_in_collections) return AM_OK;
-    bool has = false;
-    for (int b : host.top) if (host.flags[b] & F_COLLECTION) has = true;
-    if (!has) return AM_OK;
+// CollisionProcessor.getOrganizedContacts (:337-364) with getNextLayer: the
+// pairs touching a fresh contact first, then breadth-first layers of their
+// neighbours, then the remaining pairs of the collision list and of awake
+// collections; the contacts of each pair in list order.  refs >= 0 index the
+// current contact list, refs < 0 are ~slot of a contact inside a collection.
+int Ctx::singleSweepOrder(std::vector<int>& refs) {
+    refs.clear();
+    // the same flags updateBodyPairContacts clears, so the order can be asked for again
+    for (int p : M.coll.v) M.bpc[p].checked = false;
+    for (int b : host.top)
+        if (host.flags[b] & F_COLLECTION)
+            for (int p : M.bodyBpcs[b].v) M.bpc[p].checked = false;
     // fresh flags of this step's contacts (set by the warm start)
     freshH.resize(nContacts);
     if (nContacts) {
@@ -411,14 +418,29 @@ int Ctx::singleSweep(double dt) {
             for (int p : M.bodyBpcs[b].v)
                 if (!M.bpc[p].checked) { ordered.push_back(p); M.bpc[p].checked = true; }
     phaseAdd(AM_PHASE_CONTACT_ORDERING, tOrder);
+    for (int p : ordered)
+        for (int ref : M.bpc[p].list) refs.push_back(ref);
+    return AM_OK;
+}
+
+// The single sweep of CollisionProcessor.updateInCollections (:262-302) over
+// `refs` in the given order: Jacobians of contacts on collection members
+// recomputed, b and D in collection mode, Gauss-Seidel in list order
+// (iterations_in_collection passes), results scattered back; then the
+// collections' sub-body velocities (RigidCollection.java:866-937).
+int Ctx::singleSweepRefs(const std::vector<int>& refs, double dt) {
     std::vector<int> ext, extPos, in, inPos;
     int n = 0;
-    for (int p : ordered)
-        for (int ref : M.bpc[p].list) {
-            if (ref >= 0) { ext.push_back(ref); extPos.push_back(n); }
-            else { in.push_back(~ref); inPos.push_back(n); }
-            n++;
+    for (int ref : refs) {
+        if (ref >= 0) {
+            if (ref >= nContacts) { err = "single sweep: contact index out of range"; return AM_E_ARG; }
+            ext.push_back(ref); extPos.push_back(n);
+        } else {
+            if (~ref >= M.nSlots) { err = "single sweep: collection contact slot out of range"; return AM_E_ARG; }
+            in.push_back(~ref); inPos.push_back(n);
         }
+        n++;
+    }
     int r = ensureSweep(n);
     if (r) return r;
     if ((r = copyContacts(C[cur], ext, Sw, extPos, 0))) return r;
@@ -435,6 +457,18 @@ int Ctx::singleSweep(double dt) {
     }
     launch_sub_adv_vel(B, top, ntop, subOff, subIds, dt, stream);
     return syncErr();
+}
+
+bool Ctx::anyCollection() const {
+    for (int b : host.top) if (host.flags[b] & F_COLLECTION) return true;
+    return false;
+}
+
+int Ctx::singleSweep(double dt) {
+    if (!P.update_contacts_in_collections || !anyCollection()) return AM_OK;
+    std::vector<int> refs;
+    int r = singleSweepOrder(refs);
+    return r ? r : singleSweepRefs(refs, dt);
 }
 
 // ---- motion metrics on the device ------------------------------------------
@@ -858,6 +892,50 @@ bool Ctx::checkMergeCondition(int p) {             // BodyPairContact.java:151-2
     return true;
 }
 
+// The merge and unmerge predicates on the current state, read only: the
+// pairs of the collision list in Merging.merge's order with
+// checkMergeCondition (BodyPairContact.java:151-177), then the pairs inside
+// every awake collection in Merging.unmerge's order with its selection test
+// (checkContactsState or the relative-motion history, Merging.java:222-240).
+// Sleeping bits are read from the device first (the step's sleep phase sets
+// them there).
+int Ctx::mergeTests(std::vector<int>& a, std::vector<int>& b, std::vector<int>& kind, std::vector<int>& result,
+                    std::vector<double>& metric) {
+    a.clear(); b.clear(); kind.clear(); result.clear(); metric.clear();
+    if (!host.cap) { err = "no scene loaded"; return AM_E_STATE; }
+    if (nScenes > 0) { err = "merging is not part of the batched step"; return AM_E_STATE; }
+    cudaMemcpyAsync(host.flags.data(), B.flags, sizeof(int) * host.cap, cudaMemcpyDeviceToHost, stream);
+    int r = pullStates(true);
+    if (r) return r;
+    auto put = [&](const HBPC& q, int k, bool res) {
+        a.push_back(q.a);
+        b.push_back(q.b);
+        kind.push_back(k);
+        result.push_back(res ? 1 : 0);
+        metric.push_back(q.mm.empty() ? 0.0 : q.mm.back());
+    };
+    for (int p : M.coll.v) {
+        if (M.bpc[p].inCollection) continue;
+        put(M.bpc[p], 0, checkMergeCondition(p));
+    }
+    for (int t : host.top) {
+        if (sleeping(host, t) || !(host.flags[t] & F_COLLECTION)) continue;
+        for (int p : M.bodyBpcs[t].v) {
+            const HBPC& q = M.bpc[p];
+            if (!q.inCollection) continue;
+            bool sel = false;
+            for (int ref : q.list) {
+                int st = ref >= 0 ? stateH[ref] : istateH[~ref];
+                if ((st == AM_STATE_BROKEN && P.enable_unmerge_normal) ||
+                    (st == AM_STATE_ONEDGE && P.enable_unmerge_friction)) { sel = true; break; }
+            }
+            if (!sel) sel = (int)q.mm.size() >= P.step_accum_unmerging && q.list.size() < 3;
+            put(q, 1, sel);
+        }
+    }
+    return AM_OK;
+}
+
 int Ctx::merge() {
     if (!P.enable_merging) return AM_OK;
     // condition inputs: violations of every contact the external pairs refer to
@@ -1167,57 +1245,84 @@ int Ctx::flushAppendedPairs() {
 
 // ---------------------------------------------------------------------------
 // RigidBodySystem.advanceTime with merging (RigidBodySystem.java:102-185)
-int Ctx::stepWithMerging(double dt) {
-    int r;
-    appended = 0;
-    if ((r = beginStep(0))) return r;
-    double t = phaseNow();
-    if ((r = collisionDetection())) return r;
-    phaseAdd(AM_PHASE_DETECTION, t);
-    if ((r = updateBodyPairContacts())) return r;
-    t = phaseNow();
-    if ((r = warmStart())) return r;
-    phaseAdd(AM_PHASE_WARMSTART, t);
-    if ((r = wake())) return r;
-    cudaMemcpyAsync(host.flags.data(), B.flags, sizeof(int) * host.cap, cudaMemcpyDeviceToHost, stream);
-    if ((r = syncErr())) return r;
-    t = phaseNow();
-    if ((r = singleSweep(dt))) return r;
-    phaseAdd(AM_PHASE_UPDATE_COLLECTIONS, t);
-    t = phaseNow();
-    if ((r = accumulateForUnmerging())) return r;
-    if ((r = unmerge())) return r;
-    if (appended) {   // contacts handed back by unmerge join the full solve (lambda = lambdaXwarm)
-        nContacts += appended;
+// RigidBodySystem.advanceTime with merging (RigidBodySystem.java:102-185), one
+// phase at a time (the phases of am_step_phase, AM_MPHASE_*)
+int Ctx::mergingPhase(int ph, double dt) {
+    int r = AM_OK;
+    double t;
+    switch (ph) {
+    case AM_MPHASE_COLLIDE:   // forces, updateContactsMap, collisionDetection, updateBodyPairContacts (:110-124)
         appended = 0;
-        if ((r = flushAppendedPairs())) return r;
+        if ((r = beginStep(0))) return r;
+        t = phaseNow();
+        if ((r = collisionDetection())) return r;
+        phaseAdd(AM_PHASE_DETECTION, t);
+        return updateBodyPairContacts();
+    case AM_MPHASE_WARM_START:   // warmStart, sleeping.wake (:126-132)
+        t = phaseNow();
+        if ((r = warmStart())) return r;
+        phaseAdd(AM_PHASE_WARMSTART, t);
+        if ((r = wake())) return r;
+        cudaMemcpyAsync(host.flags.data(), B.flags, sizeof(int) * host.cap, cudaMemcpyDeviceToHost, stream);
+        return syncErr();
+    case AM_MPHASE_SINGLE_SWEEP:   // updateInCollections (:135)
+        t = phaseNow();
+        r = singleSweep(dt);
+        phaseAdd(AM_PHASE_UPDATE_COLLECTIONS, t);
+        return r;
+    case AM_MPHASE_UNMERGE:   // accumulateForUnmerging, merging.unmerge, forces again (:138-147)
+        t = phaseNow();
+        if ((r = accumulateForUnmerging())) return r;
+        if ((r = unmerge())) return r;
+        if (appended) {   // contacts handed back by unmerge join the full solve (lambda = lambdaXwarm)
+            nContacts += appended;
+            appended = 0;
+            if ((r = flushAppendedPairs())) return r;
+        }
+        if (mergingEvent && (r = beginStep(1))) return r;
+        phaseAdd(AM_PHASE_UNMERGING, t);
+        return AM_OK;
+    case AM_MPHASE_SOLVE:   // redoWarmStart, solveLCP, clearBodyPairContacts (:150-157)
+        if (nContacts > 0) {
+            k_solve_bodies<<<(nContacts + 127) / 128, 128, 0, stream>>>(B, C[cur], nContacts);
+            k_recompute_J<<<(nContacts + 127) / 128, 128, 0, stream>>>(B, C[cur], nContacts, 0);
+            AM_LAUNCHED(2);
+        }
+        t = phaseNow();
+        if ((r = solveLCP(dt, P.warm_start != 0))) return r;
+        phaseAdd(AM_PHASE_LCP_SOLVE, t);
+        return clearBodyPairContacts();
+    case AM_MPHASE_ADVANCE:   // advanceBodiesVelocities, accumulateForMerging, advanceBodiesPositions (:160-166)
+        advVel(dt);
+        t = phaseNow();
+        if ((r = accumulateForMerging())) return r;
+        phaseAdd(AM_PHASE_MERGING, t);
+        advPos(dt);
+        return AM_OK;
+    case AM_MPHASE_MERGE:   // merging.merge every stepsBetweenMergeEvents steps (:171-173)
+        t = phaseNow();
+        if ((totalSteps % P.steps_between_merge_events) == 0)
+            if ((r = merge())) return r;
+        phaseAdd(AM_PHASE_MERGING, t);
+        return AM_OK;
+    case AM_MPHASE_FINISH:   // sleeping.sleep (:176), counters
+        if ((r = uploadExternalFlags())) return r;
+        if ((r = sleepDecay())) return r;
+        if ((r = readCounts())) return r;
+        foldTiming();
+        perf.steps++;
+        return collectStats();
     }
-    if (mergingEvent && (r = beginStep(1))) return r;
-    phaseAdd(AM_PHASE_UNMERGING, t);
-    if (nContacts > 0) {
-        k_solve_bodies<<<(nContacts + 127) / 128, 128, 0, stream>>>(B, C[cur], nContacts);
-        k_recompute_J<<<(nContacts + 127) / 128, 128, 0, stream>>>(B, C[cur], nContacts, 0);
-        AM_LAUNCHED(2);
+    err = "unknown step phase";
+    return AM_E_ARG;
+}
+
+int Ctx::stepWithMerging(double dt) {
+    for (int ph = AM_MPHASE_COLLIDE; ph <= AM_MPHASE_FINISH; ph++) {
+        int r = mergingPhase(ph, dt);
+        if (r) return r;
     }
-    t = phaseNow();
-    if ((r = solveLCP(dt, P.warm_start != 0))) return r;
-    phaseAdd(AM_PHASE_LCP_SOLVE, t);
-    if ((r = clearBodyPairContacts())) return r;
-    advVel(dt);
-    t = phaseNow();
-    if ((r = accumulateForMerging())) return r;
-    phaseAdd(AM_PHASE_MERGING, t);
-    advPos(dt);
-    t = phaseNow();
-    if ((totalSteps % P.steps_between_merge_events) == 0)
-        if ((r = merge())) return r;
-    phaseAdd(AM_PHASE_MERGING, t);
-    if ((r = uploadExternalFlags())) return r;
-    if ((r = sleepDecay())) return r;
-    if ((r = readCounts())) return r;
-    foldTiming();
-    perf.steps++;
-    return collectStats();
+    return AM_OK;
 }
 
 // top-level list: a body is [id], a collection is [-1, members...]

@@ -19,8 +19,8 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libam.so")
 EXPORTS = [
     "am_params_default", "am_create", "am_destroy", "am_last_error", "am_set_params", "am_set_scene",
     "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
-    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_get_step_phases", "am_get_state", "am_put_state", "am_check_barrier_timeout", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats", "am_get_batch_scene_times", "am_get_batch_scene_ctas", "am_get_batch_scene_chain", "am_set_residual_target",
-    "am_set_batch_local_sweeps", "am_set_batch_accel", "am_set_batch_clusters", "am_set_batch_stage", "am_set_batch_relaxation",
+    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_get_step_phases", "am_get_state", "am_put_state", "am_merge_tests", "am_step_phase", "am_single_sweep_order", "am_single_sweep", "am_check_barrier_timeout", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats", "am_get_batch_scene_times", "am_get_batch_scene_ctas", "am_get_batch_scene_chain", "am_set_residual_target",
+    "am_set_batch_local_sweeps", "am_set_batch_accel", "am_set_batch_critical", "am_set_batch_clusters", "am_set_batch_stage", "am_set_batch_relaxation",
     "am_set_batch_cluster_stage", "am_set_batch_size_classes", "am_set_phase_timing", "am_get_phase_times",
     "am_learned_collect", "am_learned_train", "am_learned_use", "am_learned_scope", "am_learned_weights", "am_learned_info",
     "am_learned_grad", "am_learned_infer", "am_learned_infer_noalloc",
@@ -73,6 +73,7 @@ def lib():
         L.am_set_residual_target.argtypes = [vp, C.c_double, C.c_int32]
         L.am_set_batch_local_sweeps.argtypes = [vp, C.c_int32]
         L.am_set_batch_accel.argtypes = [vp, C.c_int32]
+        L.am_set_batch_critical.argtypes = [vp, C.c_double, C.c_int32]
         L.am_set_batch_clusters.argtypes = [vp, C.c_int32]
         L.am_set_batch_size_classes.argtypes = [vp, C.c_int32]
         L.am_set_batch_stage.argtypes = [vp, C.c_int32]
@@ -96,6 +97,10 @@ def lib():
         L.am_get_step_phases.argtypes = [vp, C.POINTER(C.c_double)]
         L.am_get_state.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
         L.am_put_state.argtypes = [vp, vp, C.c_int64]
+        L.am_merge_tests.argtypes = [vp, C.POINTER(abi.am_bpc_tests), C.c_int32, C.POINTER(C.c_int32)]
+        L.am_step_phase.argtypes = [vp, C.c_int32, C.c_double]
+        L.am_single_sweep_order.argtypes = [vp, ip, C.c_int32, ip]
+        L.am_single_sweep.argtypes = [vp, ip, C.c_int32, C.c_double]
         L.am_check_barrier_timeout.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
         for f in EXPORTS:
             if f not in ("am_params_default", "am_last_error"):
@@ -145,6 +150,10 @@ class BatchSystem:
     def set_accel(self, mode=1):
         """1: conjugate-gradient (NNCG) acceleration of the batched sweep; 0: plain PGS."""
         self._check(lib().am_set_batch_accel(self.h, int(mode)))
+
+    def set_critical(self, frac=0.75, cap=640):
+        """Scenes within `frac` of the costliest solve get clusters of at most `cap` records per CTA."""
+        self._check(lib().am_set_batch_critical(self.h, frac, cap))
 
     def set_local_sweeps(self, passes):
         self._check(lib().am_set_batch_local_sweeps(self.h, passes))
@@ -315,6 +324,41 @@ class System:
         self._check(lib().am_get_step_phases(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
         return dict(zip(abi.STEP_PHASES, out.tolist()))
 
+    def step_phase(self, phase, dt):
+        """One phase of the merging step (abi.MPHASES); phases 0..7 in order make one step."""
+        self._check(lib().am_step_phase(self.h, int(phase), dt))
+
+    def single_sweep_order(self):
+        n = C.c_int32(0)
+        r = lib().am_single_sweep_order(self.h, None, 0, C.byref(n))
+        if r not in (0, -2):
+            self._check(r)
+        out = np.zeros(max(1, n.value), np.int32)
+        self._check(lib().am_single_sweep_order(self.h, out.ctypes.data_as(C.POINTER(C.c_int32)), len(out),
+                                                C.byref(n)))
+        return out[:n.value]
+
+    def single_sweep(self, refs, dt):
+        refs = np.ascontiguousarray(refs, np.int32)
+        self._check(lib().am_single_sweep(self.h, refs.ctypes.data_as(C.POINTER(C.c_int32)), len(refs), dt))
+
+    def merge_tests(self):
+        """Merge / unmerge predicates on the current state (am_merge_tests):
+        dict of arrays body1, body2, kind, result, metric."""
+        n = C.c_int32(0)
+        r = lib().am_merge_tests(self.h, None, 0, C.byref(n))
+        if r not in (0, -2):
+            self._check(r)
+        m = max(1, n.value)
+        arr = {k: np.zeros(m, np.int32) for k in ("body1", "body2", "kind", "result")}
+        arr["metric"] = np.zeros(m)
+        s = abi.am_bpc_tests()
+        for k in ("body1", "body2", "kind", "result"):
+            setattr(s, k, arr[k].ctypes.data_as(C.POINTER(C.c_int32)))
+        s.metric = arr["metric"].ctypes.data_as(C.POINTER(C.c_double))
+        self._check(lib().am_merge_tests(self.h, C.byref(s), m, C.byref(n)))
+        return {k: v[:n.value] for k, v in arr.items()}
+
     def get_state(self):
         """Snapshot of the simulation state (bytes) for put_state."""
         n = C.c_int64(0)
@@ -384,7 +428,8 @@ class System:
 
 
 for _name in ("_check", "close", "__del__", "step", "advance_time", "stats", "num_contacts", "contacts", "bodies",
-              "perf", "reset_perf", "set_phase_timing", "phase_times", "step_phases", "get_state", "put_state", "stream_handle", "set_params", "topology",
+              "perf", "reset_perf", "set_phase_timing", "phase_times", "step_phases", "get_state", "put_state", "merge_tests",
+              "step_phase", "single_sweep_order", "single_sweep", "stream_handle", "set_params", "topology",
               "put_bodies_struct",
               "get_bodies_struct", "collision_detection", "warm_start", "solve_lcp", "integrate"):
     setattr(BatchSystem, _name, getattr(System, _name))

@@ -208,6 +208,63 @@ int32_t am_solve(void* ctx, double dt, am_solve_stats* stats);
 int32_t am_integrate(void* ctx, double dt);
 
 /*
+ * The step with merging on, one phase at a time, so a host can keep its own
+ * orchestration between them (read am_merge_tests before the merge phase,
+ * run the single sweep in its own contact order).  Calling the phases 0..7 in
+ * order is am_step.  Phases follow RigidBodySystem.advanceTime
+ * (RigidBodySystem.java:102-185); AM_E_STATE on a batched context or with
+ * merging off (am_collide / am_warm_start / am_solve / am_integrate cover
+ * that step).
+ */
+enum {
+    AM_MPHASE_COLLIDE = 0,      /* forces, updateContactsMap, collisionDetection, updateBodyPairContacts (:110-124); counts the step */
+    AM_MPHASE_WARM_START = 1,   /* warmStart(false), sleeping.wake (:126-132) */
+    AM_MPHASE_SINGLE_SWEEP = 2, /* updateInCollections (:135) in the reference's contact order */
+    AM_MPHASE_UNMERGE = 3,      /* accumulateForUnmerging, merging.unmerge, forces again after an event (:138-147) */
+    AM_MPHASE_SOLVE = 4,        /* redoWarmStart, solveLCP, clearBodyPairContacts (:150-157) */
+    AM_MPHASE_ADVANCE = 5,      /* advanceBodiesVelocities, accumulateForMerging, advanceBodiesPositions (:160-166) */
+    AM_MPHASE_MERGE = 6,        /* merging.merge every steps_between_merge_events steps (:171-173) */
+    AM_MPHASE_FINISH = 7        /* sleeping.sleep (:176) and the step's counters */
+};
+int32_t am_step_phase(void* ctx, int32_t phase, double dt);
+/* The contacts the single sweep of this step visits, in the order of
+ * CollisionProcessor.getOrganizedContacts (CollisionProcessor.java:337-364,
+ * breadth-first layers from the pairs with fresh contacts): refs[i] >= 0 is
+ * contact refs[i] of the current list, refs[i] < 0 is the contact inside a
+ * collection at slot ~refs[i].  Valid after AM_MPHASE_WARM_START; AM_E_CAPACITY
+ * with *n set when capacity is too small. */
+int32_t am_single_sweep_order(void* ctx, int32_t* refs, int32_t capacity, int32_t* n);
+/* In place of AM_MPHASE_SINGLE_SWEEP: the single sweep of
+ * CollisionProcessor.updateInCollections (CollisionProcessor.java:262-302,
+ * PGS.java:73-194 with iterations_in_collection passes) over the given
+ * contacts in the given order, then the collections' sub-body velocities.
+ * AM_E_ARG for a reference out of range. */
+int32_t am_single_sweep(void* ctx, const int32_t* refs, int32_t n, double dt);
+
+/*
+ * The merge and unmerge predicates on the state at the end of the last step,
+ * read only (nothing is merged or split): for a host that keeps its own
+ * merging logic and needs the decisions' inputs.  Entries come in the
+ * reference's iteration order: first every body-pair contact of the
+ * collision list that is not inside a collection, with
+ * BodyPairContact.checkMergeCondition (BodyPairContact.java:151-177) in
+ * Merging.merge's walk (Merging.java:80-82, kind 0); then every pair inside
+ * an awake collection, with Merging.unmerge's selection test
+ * (checkContactsState or the relative-motion history, Merging.java:222-240,
+ * BodyPairContact.java:255-266, kind 1).  metric is the newest entry of the
+ * pair's motion-metric history (0 when empty).  AM_E_CAPACITY with *n set
+ * when capacity is too small; AM_E_STATE on a batched context.
+ */
+typedef struct am_bpc_tests {
+    int32_t* body1;   /* [cap] */
+    int32_t* body2;   /* [cap] */
+    int32_t* kind;    /* [cap] 0 merge test, 1 unmerge test */
+    int32_t* result;  /* [cap] 1 when the pair is a candidate */
+    double*  metric;  /* [cap] */
+} am_bpc_tests;
+int32_t am_merge_tests(void* ctx, am_bpc_tests* out, int32_t capacity, int32_t* n);
+
+/*
  * Snapshot and restore between steps.  The reference rebuilds its state from
  * Java objects (RigidBodySystem.reset, RigidBodySystem.java:390-426; the
  * contact pool, ContactPool.java:23-73; body-pair contacts with their
@@ -299,6 +356,12 @@ int32_t am_set_batch_relaxation(void* ctx, double relax, int32_t symmetric);
  * projected Gauss-Seidel, PGS.java:73-194.  Wraps the reference's sweep; no
  * reference counterpart. */
 int32_t am_set_batch_accel(void* ctx, int32_t mode);
+/* the split of a large scene over a cluster: a scene whose last solve cost at
+ * least frac (0..1) of the batch's costliest one is critical, and each CTA of
+ * its cluster holds at most cap records (a multiple of 32, >= 64), so it runs
+ * on more CTAs and finishes sooner.  Default 0.75 and 640.  Results do not
+ * depend on it.  No reference counterpart. */
+int32_t am_set_batch_critical(void* ctx, double frac, int32_t cap);
 /* coloured full solve of a single scene (AM_ORDER_COLOURED): stop once the
  * relative natural-map residual is <= residual_target, tested every
  * check_every sweeps (0 disables; the reference's max-change tolerance still

@@ -141,3 +141,39 @@ int or_top_ids(void* h, int32_t* out, int cap) {
 }
 
 }  // extern "C"
+
+/* The merge and unmerge tests on the current state, in the reference's
+ * iteration order (BodyPairContact.checkMergeCondition, BodyPairContact.java:
+ * 151-177, over CollisionProcessor.bodyPairContacts as Merging.merge walks it,
+ * Merging.java:80-82; then the unmerge selection of Merging.unmerge,
+ * Merging.java:222-240, per awake collection).  kind 0: merge test of a pair
+ * in the collision list, kind 1: unmerge test of a pair inside a collection.
+ * metric: the newest entry of the pair's motion-metric history (0 if empty).
+ * Returns the number of entries (written up to cap). */
+extern "C" int or_merge_tests(void* h, int32_t* body1, int32_t* body2, int32_t* kind, int32_t* result,
+                              double* metric, int cap) {
+    World* w = (World*)h;
+    int n = 0;
+    auto put = [&](BPC* p, int k, bool r) {
+        if (n < cap) {
+            body1[n] = p->body1->id;
+            body2[n] = p->body2->id;
+            kind[n] = k;
+            result[n] = r ? 1 : 0;
+            metric[n] = p->motionMetricHist.empty() ? 0.0 : p->motionMetricHist.back();
+        }
+        n++;
+    };
+    for (BPC* p : w->bodyPairContacts.v) {
+        if (p->inCollection) continue;
+        put(p, 0, w->mergeTest(p));
+    }
+    for (Body* b : w->bodies) {
+        if (b->sleeping || !b->isCollection) continue;
+        for (BPC* p : b->bpcs.v) {
+            if (!p->inCollection) continue;
+            put(p, 1, w->unmergeTest(p));
+        }
+    }
+    return n;
+}

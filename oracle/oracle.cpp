@@ -1449,6 +1449,16 @@ static bool checkMergeCondition(const am_params& P, BPC* p) {   // BodyPairConta
     return true;
 }
 
+bool World::mergeTest(BPC* p) const { return checkMergeCondition(P, p); }
+
+bool World::unmergeTest(BPC* p) const {   // the selection in Merging.unmerge (:222-240)
+    for (Contact* c : p->contactList) {
+        if (c->state == BROKEN && P.enable_unmerge_normal) return true;
+        if (c->state == ONEDGE && P.enable_unmerge_friction) return true;
+    }
+    return (int)p->motionMetricHist.size() >= P.step_accum_unmerging && p->contactList.size() < 3;
+}
+
 static void listRemove(std::vector<Body*>& v, Body* b) {
     for (size_t i = 0; i < v.size(); i++) if (v[i] == b) { v.erase(v.begin() + i); return; }
 }

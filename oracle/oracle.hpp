@@ -227,6 +227,9 @@ struct World {
     void collUnmergeBody(Body* c, Body* b);
     void collApplyVelocitiesTo(Body* c, Body* b);
     void collUpdateBodiesPositions(Body* c);
+    // merge / unmerge predicates of one body-pair contact on the current state
+    bool mergeTest(BPC* p) const;
+    bool unmergeTest(BPC* p) const;
 };
 
 }  // namespace orc

@@ -47,6 +47,9 @@ def lib():
         L.or_topology.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int,
                                   C.POINTER(C.c_int32)]
         L.or_topology.restype = C.c_int
+        ip = C.POINTER(C.c_int32)
+        L.or_merge_tests.argtypes = [C.c_void_p, ip, ip, ip, ip, C.POINTER(C.c_double), C.c_int]
+        L.or_merge_tests.restype = C.c_int
         _lib = L
     return _lib
 
@@ -127,6 +130,18 @@ class Oracle:
         k = lib().or_topology(self.h, items.ctypes.data_as(C.POINTER(C.c_int32)),
                               off.ctypes.data_as(C.POINTER(C.c_int32)), cap, C.byref(nt))
         return decode_topology(items[:k], off[:nt.value + 1])
+
+    def merge_tests(self):
+        """Merge / unmerge predicates on the current state, reference order."""
+        ip = C.POINTER(C.c_int32)
+        for cap in (256, 1 << 20):
+            arr = {k: np.zeros(cap, np.int32) for k in ("body1", "body2", "kind", "result")}
+            arr["metric"] = np.zeros(cap)
+            n = lib().or_merge_tests(self.h, *(arr[k].ctypes.data_as(ip) for k in ("body1", "body2", "kind", "result")),
+                                     arr["metric"].ctypes.data_as(C.POINTER(C.c_double)), cap)
+            if n <= cap:
+                return {k: v[:n].copy() for k, v in arr.items()}
+        raise RuntimeError("too many body-pair contacts")
 
     def top_ids(self):
         buf = np.zeros(self.n * 2 + 16, np.int32)

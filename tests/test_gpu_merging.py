@@ -131,3 +131,78 @@ def test_coloured_converged_with_collections(gpu_lib, name, warm, cap):
     assert o.counters()["sweeps"] < cap and st.sweeps < cap, "not converged"
     assert err <= 1e-6, err
     assert st.residual_rel <= 1e-6
+
+
+@pytest.mark.parametrize("name", ["tower12", "wall_small"])
+def test_merge_tests_match_oracle(gpu_lib, name):
+    """am_merge_tests, the read-only merge / unmerge predicates a host that
+    keeps its own merging logic reads, equal the oracle's after every step:
+    the same pairs in the reference's iteration order, the same outcomes and
+    bit-identical motion metrics; merge tests turn positive in both scenes,
+    unmerge tests in the wall."""
+    from adaptivemerging_gb300 import native
+    make, dt, steps, over = CASES[name]
+    sc = make()
+    P = params(enable_merging=1, **over)
+    g = native.System(sc, P)
+    o = Oracle(sc, P)
+    seen = {0: 0, 1: 0}
+    for s in range(steps):
+        g.step(dt)
+        o.step(dt)
+        tg, to = g.merge_tests(), o.merge_tests()
+        for k in ("body1", "body2", "kind", "result", "metric"):
+            assert np.array_equal(tg[k], to[k]), f"step {s}: {k}"
+        for kind in (0, 1):
+            seen[kind] += int(((tg["kind"] == kind) & (tg["result"] == 1)).sum())
+    print(f"{name}: positive merge tests {seen[0]}, unmerge tests {seen[1]}")
+    assert seen[0] > 0 and (seen[1] > 0 or name != "wall_small")
+
+
+@pytest.mark.parametrize("name", ["tower12", "wall_small"])
+def test_phase_driven_merging_step_matches_oracle(gpu_lib, name):
+    """A host loop drives the merging step phase by phase through the C ABI
+    (am_step_phase), reads the merge / unmerge predicates (am_merge_tests)
+    and the single sweep's contact order (am_single_sweep_order) and runs the
+    single sweep itself with that order (am_single_sweep): topology, contacts,
+    bodies and event counts stay bit-exact to the oracle every step.  The
+    order is honoured: the same step with the order reversed ends elsewhere."""
+    from adaptivemerging_gb300 import abi, native
+    make, dt, steps, over = CASES[name]
+    sc = make()
+    P = params(enable_merging=1, **over)
+    g = native.System(sc, P)
+    h = native.System(sc, P)            # the same steps, until it takes one reversed order
+    o = Oracle(sc, P)
+    swept = 0
+    reversed_checked = False
+    for s in range(steps):
+        for q in ((g, h) if h is not None else (g,)):
+            q.step_phase(abi.MPHASES.index("collide"), dt)
+            q.step_phase(abi.MPHASES.index("warm_start"), dt)
+        refs = g.single_sweep_order()
+        swept += len(refs)
+        g.single_sweep(refs, dt)
+        if h is not None:
+            rev = len(refs) > 4 and not reversed_checked
+            h.single_sweep(refs[::-1] if rev else h.single_sweep_order(), dt)
+        for q in ((g, h) if h is not None else (g,)):
+            for ph in ("unmerge", "solve", "advance", "merge", "finish"):
+                q.step_phase(abi.MPHASES.index(ph), dt)
+        o.step(dt)
+        if h is not None and rev:
+            assert not np.array_equal(h.bodies()["v"], g.bodies()["v"]), "reversed order gave the same state"
+            reversed_checked = True
+            h = None
+        assert g.topology() == o.topology(), f"step {s}: topology"
+        cg, co = g.contacts(), o.contacts()
+        assert len(cg["body1"]) == len(co["body1"]), f"step {s}"
+        msg = compare_contacts(cg, co)
+        assert msg is None, f"step {s}: {msg}"
+        msg = compare_bodies(g.bodies(), o.bodies())
+        assert msg is None, f"step {s}: {msg}"
+        c, pg = o.counters(), g.perf()
+        assert (pg.merge_events, pg.unmerge_events) == (c["merges"], c["unmerges"]), f"step {s}"
+        tg, to = g.merge_tests(), o.merge_tests()
+        assert all(np.array_equal(tg[k], to[k]) for k in tg), f"step {s}: merge tests"
+    assert swept > 0 and reversed_checked and o.counters()["merges"] > 0
