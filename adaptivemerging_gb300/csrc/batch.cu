@@ -37,6 +37,9 @@ namespace am {
 using namespace amd;
 
 static const int REC = 24;      // floats per packed contact record (global memory)
+// a group's compact body id with GL_FIRST set: the group is the first, in
+// colour order, to touch that body
+static const int GL_FIRST = 1 << 30, GL_ID = GL_FIRST - 1;
 static const int RECS = 28;     // shared-memory stride of a staged record: 7 float4 positions, see rec_pos
 static const int MAXCB = 64;    // colours per scene
 static const int MAXCH = 1024;  // staging chunks per scene
@@ -328,6 +331,23 @@ __global__ void k_batch_slots(DContacts C, DPairs P, const int* pairOff, const i
         for (int k = g0 + t; k < kEnd; k += T) {
             int2 l = glid[k];
             glid[k] = make_int2(s_lid[l.x], s_lid[l.y]);
+        }
+        __syncthreads();
+        // the first group (in colour order) that touches each active body
+        // carries GL_FIRST on that body's id: a sweep that walks the colours
+        // in order reaches the body there first
+        const int nbA = s_carry;
+        for (int b = t; b < nbA; b += T) s_lid[b] = 0x7FFFFFFF;
+        __syncthreads();
+        for (int k = g0 + t; k < kEnd; k += T) {
+            int2 l = glid[k];
+            atomicMin(&s_lid[l.x], k);
+            atomicMin(&s_lid[l.y], k);
+        }
+        __syncthreads();
+        for (int k = g0 + t; k < kEnd; k += T) {
+            int2 l = glid[k];
+            glid[k] = make_int2(l.x | (s_lid[l.x] == k ? GL_FIRST : 0), l.y | (s_lid[l.y] == k ? GL_FIRST : 0));
         }
         __syncthreads();
     }
@@ -687,20 +707,10 @@ __device__ __forceinline__ void nncg_slot(float* l, float* gp, int it, float bet
     }
     *reinterpret_cast<float4*>(gp + 4) = p;
 }
-// one body: delta-v (6 floats, 8-byte aligned), and dq (12 floats, 16-byte
-// aligned): delta-v at the sweep's start, then q
-__device__ __forceinline__ void nncg_body(float* dv, float* dq, int it, float beta) {
-    float v[6], d0[6], q[6];
-    const float2* v2 = reinterpret_cast<const float2*>(dv);
-    const float4* q4 = reinterpret_cast<const float4*>(dq);
-#pragma unroll
-    for (int k = 0; k < 3; k++) { const float2 a = v2[k]; v[2 * k] = a.x; v[2 * k + 1] = a.y; }
-    {
-        const float4 a = q4[0], b = q4[1], c = q4[2];
-        d0[0] = a.x; d0[1] = a.y; d0[2] = a.z; d0[3] = a.w;
-        d0[4] = b.x; d0[5] = b.y; q[0] = b.z; q[1] = b.w;
-        q[2] = c.x; q[3] = c.y; q[4] = c.z; q[5] = c.w;
-    }
+// one body's momentum step on delta-v v, delta-v at the sweep's start d0 and
+// q (6 each): q = beta q + (v - d0), v += beta q_old, d0 = v (first
+// iteration: q = v - d0; restart: q = 0)
+__device__ __forceinline__ void nncg_body_core(float* v, float* d0, float* q, int it, float beta) {
 #pragma unroll
     for (int k = 0; k < 6; k++) {
         const float d = __fsub_rn(v[k], d0[k]);
@@ -712,13 +722,43 @@ __device__ __forceinline__ void nncg_body(float* dv, float* dq, int it, float be
             v[k] = __fmaf_rn(beta, q[k], v[k]);
             q[k] = __fmaf_rn(beta, q[k], d);
         }
+        d0[k] = v[k];
     }
+}
+// dq (12 floats, 16-byte aligned): delta-v at the sweep's start, then q
+__device__ __forceinline__ void dq_unpack(float4 a, float4 b, float4 c, float* d0, float* q) {
+    d0[0] = a.x; d0[1] = a.y; d0[2] = a.z; d0[3] = a.w;
+    d0[4] = b.x; d0[5] = b.y; q[0] = b.z; q[1] = b.w;
+    q[2] = c.x; q[3] = c.y; q[4] = c.z; q[5] = c.w;
+}
+// one body in memory: delta-v (6 floats, 8-byte aligned) and dq
+__device__ __forceinline__ void nncg_body(float* dv, float* dq, int it, float beta) {
+    float v[6], d0[6], q[6];
+    const float2* v2 = reinterpret_cast<const float2*>(dv);
+    const float4* q4 = reinterpret_cast<const float4*>(dq);
+#pragma unroll
+    for (int k = 0; k < 3; k++) { const float2 a = v2[k]; v[2 * k] = a.x; v[2 * k + 1] = a.y; }
+    dq_unpack(q4[0], q4[1], q4[2], d0, q);
+    nncg_body_core(v, d0, q, it, beta);
     float2* w2 = reinterpret_cast<float2*>(dv);
     float4* w4 = reinterpret_cast<float4*>(dq);
 #pragma unroll
     for (int k = 0; k < 3; k++) w2[k] = make_float2(v[2 * k], v[2 * k + 1]);
-    w4[0] = make_float4(v[0], v[1], v[2], v[3]);
-    w4[1] = make_float4(v[4], v[5], q[0], q[1]);
+    w4[0] = make_float4(d0[0], d0[1], d0[2], d0[3]);
+    w4[1] = make_float4(d0[4], d0[5], q[0], q[1]);
+    w4[2] = make_float4(q[2], q[3], q[4], q[5]);
+}
+// the same step on a body whose delta-v is in registers (a group's first
+// touch of the body in a sweep) and whose dq is in this CTA's shared memory
+// or in global memory
+__device__ __forceinline__ void nncg_body_reg(float* v, float* dq, int it, float beta) {
+    float d0[6], q[6];
+    const float4* q4 = reinterpret_cast<const float4*>(dq);
+    dq_unpack(q4[0], q4[1], q4[2], d0, q);
+    nncg_body_core(v, d0, q, it, beta);
+    float4* w4 = reinterpret_cast<float4*>(dq);
+    w4[0] = make_float4(d0[0], d0[1], d0[2], d0[3]);
+    w4[1] = make_float4(d0[4], d0[5], q[0], q[1]);
     w4[2] = make_float4(q[2], q[3], q[4], q[5]);
 }
 
@@ -855,7 +895,14 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
     float rmax = 0.f, lmax = 0.f;
     // one group: its two bodies' delta-v in registers across its contacts;
     // sl0 is the group's first slot in the staging buffer, slA in the scene
-    auto group = [&](int op, int sl0, int slA, int cnt, int2 id) {
+    // a momentum step left pending by the previous sweep (pendIt, pendBeta):
+    // applied to each body at its first touch and to each slot before its
+    // update, the same arithmetic as the eager passes
+    bool pend = false;
+    int pendIt = 0;
+    float pendBeta = 0.f;
+    auto group = [&](int op, int sl0, int slA, int cnt, int2 idf) {
+        const int2 id = make_int2(idf.x & GL_ID, idf.y & GL_ID);
         Pair P;
         {   // 8-byte aligned: 6 floats per body from an even offset
             const float2* da = reinterpret_cast<const float2*>(dv + 6 * id.x);
@@ -872,6 +919,11 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         }
         P.ma = mv[id.x];
         P.mb = mv[id.y];
+        const bool lazy = op == OP_SWEEP && pend;
+        if (lazy) {
+            if ((idf.x & GL_FIRST) && P.ma != 0.f) nncg_body_reg(P.a, dqB + 12 * id.x, pendIt, pendBeta);
+            if ((idf.y & GL_FIRST) && P.mb != 0.f) nncg_body_reg(P.b, dqB + 12 * id.y, pendIt, pendBeta);
+        }
         // sweeps may pass over a group's contacts `inner` times: Gauss-Seidel
         // on the body pair's own block before the sweep moves on
         const int reps = op == OP_SWEEP ? inner : 1;
@@ -885,9 +937,10 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
                 warm_contact(P, R, slot, lp);
             } else if (op == OP_SWEEP) {
                 float d[3];
+                float* g = accel ? (resident ? sgp + 8 * lam_pos(slot) : gpG + 8 * ((size_t)slA + j)) : nullptr;
+                if (lazy && rep == 0) nncg_slot(lp, g, pendIt, pendBeta);
                 sweep_contact(P, R, slot, lp, omega, comp, relax, d);
                 if (accel) {
-                    float* g = resident ? sgp + 8 * lam_pos(slot) : gpG + 8 * ((size_t)slA + j);
                     if (rep > 0)
                         for (int q = 0; q < 3; q++) d[q] = __fadd_rn(g[q], d[q]);
                     g[0] = d[0];
@@ -1003,6 +1056,7 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
             sceneFall[s] = 0;
         }
         pass(OP_WARM, false);
+        pend = false;
         float ggPrev = 0.f;
         if (accel) {   // delta-v at the first sweep's start
             for (int b = t; b < nbA; b += T)
@@ -1024,13 +1078,22 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
                 if (t < NNCG_SCALES) s_tot[par ^ 1][t] = 0ull;   // the next sweep's totals
                 e0 = nncg_e0(1, gg);
                 par ^= 1;
-                for (int i = t; i < nslots; i += T) {
-                    float* lp = resident ? slam + 4 * lam_pos(i) : lamS + 4 * ((size_t)slotS0 + i);
-                    float* gp = resident ? sgp + 8 * lam_pos(i) : gpG + 8 * ((size_t)slotS0 + i);
-                    nncg_slot(lp, gp, it, beta);
+                // eager passes where the multipliers are read next (a residual
+                // check, the last sweep) or the colours are walked backwards;
+                // otherwise the next sweep applies the step as it goes
+                const bool eager = sym || done == iters || (check > 0 && done % check == 0);
+                if (eager) {
+                    for (int i = t; i < nslots; i += T) {
+                        float* lp = resident ? slam + 4 * lam_pos(i) : lamS + 4 * ((size_t)slotS0 + i);
+                        float* gp = resident ? sgp + 8 * lam_pos(i) : gpG + 8 * ((size_t)slotS0 + i);
+                        nncg_slot(lp, gp, it, beta);
+                    }
+                    for (int b = t; b < nbA; b += T) nncg_body(dv + 6 * b, dqB + 12 * b, it, beta);
                 }
-                for (int b = t; b < nbA; b += T) nncg_body(dv + 6 * b, dqB + 12 * b, it, beta);
-                __syncthreads();
+                pend = !eager;
+                pendIt = it;
+                pendBeta = beta;
+                __syncthreads();   // also orders the totals' reset before the next sweep adds to them
             }
             // the same check points as the cluster kernel, so a scene stops at
             // the same sweep whichever kernel solves it
@@ -1260,9 +1323,25 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
     Acc4 acc;
     int e0 = 0, par = 0;
     float rmax = 0.f, lmax = 0.f;
+    // a momentum step left pending by the previous sweep, applied as the
+    // one-CTA kernel applies it (each body at its first touch, each slot
+    // before its update); a body's dq lives with its owner CTA
+    bool pend = false;
+    int pendIt = 0;
+    float pendBeta = 0.f;
+    auto dq_remote = [&](float* v, int b) {
+        const unsigned a = dsm_map(dq + 12 * (b / K), b % K);
+        float d0[6], q[6];
+        dq_unpack(dsm_ld4(a), dsm_ld4(a + 16), dsm_ld4(a + 32), d0, q);
+        nncg_body_core(v, d0, q, pendIt, pendBeta);
+        dsm_st4(a, d0[0], d0[1], d0[2], d0[3]);
+        dsm_st4(a + 16, d0[4], d0[5], q[0], q[1]);
+        dsm_st4(a + 32, q[2], q[3], q[4], q[5]);
+    };
     auto group = [&](int op, int col, int kk) {
         int2 gi = sgi[kk];
-        int2 id = sgl[kk];
+        const int2 idf = sgl[kk];
+        const int2 id = make_int2(idf.x & GL_ID, idf.y & GL_ID);
         int sl0 = s_sb[col] + (gi.x - s_gs[col]);
         // each body's delta-v and inverse inertia live with its owner CTA
         unsigned pa = dsm_map(dvOwn + 12 * (id.x / K), id.x % K);
@@ -1278,6 +1357,11 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
         }
         P.ma = mv[id.x];
         P.mb = mv[id.y];
+        const bool lazy = op == OP_SWEEP && pend;
+        if (lazy) {
+            if ((idf.x & GL_FIRST) && P.ma != 0.f) dq_remote(P.a, id.x);
+            if ((idf.y & GL_FIRST) && P.mb != 0.f) dq_remote(P.b, id.y);
+        }
         const int cnt = gi.y;
         const int reps = op == OP_SWEEP ? inner : 1;
         float gsq = 0.f;
@@ -1290,6 +1374,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
                 warm_contact(P, R, slot, lp);
             } else if (op == OP_SWEEP) {
                 float d[3];
+                if (lazy && jj < cnt) nncg_slot(lp, sgp + 8 * lam_pos(slot), pendIt, pendBeta);
                 sweep_contact(P, R, slot, lp, omega, comp, relax, d);
                 if (accel) {
                     float* g = sgp + 8 * lam_pos(slot);
@@ -1359,11 +1444,22 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
             if (t < NNCG_SCALES) s_tot[par ^ 1][t] = 0ull;   // the next sweep's totals
             e0 = nncg_e0(1, gg);
             par ^= 1;
-            for (int i = t; i < s_sb[ncol]; i += T) nncg_slot(slam + 4 * lam_pos(i), sgp + 8 * lam_pos(i), it, beta);
-            for (int i = t; i < own; i += T) nncg_body(dvOwn + 12 * i, dq + 12 * i, it, beta);
-            // delta-v of every CTA updated before the next sweep reads it, and
-            // every CTA done reading the squared changes before they are rewritten
-            cluster_sync_all();
+            // the one-CTA kernel's rule: eager passes where the multipliers are
+            // read next or the colours run backwards, else applied as the next
+            // sweep goes
+            const bool eager = sym || done == iters || (check > 0 && done % check == 0);
+            if (eager) {
+                for (int i = t; i < s_sb[ncol]; i += T)
+                    nncg_slot(slam + 4 * lam_pos(i), sgp + 8 * lam_pos(i), it, beta);
+                for (int i = t; i < own; i += T) nncg_body(dvOwn + 12 * i, dq + 12 * i, it, beta);
+                // delta-v of every CTA updated before anyone reads it again
+                cluster_sync_all();
+            } else {
+                __syncthreads();   // this CTA's totals reset before its next additions
+            }
+            pend = !eager;
+            pendIt = it;
+            pendBeta = beta;
         }
         if (check > 0 && (done % check == 0 || done == iters)) {
             if (t == 0) { s_res = 0; s_lam = 0; }
