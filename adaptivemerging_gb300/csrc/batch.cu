@@ -1058,9 +1058,12 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
         pass(OP_WARM, false);
         pend = false;
         float ggPrev = 0.f;
-        if (accel) {   // delta-v at the first sweep's start
+        if (accel) {   // delta-v at the first sweep's start, q = 0
             for (int b = t; b < nbA; b += T)
-                for (int k = 0; k < 6; k++) dqB[12 * b + k] = dv[6 * b + k];
+                for (int k = 0; k < 6; k++) {
+                    dqB[12 * b + k] = dv[6 * b + k];
+                    dqB[12 * b + 6 + k] = 0.f;
+                }
             if (t < 2 * NNCG_SCALES) s_tot[t / NNCG_SCALES][t % NNCG_SCALES] = 0ull;
             e0 = nncg_e0(0, 0.f);
             __syncthreads();
@@ -1088,7 +1091,9 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
                         float* gp = resident ? sgp + 8 * lam_pos(i) : gpG + 8 * ((size_t)slotS0 + i);
                         nncg_slot(lp, gp, it, beta);
                     }
-                    for (int b = t; b < nbA; b += T) nncg_body(dv + 6 * b, dqB + 12 * b, it, beta);
+                    // pinned bodies keep delta-v 0 (the lazy path skips them too)
+                    for (int b = t; b < nbA; b += T)
+                        if (mv[b] != 0.f) nncg_body(dv + 6 * b, dqB + 12 * b, it, beta);
                 }
                 pend = !eager;
                 pendIt = it;
@@ -1413,7 +1418,10 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
     pass(OP_WARM, false);
     if (accel) {   // delta-v of the owned bodies at the first sweep's start
         for (int i = t; i < own; i += T)
-            for (int k = 0; k < 6; k++) dq[12 * i + k] = dvOwn[12 * i + k];
+            for (int k = 0; k < 6; k++) {
+                dq[12 * i + k] = dvOwn[12 * i + k];
+                dq[12 * i + 6 + k] = 0.f;
+            }
         if (t < 2 * NNCG_SCALES) s_tot[t / NNCG_SCALES][t % NNCG_SCALES] = 0ull;
         e0 = nncg_e0(0, 0.f);
         // every CTA has copied its bodies (and cleared its totals) before any
@@ -1451,7 +1459,11 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
             if (eager) {
                 for (int i = t; i < s_sb[ncol]; i += T)
                     nncg_slot(slam + 4 * lam_pos(i), sgp + 8 * lam_pos(i), it, beta);
-                for (int i = t; i < own; i += T) nncg_body(dvOwn + 12 * i, dq + 12 * i, it, beta);
+                // pinned bodies (and padding) keep delta-v 0, as in the lazy path
+                for (int i = t; i < own; i += T) {
+                    const int lb = i * K + (int)rank;
+                    if (lb < nbA && mv[lb] != 0.f) nncg_body(dvOwn + 12 * i, dq + 12 * i, it, beta);
+                }
                 // delta-v of every CTA updated before anyone reads it again
                 cluster_sync_all();
             } else {

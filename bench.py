@@ -661,17 +661,19 @@ def run_ours(args):
                               "to the step, host waits included")
         sysm.close()
         # the same kernels and scenes, plain projected Gauss-Seidel
-        pg = _batch_system(sc, P, args.threads, 0, args.stage)
-        pstream = torch.cuda.ExternalStream(pg.stream_handle())
-        for _ in range(args.warmup):
-            pg.step(dt)
-        pw = time_batch_window(pg, dt, args.steps, flush, pstream)
-        plain = summarise_window(pw, args.steps, n_units, args.warmup, "the timed steps")
-        plain["pgs"] = "FP32 projected Gauss-Seidel, no acceleration, previous-frame warm start, same kernels"
-        out["plain_gpu_pgs"] = plain
-        out["accelerated_over_plain"] = value / plain["value"]
+        if not args.no_plain:
+            pg = _batch_system(sc, P, args.threads, 0, args.stage)
+            pstream = torch.cuda.ExternalStream(pg.stream_handle())
+            for _ in range(args.warmup):
+                pg.step(dt)
+            pw = time_batch_window(pg, dt, args.steps, flush, pstream)
+            plain = summarise_window(pw, args.steps, n_units, args.warmup, "the timed steps")
+            plain["pgs"] = "FP32 projected Gauss-Seidel, no acceleration, previous-frame warm start, same kernels"
+            out["plain_gpu_pgs"] = plain
+            out["accelerated_over_plain"] = value / plain["value"]
+            pg.close()
         # the steady window (steps 21..60) beside the timed one, both arms
-        if (args.warmup, args.steps) != STEADY and not args.no_steady:
+        if (args.warmup, args.steps) != STEADY and not args.no_steady and not args.no_plain:
             steady = {}
             for name, acc in (("accelerated", 1), ("plain", 0)):
                 g = _batch_system(sc, P, args.threads, acc, args.stage)
@@ -683,7 +685,6 @@ def run_ours(args):
                 g.close()
             steady["accelerated_over_plain"] = steady["accelerated"]["value"] / steady["plain"]["value"]
             out["steady_window"] = steady
-        pg.close()
         if not args.no_plain:
             k1 = min(args.steps, 10)
             one = plain_fp32_one_scene_at_a_time(sc, P, dt, args.warmup, k1, flush)
@@ -711,7 +712,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-plain", action="store_true", help="skip the one-scene-at-a-time comparison arms")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the comparison arms (plain batched PGS, one scene at a time; profiling runs only)")
     ap.add_argument("--no-steady", action="store_true", help="skip the steady-window (steps 21..60) figures")
     ap.add_argument("--learned", action="store_true", help="also run the learned warm-start protocol")
     ap.add_argument("--threads", type=int, default=0, help="batched solve: CTA size (0: autotuned)")

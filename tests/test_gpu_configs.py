@@ -160,17 +160,17 @@ def _oracle_converged(scene, P):
 
 
 def test_config3_cluster_bins_against_oracle(gpu_lib):
-    """With piles formed (step 50), the bins the device solves with clusters:
-    contacts from the device's state are the oracle's bit for bit, and after
-    one step solved to a fixed point on both sides (60000 FP32 sweeps on the
-    device, residual 1e-10 in FP64 on the oracle) the bodies' velocities agree
-    within 1e-4 relative to max(1, |v|).  The multipliers agree within 2e-4
-    on most bins; on bins with many redundant contacts (coplanar box faces)
-    the FP32 fixed point shifts impulse between them, which leaves the
-    velocities in place (one bin sits 1.25e-3 from FP64 from the warm start
-    and 1.5e-5 from a cold start).  The batch itself solves its large bins
-    with clusters of 2 and 4 CTAs; the same bins, loaded from that state into
-    a batch whose CTAs hold at most 320 records, run on clusters of 8."""
+    """With piles formed (step 50) the batch solves its large bins with
+    clusters of 2 and 4 CTAs.  The device state of the largest bins and of
+    bins on each cluster size is handed to the oracle: their contact sets are
+    the oracle's bit for bit.  The same states, loaded into fresh batches whose
+    CTAs hold at most 2048, 640 and 320 records (clusters of 2, 4 and 8 CTAs),
+    are solved from the same cold start as the oracle to a fixed point (60000
+    FP32 sweeps; residual 1e-10 in FP64): multipliers within 2e-4 relative,
+    body velocities within 1e-4.  (Box friction makes the problem non-monotone,
+    so a frictional pile can hold several solutions: from its own warm start
+    the batch settles on another one, converged as tightly; cold start against
+    cold start is the comparison that pins the solver.)"""
     from adaptivemerging_gb300 import native
     sc = scenes.batch_scenes(512, seed=3)
     P = _batch_params(enable_sleeping=0)
@@ -179,14 +179,10 @@ def test_config3_cluster_bins_against_oracle(gpu_lib):
         g.step(BATCH_DT)
     b = g.bodies()
     offs = g.offsets
-    # one step solved to a fixed point from here on both sides
-    Pfix = _batch_params(enable_sleeping=0, iterations=60000)
-    g.set_params(Pfix)
-    g._check(native.lib().am_set_batch_options(g.h, 0, 0.0, 0))
     g.step(BATCH_DT)
     ctas = g.scene_ctas()
     ks = {int(k): int((ctas == k).sum()) for k in np.unique(ctas)}
-    print("CTAs per scene at the fixed-point step:", ks)
+    print("CTAs per scene at step 51:", ks)
     assert ks.get(2, 0) > 0 and ks.get(4, 0) > 0, ks
     parts = _split(g.contacts(), sc)
     nc = np.array([len(p["body1"]) for p in parts])
@@ -198,42 +194,42 @@ def test_config3_cluster_bins_against_oracle(gpu_lib):
     for k in pick:
         lo, hi = offs[k], offs[k + 1]
         inj[k] = _inject(sc[k], b["x"][lo:hi], b["R"][lo:hi], b["v"][lo:hi], b["omega"][lo:hi])
-    # the same states in a batch of small cluster parts: clusters of 8
-    big = [k for k in pick if ctas[k] > 1]
-    h = native.BatchSystem([inj[k] for k in big], Pfix, threads=0, residual_target=0.0, check_every=0,
-                           cluster_stage=320)
-    h.step(BATCH_DT)
-    hct = h.scene_ctas()
-    print("small-part batch CTAs:", dict(zip(big, hct.tolist())))
-    assert (hct == 8).any(), hct
-    hparts = _split(h.contacts(), [inj[k] for k in big])
     Po = _batch_params(enable_sleeping=0, iterations=400000, tolerance=0.0)
     with cf.ThreadPoolExecutor(max_workers=16) as ex:
         jobs = {k: ex.submit(_oracle_converged, inj[k], Po) for k in pick}
-    vb = g.bodies()["v"]
-    hb = h.bodies()["v"]
-    hoffs = np.cumsum([0] + [inj[k].n for k in big])
+    res = {k: jobs[k].result() for k in pick}
+    for k in pick:   # the batch's own contact sets at step 51
+        co = res[k][0]
+        assert len(parts[k]["body1"]) == len(co["body1"]) > 0, f"bin {k}"
+        msg = compare_contacts(parts[k], co, fields=GEOMETRY)
+        assert msg is None, f"bin {k} ({ctas[k]} CTAs): {msg}"
+    big = [k for k in pick if ctas[k] > 1]
+    seen = set()
     errs, verrs = [], []
-    for k in pick:
-        co, sweeps, vo = jobs[k].result()
-        assert sweeps < 400000, f"bin {k}: oracle did not converge"
-        scale = max(1.0, float(np.abs(co["lambda"]).max()))
-        vscale = max(1.0, float(np.abs(vo).max()))
-        cases = [(parts[k], int(ctas[k]), vb[offs[k]:offs[k + 1]])]
-        if k in big:
-            i = big.index(k)
-            cases.append((hparts[i], int(hct[i]), hb[hoffs[i]:hoffs[i + 1]]))
-        for pk, kk, vk in cases:
-            assert len(pk["body1"]) == len(co["body1"]) > 0, f"bin {k}"
+    Pfix = _batch_params(enable_sleeping=0, iterations=60000)
+    for stage in (0, 640, 320):
+        h = native.BatchSystem([inj[k] for k in big], Pfix, threads=0, residual_target=0.0, check_every=0,
+                               cluster_stage=stage)
+        h.step(BATCH_DT)
+        hct = h.scene_ctas()
+        seen.update(int(x) for x in hct)
+        hparts = _split(h.contacts(), [inj[k] for k in big])
+        hb = h.bodies()["v"]
+        hoffs = np.cumsum([0] + [inj[k].n for k in big])
+        for i, k in enumerate(big):
+            co, sweeps, vo = res[k]
+            assert sweeps < 400000, f"bin {k}: oracle did not converge"
+            pk = hparts[i]
             msg = compare_contacts(pk, co, fields=GEOMETRY)
-            assert msg is None, f"bin {k} ({kk} CTAs): {msg}"
+            assert msg is None, f"bin {k} ({hct[i]} CTAs): {msg}"
             assert np.array_equal(pk["violation"][:, 0], co["violation"][:, 0]), f"bin {k}"
-            err = float(np.abs(pk["lambda"] - co["lambda"]).max()) / scale
-            verr = float(np.abs(vk - vo).max()) / vscale
-            print(f"bin {k}: {sc[k].n} bodies, {len(co['body1'])} contacts, {kk} CTAs, oracle sweeps {sweeps}, "
+            err = float(np.abs(pk["lambda"] - co["lambda"]).max()) / max(1.0, float(np.abs(co["lambda"]).max()))
+            verr = float(np.abs(hb[hoffs[i]:hoffs[i + 1]] - vo).max()) / max(1.0, float(np.abs(vo).max()))
+            print(f"bin {k}: {sc[k].n} bodies, {len(co['body1'])} contacts, {hct[i]} CTAs, oracle sweeps {sweeps}, "
                   f"lambda rel err {err:.2e}, velocity rel err {verr:.2e}")
             errs.append(err)
             verrs.append(verr)
-            assert verr <= 1e-4, f"bin {k} ({kk} CTAs): velocity {verr}"
-    print(f"{len(pick)} bins: worst lambda {max(errs):.2e}, worst velocity {max(verrs):.2e}")
-    assert np.mean(np.array(errs) <= 2e-4) >= 0.75, errs
+            assert err <= 2e-4 and verr <= 1e-4, f"bin {k} ({hct[i]} CTAs): {err} {verr}"
+        h.close()
+    print(f"cluster sizes {sorted(seen)}; worst lambda {max(errs):.2e}, worst velocity {max(verrs):.2e}")
+    assert {2, 4, 8} <= seen, seen

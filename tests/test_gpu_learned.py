@@ -125,19 +125,20 @@ def test_training_reduces_loss(gpu_lib):
 
 
 def test_learned_start_meets_residual_target_and_reports_gain(gpu_lib):
-    """Two identical batches step in lockstep; one records and trains, then
-    the other switches to the learned start.  The learned batch must reach the
-    residual target on at least as many scenes as the plain one (a scene whose
-    learned start falls short is solved again from the plain start); the
-    contact-sweeps ratio is the net gain."""
+    """One batch records (features, converged impulse) pairs and trains the
+    network; then, for 40 steps, a second context loads the first one's state
+    before each step (am_put_state) and solves the same step from the learned
+    start.  Both solve identical problems, so the learned start must reach the
+    residual target on at least every scene the plain start does (a scene
+    whose learned start falls short is solved again from the plain start in
+    the same CTA); the contact-sweeps ratio is the learned start's net gain on
+    equal problems."""
     # bodies dropped from a grid: contacts keep appearing while the piles form
     a = _system(n_scenes=16, seed=21, sizes=(100, 400), gap=0.01)
     b = _system(n_scenes=16, seed=21, sizes=(100, 400), gap=0.01)
     a.learned_collect(True, 500_000)
     for _ in range(150):
         a.step(DT)
-        b.step(DT)
-    assert np.array_equal(a.bodies()["x"], b.bodies()["x"]), "batched pipeline must be deterministic"
     n = a.learned_info()["n_samples"]
     assert n >= 256, n
     a.learned_train(epochs=40, batch=min(1024, n // 4), lr=2e-3)
@@ -149,6 +150,7 @@ def test_learned_start_meets_residual_target_and_reports_gain(gpu_lib):
     conv_plain = conv_learned = 0
     falls = 0
     for _ in range(40):
+        b.put_state(a.get_state())
         a.step(DT)
         b.step(DT)
         sa, sb = a.batch_stats(), b.batch_stats()
@@ -158,11 +160,11 @@ def test_learned_start_meets_residual_target_and_reports_gain(gpu_lib):
         conv_learned += sb.converged
         falls += b.learned_info()["fallback_scenes"]
     gain = cs_plain / max(1, cs_learned)
-    print(f"learned start: contact-sweeps plain {cs_plain}, learned {cs_learned} (x{gain:.2f}); "
+    print(f"learned start on equal problems: contact-sweeps plain {cs_plain}, learned {cs_learned} (x{gain:.2f}); "
           f"converged scene-steps plain {conv_plain}, learned {conv_learned} of {40 * 16}; "
           f"fallback scene-steps {falls}")
     assert cs_learned > 0
-    assert conv_learned >= conv_plain - 8   # the trajectories differ within the residual target
+    assert conv_learned >= conv_plain
 
 
 def test_grid_barrier_wait_gives_up(gpu_lib):
