@@ -26,7 +26,7 @@ AM_BV_NULL = -1
 MPHASES = ("collide", "warm_start", "single_sweep", "unmerge", "solve", "advance", "merge", "finish")
 # device phases of a batched step (am_get_step_phases)
 STEP_PHASES = ("detection", "warm_start", "solve_setup", "sweeps", "integration", "statistics")
-AM_ORDER_REFERENCE, AM_ORDER_COLOURED = 0, 1
+AM_ORDER_REFERENCE, AM_ORDER_COLOURED, AM_ORDER_MIXED = 0, 1, 2
 # am_get_phase_times order: the reference's CSV time columns
 # (RigidBodySystem.exportDataToFile, RigidBodySystem.java:495-542)
 PHASES = ("detection", "warmstart", "LCPSolve", "updateCollections", "contactOrdering", "singleItPGS",

@@ -116,7 +116,11 @@ struct DCount {
     int need_pairs;
     int sweeps;
     int error;       // AM_E_* raised on device
-    unsigned long long maxchg[2];  // max |delta lambda| (bits of a non-negative double) per sweep parity
+    // max |delta lambda| of a sweep (bits of a non-negative double), slot sweep % 3: a sweep
+    // clears the next sweep's slot before its own last barrier, after every reader of
+    // that slot's previous use passed the barrier before (with two slots a one-colour
+    // sweep could clear a slot that another block had already written)
+    unsigned long long maxchg[3];
     int n_colours;
     int bar_count;   // grid-barrier arrivals of the running cooperative sweep (counts up)
     double res_abs;  // residual
@@ -163,6 +167,26 @@ void launch_pgs_fast(const DBodies& B, DContacts& C, DPairs& P, const int* group
                      int ncol, int nc, int iters, double omega, double comp, double tol, bool early, int fo,
                      double fv, double slide, double* Mj, double* K, int mcap, DCount* dc, int gridBlocks,
                      cudaStream_t s, double resTol = 0.0, int check = 0);
+// AM_ORDER_MIXED: the coloured solve's sweeps in FP32 on the correction to an
+// FP64 base point, refined in FP64 every `refine` sweeps (and at every
+// residual check); F holds pgs_mixed_frows() floats per contact (mcap
+// contacts), BM 8 floats and U 6 floats per body, GI one int4 per coloured
+// group (ng of them)
+void launch_pgs_mixed(const DBodies& B, DContacts& C, DPairs& P, const int* groupOrder, const int* colourOff,
+                      int ncol, int nc, int iters, double omega, double comp, double tol, bool early, int fo,
+                      double fv, double slide, double* Mj, double* K, float* F, float* BM, float* U, int4* GI,
+                      int ng, int nbodies, int mcap, DCount* dc, int gridBlocks, int mode, cudaStream_t s,
+                      double resTol, int check, int refine);
+int pgs_mixed_frows();
+// blocks of the grid form for a widest colour of `widest` groups
+int pgs_mixed_grid_blocks(int widest, int coopBlocks);
+// the form of the mixed solve for these colours: 0, a cooperative grid of
+// gridBlocks 128-thread blocks; 1, one 256-thread block (block barriers, body
+// data and delta-v corrections in shared memory); 2, one block with the
+// contact records in shared memory too
+int pgs_mixed_mode(const std::vector<int>& colOff, int gridBlocks, int nbodies, int nc);
+// whether form `mode` of the mixed solve fits these sizes (shared memory)
+bool pgs_mixed_fits(int mode, const std::vector<int>& colOff, int nbodies, int nc);
 // rows of the coloured solve's per-contact constant table (1/(D+c), A, q,
 // couplings, friction coefficient), each `mcap` doubles
 int pgs_fast_krows();

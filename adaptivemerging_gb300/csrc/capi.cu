@@ -277,6 +277,20 @@ int32_t am_set_residual_target(void* ctx, double residual_target, int32_t check_
     return AM_OK;
 }
 
+int32_t am_set_mixed_form(void* ctx, int32_t form, int32_t refine) {
+    if (!ctx || form < -1 || form > 2 || refine < 0) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    c->mixedForm = form;
+    c->mixedRefine = refine;
+    return AM_OK;
+}
+
+int32_t am_get_mixed_form(void* ctx, int32_t* form) {
+    if (!ctx || !form) return AM_E_ARG;
+    *form = ((Ctx*)ctx)->mixedLastForm;
+    return AM_OK;
+}
+
 int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, int32_t* fell_back, int32_t* colours) {
     if (!ctx) return AM_E_ARG;
     Ctx* c = (Ctx*)ctx;

@@ -206,6 +206,12 @@ struct Ctx {
     double* Mj = nullptr;     // coloured sweep: M^-1 J^T per row and lane (36 per contact)
     double* invD = nullptr;   // coloured sweep constants per contact: 1/(D + c), A, q per row, couplings, mu
     int mjCap = 0;
+    float* mixF = nullptr;    // AM_ORDER_MIXED: FP32 operands, base constants and corrections (mjCap stride)
+    float* mixU = nullptr;    // AM_ORDER_MIXED: FP32 delta-v corrections, 6 per body
+    int* mixG = nullptr;      // AM_ORDER_MIXED: group records, 4 ints per coloured group
+    int mixFCap = 0, mixUCap = 0, mixGCap = 0;
+    int mixedForm = -1, mixedRefine = 0;   // am_set_mixed_form
+    int mixedLastForm = -1;                // form of the last mixed solve
     int nScene = 0, ntop = 0, nContacts = 0, nPrev = 0, nPairs = 0;
     int totalSteps = 0;
     bool mergingEvent = false;
@@ -485,6 +491,7 @@ int Ctx::alloc(T** p, size_t n) {
 }
 
 const void* pgs_fast_kernel();
+const void* pgs_mixed_kernel();
 const void* gs_levels_kernel();
 const void* batch_sweep_kernel();
 int learned_num_params();

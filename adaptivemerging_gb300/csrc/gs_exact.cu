@@ -96,7 +96,8 @@ __global__ void k_gs_levels(DBodies B, DContacts C, const int* order, const int*
     int iter = iters, done = 0;
     double change = 0;
     while (iter > 0) {
-        const int par = done & 1;
+        const int par = done % 3;
+        if (blockIdx.x == 0 && threadIdx.x == 0) dc->maxchg[(done + 1) % 3] = 0ull;   // the next sweep's slot
         double mx = 0;
         for (int L = 0; L < nLevels; L++) {
             for (int k = levelOff[L] + warp; k < levelOff[L + 1]; k += nwarps) {
@@ -160,7 +161,6 @@ __global__ void k_gs_levels(DBodies B, DContacts C, const int* order, const int*
         iter--;
         done++;
         change = __longlong_as_double((long long)*(volatile unsigned long long*)&dc->maxchg[par]);
-        if (blockIdx.x == 0 && threadIdx.x == 0) dc->maxchg[par ^ 1] = 0ull;
         if (early && change < tol) break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -204,7 +204,7 @@ void launch_gs_levels(const DBodies& B, DContacts& C, const int* order, const in
                       double omega, double comp, double tol, bool early, int fo, double fv, double slide,
                       DCount* dc, int blocks, cudaStream_t s) {
     if (nLevels <= 0) return;
-    cudaMemsetAsync(&dc->maxchg, 0, sizeof(unsigned long long) * 2, s);
+    cudaMemsetAsync(&dc->maxchg, 0, sizeof(dc->maxchg), s);
     cudaMemsetAsync(&dc->bar_count, 0, sizeof(int), s);
     int earlyI = early ? 1 : 0;
     DBodies Bc = B;

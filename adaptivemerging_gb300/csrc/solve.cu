@@ -320,32 +320,41 @@ __device__ void warm_apply(const DBodies& B, const DContacts& C, int c) {
 }
 
 // ---------------------------------------------------------------------------
-// greedy colouring of body-pair groups (independent-set rounds): in round r
-// every uncoloured group whose priority is the largest among the uncoloured
-// groups at each of its dynamic bodies takes colour r.  Groups of one colour
-// never share a dynamic body, so they can update delta-v concurrently.
-__device__ __forceinline__ unsigned long long prio(int g) {
+// colouring of body-pair groups: Jones-Plassmann rounds with first-fit
+// colours.  Each round, every uncoloured group whose priority is the largest
+// among the uncoloured groups at each of its dynamic bodies takes the
+// smallest colour not yet used at either body.  Groups selected in one round
+// share no dynamic body, so the per-body colour masks (maxC bits) need no
+// atomics between them; groups of one colour never share a dynamic body, so
+// they can update delta-v concurrently.  A chain of groups (a stack) takes
+// three colours at most.  Groups with more contacts go first (low colours),
+// ties broken by a hash, made unique by the group index.
+__device__ __forceinline__ unsigned long long prio(const DPairs& P, int g) {
     unsigned h = (unsigned)g * 2654435761u;
     h ^= h >> 16; h *= 0x7feb352du; h ^= h >> 15;
-    return ((unsigned long long)h << 32) | (unsigned)g;
+    unsigned long long cnt = (unsigned long long)min(P.count[g], 255);
+    return (cnt << 56) | ((unsigned long long)(h & 0xFFFFFFu) << 32) | (unsigned)g;
 }
 
 __global__ void k_colour(DBodies B, DContacts C, DPairs P, int npairs, int* colourOf, int* colourCnt, int maxC,
-                         unsigned long long* bodyMax, int nbodies, DCount* dc) {
-    __shared__ int s_left, s_round;
+                         unsigned long long* bodyMax, unsigned long long* used, int nbodies, DCount* dc) {
+    __shared__ int s_left, s_full, s_ncol;
+    const int W = (maxC + 63) / 64;   // 64-bit words of a body's colour mask
     int t = threadIdx.x, T = blockDim.x;
     for (int g = t; g < npairs; g += T) colourOf[g] = (P.count[g] > 0) ? -1 : -2;
-    if (t == 0) s_round = 0;
+    for (int b = t; b < nbodies * W; b += T) used[b] = 0ull;
+    if (t == 0) { s_full = 0; s_ncol = 0; s_left = 1; }
     __syncthreads();
-    for (int round = 0; round < maxC; round++) {
+    const int maxRounds = 1 << 16;
+    for (int round = 0; round < maxRounds; round++) {
         for (int b = t; b < nbodies; b += T) bodyMax[b] = 0ull;
-        if (t == 0) s_left = 0;
         __syncthreads();
+        if (t == 0) s_left = 0;
         for (int g = t; g < npairs; g += T) {
             if (colourOf[g] != -1) continue;
             int c = P.off[g];
             int s1 = C.sb1[c], s2 = C.sb2[c];
-            unsigned long long pr = prio(g);
+            unsigned long long pr = prio(P, g);
             if (!(B.flags[s1] & F_PINNED)) atomicMax(&bodyMax[s1], pr);
             if (!(B.flags[s2] & F_PINNED)) atomicMax(&bodyMax[s2], pr);
         }
@@ -354,20 +363,29 @@ __global__ void k_colour(DBodies B, DContacts C, DPairs P, int npairs, int* colo
             if (colourOf[g] != -1) continue;
             int c = P.off[g];
             int s1 = C.sb1[c], s2 = C.sb2[c];
-            unsigned long long pr = prio(g);
-            bool ok = ((B.flags[s1] & F_PINNED) || bodyMax[s1] == pr) && ((B.flags[s2] & F_PINNED) || bodyMax[s2] == pr);
-            if (ok) { colourOf[g] = round; atomicAdd(&colourCnt[round], 1); }
-            else atomicAdd(&s_left, 1);
+            bool p1 = B.flags[s1] & F_PINNED, p2 = B.flags[s2] & F_PINNED;
+            unsigned long long pr = prio(P, g);
+            if (!((p1 || bodyMax[s1] == pr) && (p2 || bodyMax[s2] == pr))) { atomicAdd(&s_left, 1); continue; }
+            int col = -1;
+            for (int w = 0; w < W && col < 0; w++) {
+                unsigned long long m = (p1 ? 0ull : used[(size_t)s1 * W + w]) | (p2 ? 0ull : used[(size_t)s2 * W + w]);
+                if (m != ~0ull) col = 64 * w + __ffsll((long long)~m) - 1;
+            }
+            if (col < 0 || col >= maxC) { colourOf[g] = -2; s_full = 1; continue; }   // more than maxC colours
+            if (!p1) used[(size_t)s1 * W + col / 64] |= 1ull << (col % 64);
+            if (!p2) used[(size_t)s2 * W + col / 64] |= 1ull << (col % 64);
+            colourOf[g] = col;
+            atomicAdd(&colourCnt[col], 1);
+            atomicMax(&s_ncol, col + 1);
         }
         __syncthreads();
-        if (t == 0) s_round = round + 1;
         int left = s_left;
         __syncthreads();
         if (left == 0) break;
     }
     if (t == 0) {
-        dc->n_colours = s_round;
-        if (s_left != 0) dc->error = AM_E_CAPACITY;
+        dc->n_colours = s_ncol;
+        if (s_left != 0 || s_full) dc->error = AM_E_CAPACITY;
     }
 }
 
@@ -387,7 +405,8 @@ void colour_groups(const DBodies& B, const DContacts& C, DPairs& P, int npairs, 
                    DCount* dc, Scratch& sc, cudaStream_t s) {
     if (npairs <= 0) { cudaMemsetAsync(&dc->n_colours, 0, sizeof(int), s); return; }
     cudaMemsetAsync(colourCnt, 0, sizeof(int) * (maxC + 1), s);
-    k_colour<<<1, 1024, 0, s>>>(B, C, P, npairs, colourOf, colourCnt, maxC, bodyMax, nbodies, dc);
+    k_colour<<<1, 1024, 0, s>>>(B, C, P, npairs, colourOf, colourCnt, maxC, bodyMax, bodyMax + nbodies, nbodies,
+                                dc);
     AM_LAUNCHED(1);
     launch_scan(colourCnt, colourOff, maxC + 1, sc, nullptr, s);
     cudaMemsetAsync(fill, 0, sizeof(int) * maxC, s);

@@ -339,6 +339,9 @@ void Ctx::release() {
     candCap = 0;
     Mj = invD = nullptr;
     mjCap = 0;
+    mixF = mixU = nullptr;
+    mixG = nullptr;
+    mixFCap = mixUCap = mixGCap = 0;
     levOrder = levOff = nullptr;
     levCap = 0;
     idxA = idxB = nullptr;
@@ -465,7 +468,8 @@ int Ctx::setScene(const am_scene& s) {
     r |= alloc(&B.B2C, 12 * cap);
     r |= alloc(&top, cap); r |= alloc(&subOff, cap + 1); r |= alloc(&subIds, cap);
     r |= alloc(&rowCount, cap + 1); r |= alloc(&rowOff, cap + 1); r |= alloc(&wakeFlag, cap); r |= alloc(&extFlag, cap);
-    r |= alloc(&bodyMax, 2 * (size_t)cap);   // 64-bit colouring priorities
+    // colouring: a 64-bit priority, then a mask of Ctx::MAXC colours (4 words) per body
+    r |= alloc(&bodyMax, 10 * (size_t)cap);
     r |= alloc(&colourCnt, MAXC + 1); r |= alloc(&colourOff, MAXC + 2); r |= alloc(&colourFill, MAXC + 1);
     N.n = s.n_nodes;
     r |= alloc(&N.cB, 3 * (size_t)N.n); r |= alloc(&N.cW, 3 * (size_t)N.n); r |= alloc(&N.r, N.n);
@@ -738,10 +742,12 @@ int Ctx::runPGS(int nc, const int* order, int iters, bool inColl, double dt, boo
         int r = readCounts();
         if (r) return r;
         int ncol = hc->n_colours;
-        if (!coopBlocks) {
-            int per = 0;
+        const bool mixed = P.solver_order == AM_ORDER_MIXED;
+        if (!coopBlocks) {   // both coloured kernels: 128 threads, at most 4 blocks per SM
+            int per = 0, perM = 0;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pgs_fast_kernel(), 128, 0);
-            coopBlocks = std::max(1, std::min(per, 4)) * g_numSMs;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perM, pgs_mixed_kernel(), 128, 0);
+            coopBlocks = std::max(1, std::min(std::min(per, perM), 4)) * g_numSMs;
         }
         if (nc > mjCap) {
             int cap2 = std::max(nc + nc / 2, 1024);
@@ -758,10 +764,38 @@ int Ctx::runPGS(int nc, const int* order, int iters, bool inColl, double dt, boo
         int widest = 0;
         for (int k = 0; k < ncol; k++) widest = std::max(widest, hColOff[k + 1] - hColOff[k]);
         int blocks = std::min(coopBlocks, std::max(1, (widest + 7) / 8));
-        if (timed) cudaEventRecord(evA, stream);   // time the sweep (prep + persistent kernel)
-        launch_pgs_fast(B, c, PR, groupOrder, colourOff, ncol, nc, iters, P.omega, comp, P.tolerance, !inColl,
-                        P.friction_override, P.friction, P.sliding_threshold, Mj, invD, mjCap, dc, blocks, stream,
-                        inColl ? 0.0 : solveTol, inColl ? 0 : solveCheck);
+        if (mixed) {
+            if (mjCap > mixFCap) {
+                if (alloc(&mixF, (size_t)pgs_mixed_frows() * mjCap)) return AM_E_CUDA;
+                mixFCap = mjCap;
+            }
+            if (host.cap > mixUCap) {
+                if (alloc(&mixU, 14 * (size_t)host.cap)) return AM_E_CUDA;   // body data (8) and corrections (6)
+                mixUCap = host.cap;
+            }
+            const int ng = hColOff[ncol];
+            if (ng > mixGCap) {
+                int cap2 = std::max(ng + ng / 2, 256);
+                if (alloc(&mixG, 4 * (size_t)cap2)) return AM_E_CUDA;
+                mixGCap = cap2;
+            }
+            const int mblocks = pgs_mixed_grid_blocks(widest, coopBlocks);
+            int form = pgs_mixed_mode(hColOff, mblocks, host.cap, nc);
+            if (mixedForm >= 0) form = pgs_mixed_fits(mixedForm, hColOff, host.cap, nc) ? mixedForm : form;
+            mixedLastForm = form;
+            const int refine = mixedRefine > 0 ? mixedRefine : (solveCheck > 0 ? solveCheck : 50);
+            if (timed) cudaEventRecord(evA, stream);
+            // refined every `refine` sweeps and at every residual check
+            launch_pgs_mixed(B, c, PR, groupOrder, colourOff, ncol, nc, iters, P.omega, comp, P.tolerance, !inColl,
+                             P.friction_override, P.friction, P.sliding_threshold, Mj, invD, mixF, mixU,
+                             mixU + 8 * (size_t)host.cap, reinterpret_cast<int4*>(mixG), ng, host.cap, mjCap,
+                             dc, mblocks, form, stream, inColl ? 0.0 : solveTol, inColl ? 0 : solveCheck, refine);
+        } else {
+            if (timed) cudaEventRecord(evA, stream);   // time the sweep (prep + persistent kernel)
+            launch_pgs_fast(B, c, PR, groupOrder, colourOff, ncol, nc, iters, P.omega, comp, P.tolerance, !inColl,
+                            P.friction_override, P.friction, P.sliding_threshold, Mj, invD, mjCap, dc, blocks,
+                            stream, inColl ? 0.0 : solveTol, inColl ? 0 : solveCheck);
+        }
     }
     if (timed) { cudaEventRecord(evB, stream); pgsPending = true; }
     return AM_OK;

@@ -65,7 +65,7 @@ RESIDUAL_TARGET = 1e-6
 STEADY = (20, 40)                    # the steady window: steps 21..60
 
 
-def workload(name, n_scenes=BATCH_SCENES):
+def workload(name, n_scenes=BATCH_SCENES, order="mixed"):
     """Scene (or list of scenes), parameters, dt and a description of the named
     workload.  `n_scenes` shrinks the batch for profiling runs only; the
     benchmark figure is the 512-bin batch."""
@@ -82,25 +82,29 @@ def workload(name, n_scenes=BATCH_SCENES):
                    f"a 2-8 CTA cluster for the largest; each scene swept until its relative LCP residual <= "
                    f"{RESIDUAL_TARGET:g} (checked every 10 sweeps, cap {SWEEP_CAP})",
             "merging": "off", "precision": "fp32 solve, fp64 collision/contact setup/integration"}
+    so = {"reference": abi.AM_ORDER_REFERENCE, "coloured": abi.AM_ORDER_COLOURED, "mixed": abi.AM_ORDER_MIXED}[order]
+    otext = {"reference": "list order (bit-exact)", "coloured": "coloured, FP64 sweeps",
+             "mixed": "coloured, FP32 sweeps on the correction to an FP64 base point, FP64 refinement "
+                      "every 50 sweeps"}[order]
     if name in ("wall", "wall_nomerge"):
         merging = name == "wall"
         sc = scenes.wall(cols=40, rows=25, seed=2)
         P = abi.default_params(gravity_amount=9.81, friction_override=1, friction=0.5, restitution_override=1,
                                restitution=0.0, iterations=200, enable_merging=int(merging),
-                               solver_order=abi.AM_ORDER_COLOURED)
+                               solver_order=so)
         return sc, P, 0.005, {
             "workload": "brick wall 40x25 (0.4x0.2x0.2 m, 1000 kg/m3) + 50 kg sphere at 15 m/s",
             "bodies": int(sc.n), "dt": 0.005, "pgs_iterations": 200, "mu": 0.5,
-            "merging": "on" if merging else "off", "pgs_order": "coloured full solve, exact single sweep",
-            "precision": "fp64"}
+            "merging": "on" if merging else "off", "pgs_order": f"full solve {otext}; exact single sweep",
+            "precision": "fp64 state and multipliers"}
     if name == "tower":
         sc = scenes.tower(25, seed=1)
         P = abi.default_params(gravity_amount=9.81, friction_override=1, friction=0.6, restitution_override=1,
                                restitution=0.0, iterations=100, enable_merging=0,
-                               solver_order=abi.AM_ORDER_COLOURED)
+                               solver_order=so)
         return sc, P, 0.01, {"workload": "tower of 25 boxes 1.0x0.5x1.0 m", "bodies": int(sc.n), "dt": 0.01,
-                             "pgs_iterations": 100, "mu": 0.6, "merging": "off", "pgs_order": "coloured",
-                             "precision": "fp64"}
+                             "pgs_iterations": 100, "mu": 0.6, "merging": "off", "pgs_order": otext,
+                             "precision": "fp64 state and multipliers"}
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -311,7 +315,7 @@ def run_reference(args):
     ws, rank, _ = dist_init()
     if rank != 0:
         return
-    sc, P, dt, cfg = workload(args.workload, args.scenes)
+    sc, P, dt, cfg = workload(args.workload, args.scenes, args.order)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_binding import Oracle
     P.solver_order = abi.AM_ORDER_REFERENCE
@@ -336,7 +340,7 @@ def run_reference(args):
         el = time.perf_counter() - t0
         v = args.steps / el
         desc = f"{args.steps} steps after {args.warmup} warm-up steps, single thread"
-        cfg = dict(cfg, pgs_order="reference list order")
+        cfg = dict(cfg, pgs_order="reference list order", precision="fp64 throughout (the oracle)")
     out = {"metric": METRIC, "value": v, "unit": unit, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
@@ -531,7 +535,7 @@ def run_ours(args):
     if local == 0:                    # one compiler per node; the others wait for the library
         build.build()
     barrier(ws)
-    sc, P, dt, cfg = workload(args.workload, args.scenes)
+    sc, P, dt, cfg = workload(args.workload, args.scenes, args.order)
     batch = args.workload == "batch"
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     if batch:
@@ -711,6 +715,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch")
+    ap.add_argument("--order", default="mixed", choices=("reference", "coloured", "mixed"),
+                    help="full-solve order of the single-scene workloads (tower, wall, wall_nomerge)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the comparison arms (plain batched PGS, one scene at a time; profiling runs only)")

@@ -48,6 +48,8 @@ extern "C" {
 /* ---- Gauss-Seidel ordering on the device -------------------------------- */
 #define AM_ORDER_REFERENCE 0  /* contacts in list order: bit-exact to PGS.java */
 #define AM_ORDER_COLOURED  1  /* body-pair groups coloured, colours in parallel */
+#define AM_ORDER_MIXED     2  /* AM_ORDER_COLOURED with FP32 sweeps on the correction to an FP64
+                                 base point, refined in FP64 (same fixed point, FP64 multipliers) */
 
 /*
  * Solver / system parameters.  Field names and defaults follow the reference
@@ -367,6 +369,16 @@ int32_t am_set_batch_critical(void* ctx, double frac, int32_t cap);
  * check_every sweeps (0 disables; the reference's max-change tolerance still
  * applies).  No reference counterpart: PGS.java stops on max |delta lambda| only. */
 int32_t am_set_residual_target(void* ctx, double residual_target, int32_t check_every);
+/* AM_ORDER_MIXED: the form of the solve kernel (-1, default: chosen per
+ * step from the colours and sizes; 0: a cooperative grid; 1: one block, body
+ * data in shared memory; 2: one block, contact records in shared memory too,
+ * taken only when they fit) and the FP64 refinement interval in sweeps (0,
+ * default: every 50 sweeps, or at every residual check when a residual target
+ * is set).  Results do not depend on the form beyond FP32 rounding.  No
+ * reference counterpart. */
+int32_t am_set_mixed_form(void* ctx, int32_t form, int32_t refine);
+/* the form the last AM_ORDER_MIXED solve ran in (-1 before the first) */
+int32_t am_get_mixed_form(void* ctx, int32_t* form);
 /* per-scene figures of the last step (arrays of n_scenes; NULL skips one):
  * sweeps, relative residual, learned start fell back, colours of the contact groups */
 int32_t am_get_batch_scene_stats(void* ctx, int32_t* sweeps, float* residual, int32_t* fell_back, int32_t* colours);

@@ -93,8 +93,10 @@ def test_device_matches_committed_golden(gpu_lib):
         assert _digest(g) == want, f"step {s}"
 
 
+# AM_ORDER_COLOURED; AM_ORDER_MIXED with its kernel form chosen per step, and on a grid
+@pytest.mark.parametrize("order,form", [(1, -1), (2, -1), (2, 0)], ids=["fp64", "mixed", "mixed-grid"])
 @pytest.mark.parametrize("name,warm,cap", [("wall_small", 94, 60000), ("tower12", 54, 500000)])
-def test_coloured_converged_with_collections(gpu_lib, name, warm, cap):
+def test_coloured_converged_with_collections(gpu_lib, name, warm, cap, order, form):
     """The coloured FP64 full solve (AM_ORDER_COLOURED) with merged
     collections as solve bodies: from an identical merged state (reference
     order first, bit-exact), one step solved to a fixed point on both sides
@@ -112,7 +114,8 @@ def test_coloured_converged_with_collections(gpu_lib, name, warm, cap):
     o.step(dt, warm)
     assert g.topology() == o.topology()
     conv = dict(over, iterations=cap, tolerance=1e-13)
-    g.set_params(params(enable_merging=1, solver_order=abi.AM_ORDER_COLOURED, **conv))
+    g.set_params(params(enable_merging=1, solver_order=order, **conv))
+    g.set_mixed_form(form)
     o.set_params(params(enable_merging=1, **conv))
     g.step(dt)
     o.step(dt)

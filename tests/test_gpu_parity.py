@@ -86,12 +86,23 @@ def test_phase_by_phase(gpu_lib):
     assert st.sweeps == o.counters()["sweeps"]
 
 
+# (solver order, form of the mixed kernel: -1 chosen per step, 0 grid, 1 one
+# block, 2 one block with the contact records in shared memory)
+ORDERS = pytest.mark.parametrize("order,form", [(abi.AM_ORDER_COLOURED, -1), (abi.AM_ORDER_MIXED, -1),
+                                                (abi.AM_ORDER_MIXED, 0), (abi.AM_ORDER_MIXED, 1),
+                                                (abi.AM_ORDER_MIXED, 2)],
+                                 ids=["fp64", "mixed", "mixed-grid", "mixed-block", "mixed-shared"])
+
+
+@ORDERS
 @pytest.mark.parametrize("name", ["tower6", "pile_box_sphere", "wall_small"])
-def test_coloured_converged(gpu_lib, name):
+def test_coloured_converged(gpu_lib, name, order, form):
     """AM_ORDER_COLOURED reorders Gauss-Seidel, so multipliers match only at
     convergence: from an identical state (reference-order steps first), both
     sides iterate to a fixed point and must agree within 1e-6 relative
-    (compliance 1e-3 makes the regularised LCP's solution unique)."""
+    (compliance 1e-3 makes the regularised LCP's solution unique).
+    AM_ORDER_MIXED (FP32 sweeps on the correction, FP64 refinement) must
+    reach the same fixed point to the same bound."""
     from adaptivemerging_gb300 import native
     sc = SCENES[name]()
     P = params(iterations=100)
@@ -102,10 +113,13 @@ def test_coloured_converged(gpu_lib, name):
     o.step(DT, warm)
     assert compare_bodies(g.bodies(), o.bodies()) is None
     iters = {"tower6": 6000, "pile_box_sphere": 6000, "wall_small": 60000}[name]
-    g.set_params(params(iterations=iters, tolerance=1e-13, solver_order=abi.AM_ORDER_COLOURED))
+    g.set_params(params(iterations=iters, tolerance=1e-13, solver_order=order))
+    g.set_mixed_form(form)
     o.set_params(params(iterations=iters, tolerance=1e-13))
     g.step(DT)
     o.step(DT)
+    if order == abi.AM_ORDER_MIXED and form >= 0:
+        assert g.mixed_form() == form
     lg, lo = g.contacts()["lambda"], o.contacts()["lambda"]
     assert lg.shape == lo.shape and lo.size > 0
     scale = max(1.0, float(np.abs(lo).max()))
@@ -116,7 +130,8 @@ def test_coloured_converged(gpu_lib, name):
     assert st.residual_rel <= 1e-6
 
 
-def test_coloured_residual_target_stops_at_target(gpu_lib):
+@ORDERS
+def test_coloured_residual_target_stops_at_target(gpu_lib, order, form):
     """am_set_residual_target: the coloured FP64 solve stops as soon as the
     relative natural-map residual is <= the target (the reference's
     max-change tolerance switched off), well before the sweep cap, and the
@@ -128,7 +143,8 @@ def test_coloured_residual_target_stops_at_target(gpu_lib):
     o = Oracle(sc, P)
     g.step(DT, 90)
     o.step(DT, 90)
-    g.set_params(params(iterations=60000, tolerance=0.0, solver_order=abi.AM_ORDER_COLOURED))
+    g.set_params(params(iterations=60000, tolerance=0.0, solver_order=order))
+    g.set_mixed_form(form)
     g.set_residual_target(1e-7, 10)
     o.set_params(params(iterations=60000, tolerance=1e-13))
     g.step(DT)
