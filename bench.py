@@ -635,17 +635,19 @@ def run_ours(args):
         sweep_ms = pgs_ms / args.steps
         bytes_step = head["contacts_mean"] * SWEEP_HBM_BYTES_PER_CONTACT + cfg["bodies"] * SWEEP_HBM_BYTES_PER_BODY
         achieved = bytes_step / (sweep_ms / 1e3) / 1e9 if sweep_ms > 0 else 0.0
-        traffic = None
+        traffic = traffic_basis = None
         tf = os.path.join(ROOT, "profiles", "k_batch_sweep_traffic.json")
         if os.path.exists(tf):
             with open(tf) as f:
                 tj = json.load(f)
             if tj.get("warmup") == args.warmup and tj.get("steps") == args.steps:
                 traffic = tj.get("dram_bytes_per_step")
+                traffic_basis = tj.get("basis")
         floor_ms = w["floor_cycles"] / (sm_mhz * 1e3) / args.steps
         out["roofline"] = {
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak if peak else None, "traffic": traffic, "peak_source": peak_kind,
+            "frac": achieved / peak if peak else None, "traffic": traffic, "traffic_basis": traffic_basis,
+            "peak_source": peak_kind,
             "kernel": "k_batch_sweep + k_batch_sweep_cluster (all sweep launches of a step)",
             "sweep_ms_per_step": sweep_ms,
             "algorithmic_bytes_per_step": bytes_step,
