@@ -509,11 +509,10 @@ __device__ __forceinline__ void pair_impulse(Pair& P, const Rec& c, const float*
 // instead of three dot products and three updates.  (D lam - w) / (D + c) is
 // evaluated as lam - (c lam + w) / (D + c), and the relaxation factor (1:
 // plain) scales 1 / (D + c).
-__device__ __forceinline__ void sweep_contact(Pair& P, const float* R, int slot, float* lp, float omega,
-                                              float comp, float relax, float* dOut) {
+__device__ __forceinline__ void sweep_contact_l(Pair& P, const float* R, int slot, const float4 l, float* lp,
+                                                float omega, float comp, float relax, float* dOut) {
     Rec c;
     load_rec(R, slot, c);
-    const float4 l = sld4(lp);
     float rv[3];
     rel_vel(P, c, rv);
     const float lq[3] = {l.x, l.y, l.z};
@@ -543,6 +542,11 @@ __device__ __forceinline__ void sweep_contact(Pair& P, const float* R, int slot,
 #pragma unroll
     for (int q = 0; q < 3; q++) F[q] = fmaf(d2, c.f[2][q], fmaf(d1, c.f[1][q], d0 * c.f[0][q]));
     pair_impulse(P, c, F);
+}
+
+__device__ __forceinline__ void sweep_contact(Pair& P, const float* R, int slot, float* lp, float omega,
+                                              float comp, float relax, float* dOut) {
+    sweep_contact_l(P, R, slot, sld4(lp), lp, omega, comp, relax, dOut);
 }
 
 // PGS.confidentWarmStart: delta-v += M^-1 J^T lambda
@@ -706,6 +710,24 @@ __device__ __forceinline__ void nncg_slot(float* l, float* gp, int it, float bet
         *reinterpret_cast<float4*>(l) = L;
     }
     *reinterpret_cast<float4*>(gp + 4) = p;
+}
+// nncg_slot on a multiplier slot already in registers (the sweep update that
+// follows loads and stores it once)
+__device__ __forceinline__ float4 nncg_slot_reg(float4 L, float* gp, int it, float beta) {
+    const float4 g = *reinterpret_cast<const float4*>(gp);
+    float4 p = *reinterpret_cast<const float4*>(gp + 4);
+    if (it == 0) {
+        p = g;
+    } else if (beta < 0.f) {
+        p = make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+        L.x = __fmaf_rn(beta, p.x, L.x);
+        L.y = __fmaf_rn(beta, p.y, L.y);
+        L.z = __fmaf_rn(beta, p.z, L.z);
+        p = make_float4(__fmaf_rn(beta, p.x, g.x), __fmaf_rn(beta, p.y, g.y), __fmaf_rn(beta, p.z, g.z), 0.f);
+    }
+    *reinterpret_cast<float4*>(gp + 4) = p;
+    return L;
 }
 // one body's momentum step on delta-v v, delta-v at the sweep's start d0 and
 // q (6 each): q = beta q + (v - d0), v += beta q_old, d0 = v (first
@@ -938,14 +960,13 @@ __global__ void __launch_bounds__(512) k_batch_sweep(
             } else if (op == OP_SWEEP) {
                 float d[3];
                 float* g = accel ? (resident ? sgp + 8 * lam_pos(slot) : gpG + 8 * ((size_t)slA + j)) : nullptr;
-                if (lazy && rep == 0) nncg_slot(lp, g, pendIt, pendBeta);
-                sweep_contact(P, R, slot, lp, omega, comp, relax, d);
+                float4 l = sld4(lp);
+                if (lazy && rep == 0) l = nncg_slot_reg(l, g, pendIt, pendBeta);
+                sweep_contact_l(P, R, slot, l, lp, omega, comp, relax, d);
                 if (accel) {
                     if (rep > 0)
                         for (int q = 0; q < 3; q++) d[q] = __fadd_rn(g[q], d[q]);
-                    g[0] = d[0];
-                    g[1] = d[1];
-                    g[2] = d[2];
+                    *reinterpret_cast<float4*>(g) = make_float4(d[0], d[1], d[2], 0.f);
                     if (rep == reps - 1) gsq = sq3_acc(d, gsq);
                 }
             } else if (op == OP_RES) {
@@ -1379,15 +1400,14 @@ __global__ void __launch_bounds__(256, 1) k_batch_sweep_cluster(
                 warm_contact(P, R, slot, lp);
             } else if (op == OP_SWEEP) {
                 float d[3];
-                if (lazy && jj < cnt) nncg_slot(lp, sgp + 8 * lam_pos(slot), pendIt, pendBeta);
-                sweep_contact(P, R, slot, lp, omega, comp, relax, d);
+                float4 l = sld4(lp);
+                if (lazy && jj < cnt) l = nncg_slot_reg(l, sgp + 8 * lam_pos(slot), pendIt, pendBeta);
+                sweep_contact_l(P, R, slot, l, lp, omega, comp, relax, d);
                 if (accel) {
                     float* g = sgp + 8 * lam_pos(slot);
                     if (jj >= cnt)
                         for (int q = 0; q < 3; q++) d[q] = __fadd_rn(g[q], d[q]);
-                    g[0] = d[0];
-                    g[1] = d[1];
-                    g[2] = d[2];
+                    *reinterpret_cast<float4*>(g) = make_float4(d[0], d[1], d[2], 0.f);
                     if (jj >= (reps - 1) * cnt) gsq = sq3_acc(d, gsq);
                 }
             } else if (op == OP_RES) {

@@ -203,6 +203,7 @@ struct Ctx {
     static const int MAXC = 256;
     int coopBlocks = 0;
     std::vector<int> hColOff;    // colour offsets of the coloured full solve (host copy)
+    int* hColPin = nullptr;      // pinned staging of the colour offsets (MAXC + 1)
     double* Mj = nullptr;     // coloured sweep: M^-1 J^T per row and lane (36 per contact)
     double* invD = nullptr;   // coloured sweep constants per contact: 1/(D + c), A, q per row, couplings, mu
     int mjCap = 0;

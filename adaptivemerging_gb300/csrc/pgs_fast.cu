@@ -49,10 +49,8 @@ __device__ __forceinline__ double mu_fast(const DBodies& B, const DContacts& C, 
 // per-contact precompute: Mj[36] (M^-1 J^T entries, row-major by row then
 // lane k) and the constant table K: 1/(D + c), A, q per row, the couplings
 // G10, G20, G21 and the contact's friction coefficient
-__global__ void k_fast_prep(DBodies B, DContacts C, int nc, double comp, double omega, int fo, double fv,
-                            double* Mj, double* K, int cap) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nc) return;
+__device__ __forceinline__ void fast_prep_contact(const DBodies& B, const DContacts& C, int c, double comp,
+                                                  double omega, int fo, double fv, double* Mj, double* K, int cap) {
     int ccap = C.cap;
     int s1 = C.sb1[c], s2 = C.sb2[c];
     double m1 = B.minv[s1], m2 = B.minv[s2];
@@ -85,6 +83,13 @@ __global__ void k_fast_prep(DBodies B, DContacts C, int nc, double comp, double 
     K[K_G20 * cap + c] = g20;
     K[K_G21 * cap + c] = g21;
     K[K_MU * cap + c] = mu_fast(B, C, c, fo, fv);
+}
+
+__global__ void k_fast_prep(DBodies B, DContacts C, int nc, double comp, double omega, int fo, double fv,
+                            double* Mj, double* K, int cap) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    fast_prep_contact(B, C, c, comp, omega, fo, fv, Mj, K, cap);
 }
 
 __device__ __forceinline__ double hw_sum(double v, unsigned mask) {
@@ -375,9 +380,7 @@ enum : int {
 };
 int pgs_mixed_frows() { return MIX_REC; }
 
-__global__ void k_mixed_pack(DContacts C, int nc, const double* K, float* F, int cap) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nc) return;
+__device__ __forceinline__ void mixed_pack_contact(const DContacts& C, int c, const double* K, float* F, int cap) {
     const int ccap = C.cap;
     float r[MIX_REC];
     for (int q = 0; q < 3; q++)
@@ -399,20 +402,29 @@ __global__ void k_mixed_pack(DContacts C, int nc, const double* K, float* F, int
     for (int k = 0; k < MIX_REC / 4; k++) dst[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
 }
 
-__global__ void k_mixed_bodies(DBodies B, int nb, float* BM) {
-    int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nb) return;
-    const double* J = B.jinv + 9 * (size_t)b;
-    float4* d = reinterpret_cast<float4*>(BM + 8 * (size_t)b);
-    d[0] = make_float4((float)B.minv[b], (float)J[0], (float)J[4], (float)J[8]);
-    d[1] = make_float4((float)J[1], (float)J[2], (float)J[5], 0.f);
+// the FP64 constants (as k_fast_prep) and the FP32 record of a contact
+__global__ void k_mixed_prep(DBodies B, DContacts C, int nc, double comp, double omega, int fo, double fv,
+                             double* Mj, double* K, float* F, int cap) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    fast_prep_contact(B, C, c, comp, omega, fo, fv, Mj, K, cap);
+    mixed_pack_contact(C, c, K, F, cap);
 }
 
 // the coloured groups in sweep order, flattened: first contact, contact
 // count and the two solve bodies (bit 31 set for a pinned body), so that a
 // sweep reads one record per group instead of a chain of four indirections
-__global__ void k_mixed_groups(DBodies B, DContacts C, DPairs P, const int* groupOrder, int ng, int4* GI) {
+// ... and per body (b < nb) its FP32 inverse mass and the symmetric part of
+// its world inverse inertia
+__global__ void k_mixed_groups(DBodies B, DContacts C, DPairs P, const int* groupOrder, int ng, int4* GI, int nb,
+                               float* BM) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nb) {
+        const double* J = B.jinv + 9 * (size_t)k;
+        float4* d = reinterpret_cast<float4*>(BM + 8 * (size_t)k);
+        d[0] = make_float4((float)B.minv[k], (float)J[0], (float)J[4], (float)J[8]);
+        d[1] = make_float4((float)J[1], (float)J[2], (float)J[5], 0.f);
+    }
     if (k >= ng) return;
     const int g = groupOrder[k];
     const int c0 = P.off[g];
@@ -834,16 +846,12 @@ void launch_pgs_mixed(const DBodies& B, DContacts& C, DPairs& P, const int* grou
                       int ng, int nbodies, int mcap, DCount* dc, int gridBlocks, int mode, cudaStream_t s,
                       double resTol, int check, int refine) {
     if (ncol <= 0 || nc <= 0) return;
-    k_fast_prep<<<(nc + 127) / 128, 128, 0, s>>>(B, C, nc, comp, omega, fo, fv, Mj, K, mcap);
-    k_mixed_pack<<<(nc + 127) / 128, 128, 0, s>>>(C, nc, K, F, mcap);
-    k_mixed_bodies<<<(nbodies + 127) / 128, 128, 0, s>>>(B, nbodies, BM);
-    k_mixed_groups<<<(ng + 127) / 128, 128, 0, s>>>(B, C, P, groupOrder, ng, GI);
-    AM_LAUNCHED(4);
-    cudaMemsetAsync(&dc->maxchg, 0, sizeof(dc->maxchg), s);
-    cudaMemsetAsync(&dc->bar_count, 0, sizeof(int), s);
-    cudaMemsetAsync(&dc->reschk, 0, sizeof(unsigned long long) * 4, s);
+    k_mixed_prep<<<(nc + 127) / 128, 128, 0, s>>>(B, C, nc, comp, omega, fo, fv, Mj, K, F, mcap);
+    const int nk = std::max(ng, nbodies);
+    k_mixed_groups<<<(nk + 127) / 128, 128, 0, s>>>(B, C, P, groupOrder, ng, GI, nbodies, BM);
+    AM_LAUNCHED(2);
     int earlyI = early ? 1 : 0;
-    if (mode == 1 || mode == 2) {
+    if (mode == 1 || mode == 2) {   // one block: its sweep maxima and residuals live in shared memory
         static bool attr = false;
         if (!attr) {
             cudaFuncSetAttribute(k_pgs_mixed<1, MIXED_ONE_NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -859,6 +867,9 @@ void launch_pgs_mixed(const DBodies& B, DContacts& C, DPairs& P, const int* grou
         AM_LAUNCHED(1);
         return;
     }
+    cudaMemsetAsync(&dc->maxchg, 0, sizeof(dc->maxchg), s);
+    cudaMemsetAsync(&dc->bar_count, 0, sizeof(int), s);
+    cudaMemsetAsync(&dc->reschk, 0, sizeof(unsigned long long) * 4, s);
     DBodies Bc = B;
     const double* Mjc = Mj;
     const double* Kc = K;

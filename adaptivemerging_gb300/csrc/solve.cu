@@ -389,6 +389,60 @@ __global__ void k_colour(DBodies B, DContacts C, DPairs P, int npairs, int* colo
     }
 }
 
+// Small scenes: sequential first-fit in group order (the broad phase's
+// (i, j) order), one thread over shared-memory copies of the groups' bodies
+// and the bodies' colour masks.  A stack of bodies, whose groups come in
+// order along the stack, takes two colours (Jones-Plassmann up to three),
+// and a colour costs the single-scene sweep a barrier and a group chain.
+__global__ void k_colour_seq(DBodies B, DContacts C, DPairs P, int npairs, int* colourOf, int* colourCnt, int maxC,
+                             int nbodies, DCount* dc) {
+    extern __shared__ unsigned long long sq[];
+    const int W = (maxC + 63) / 64;
+    unsigned long long* used = sq;                                    // nbodies * W
+    int2* gb = reinterpret_cast<int2*>(sq + (size_t)nbodies * W);     // npairs
+    int* cnt = reinterpret_cast<int*>(gb + npairs);                   // maxC
+    const int t = threadIdx.x, T = blockDim.x;
+    const int PIN = (int)0x80000000u;
+    for (int b = t; b < nbodies * W; b += T) used[b] = 0ull;
+    for (int k = t; k < maxC; k += T) cnt[k] = 0;
+    for (int g = t; g < npairs; g += T) {
+        if (P.count[g] <= 0) { gb[g] = make_int2(-1, -1); continue; }
+        const int c = P.off[g];
+        const int s1 = C.sb1[c], s2 = C.sb2[c];
+        gb[g] = make_int2(s1 | ((B.flags[s1] & F_PINNED) ? PIN : 0), s2 | ((B.flags[s2] & F_PINNED) ? PIN : 0));
+    }
+    __syncthreads();
+    __shared__ int s_ncol, s_full;
+    if (t == 0) {
+        int ncol = 0, full = 0;
+        for (int g = 0; g < npairs; g++) {
+            const int2 q = gb[g];
+            if (q.x == -1 && q.y == -1) { colourOf[g] = -2; continue; }
+            const bool p1 = q.x < 0, p2 = q.y < 0;
+            const int s1 = q.x & 0x7fffffff, s2 = q.y & 0x7fffffff;
+            int col = -1;
+            for (int w = 0; w < W && col < 0; w++) {
+                unsigned long long m = (p1 ? 0ull : used[(size_t)s1 * W + w]) | (p2 ? 0ull : used[(size_t)s2 * W + w]);
+                if (m != ~0ull) col = 64 * w + __ffsll((long long)~m) - 1;
+            }
+            if (col < 0 || col >= maxC) { colourOf[g] = -2; full = 1; continue; }
+            if (!p1) used[(size_t)s1 * W + col / 64] |= 1ull << (col % 64);
+            if (!p2) used[(size_t)s2 * W + col / 64] |= 1ull << (col % 64);
+            colourOf[g] = col;
+            cnt[col]++;
+            ncol = max(ncol, col + 1);
+        }
+        s_ncol = ncol;
+        s_full = full;
+    }
+    __syncthreads();
+    for (int k = t; k < maxC; k += T) colourCnt[k] = cnt[k];
+    if (t == 0) {
+        dc->n_colours = s_ncol;
+        if (s_full) dc->error = AM_E_CAPACITY;
+    }
+}
+
 __global__ void k_colour_place(DPairs P, int npairs, const int* colourOf, const int* colourOff, int* fill,
                                int* groupOrder) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -405,8 +459,13 @@ void colour_groups(const DBodies& B, const DContacts& C, DPairs& P, int npairs, 
                    DCount* dc, Scratch& sc, cudaStream_t s) {
     if (npairs <= 0) { cudaMemsetAsync(&dc->n_colours, 0, sizeof(int), s); return; }
     cudaMemsetAsync(colourCnt, 0, sizeof(int) * (maxC + 1), s);
-    k_colour<<<1, 1024, 0, s>>>(B, C, P, npairs, colourOf, colourCnt, maxC, bodyMax, bodyMax + nbodies, nbodies,
-                                dc);
+    const int W = (maxC + 63) / 64;
+    const size_t seqSmem = 8 * (size_t)nbodies * W + 8 * (size_t)npairs + 4 * (size_t)maxC;
+    if (npairs <= 128 && seqSmem <= 48 * 1024)
+        k_colour_seq<<<1, 256, seqSmem, s>>>(B, C, P, npairs, colourOf, colourCnt, maxC, nbodies, dc);
+    else
+        k_colour<<<1, 1024, 0, s>>>(B, C, P, npairs, colourOf, colourCnt, maxC, bodyMax, bodyMax + nbodies,
+                                    nbodies, dc);
     AM_LAUNCHED(1);
     launch_scan(colourCnt, colourOff, maxC + 1, sc, nullptr, s);
     cudaMemsetAsync(fill, 0, sizeof(int) * maxC, s);

@@ -314,6 +314,8 @@ void Ctx::release() {
     if (flagStage) cudaFreeHost(flagStage);
     flagStage = nullptr;
     flagStageCap = 0;
+    if (hColPin) cudaFreeHost(hColPin);
+    hColPin = nullptr;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
     for (int q = 0; q < NPOOL; q++) {
@@ -442,6 +444,7 @@ int Ctx::setScene(const am_scene& s) {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaMalloc((void**)&dc, sizeof(DCount)));
     CK(cudaMallocHost((void**)&hc, sizeof(DCount)));
+    CK(cudaMallocHost((void**)&hColPin, sizeof(int) * (MAXC + 1)));
     CK(cudaMemsetAsync(dc, 0, sizeof(DCount), stream));
     if (!g_numSMs) {
         int dev = 0;
@@ -739,6 +742,8 @@ int Ctx::runPGS(int nc, const int* order, int iters, bool inColl, double dt, boo
     } else {
         colour_groups(B, c, PR, nPairs, colourOf, colourCnt, colourOff, colourFill, groupOrder, MAXC,
                       (unsigned long long*)bodyMax, host.cap, dc, SC, stream);
+        // the colour offsets come back with the counts (one wait)
+        cudaMemcpyAsync(hColPin, colourOff, sizeof(int) * (MAXC + 1), cudaMemcpyDeviceToHost, stream);
         int r = readCounts();
         if (r) return r;
         int ncol = hc->n_colours;
@@ -756,11 +761,8 @@ int Ctx::runPGS(int nc, const int* order, int iters, bool inColl, double dt, boo
         }
         // 8 half-warp groups per block; enough blocks for every group of the
         // largest colour (more blocks only make the grid barriers slower)
-        hColOff.resize(ncol + 1);
-        if (ncol > 0) {
-            cudaMemcpyAsync(hColOff.data(), colourOff, sizeof(int) * (ncol + 1), cudaMemcpyDeviceToHost, stream);
-            if ((r = syncErr())) return r;
-        }
+        hColOff.assign(hColPin, hColPin + ncol + 1);
+        if (ncol == 0) hColOff[0] = 0;
         int widest = 0;
         for (int k = 0; k < ncol; k++) widest = std::max(widest, hColOff[k + 1] - hColOff[k]);
         int blocks = std::min(coopBlocks, std::max(1, (widest + 7) / 8));
@@ -783,7 +785,7 @@ int Ctx::runPGS(int nc, const int* order, int iters, bool inColl, double dt, boo
             int form = pgs_mixed_mode(hColOff, mblocks, host.cap, nc);
             if (mixedForm >= 0) form = pgs_mixed_fits(mixedForm, hColOff, host.cap, nc) ? mixedForm : form;
             mixedLastForm = form;
-            const int refine = mixedRefine > 0 ? mixedRefine : (solveCheck > 0 ? solveCheck : 50);
+            const int refine = mixedRefine > 0 ? mixedRefine : (solveCheck > 0 ? solveCheck : 100);
             if (timed) cudaEventRecord(evA, stream);
             // refined every `refine` sweeps and at every residual check
             launch_pgs_mixed(B, c, PR, groupOrder, colourOff, ncol, nc, iters, P.omega, comp, P.tolerance, !inColl,

@@ -85,7 +85,7 @@ def workload(name, n_scenes=BATCH_SCENES, order="mixed"):
     so = {"reference": abi.AM_ORDER_REFERENCE, "coloured": abi.AM_ORDER_COLOURED, "mixed": abi.AM_ORDER_MIXED}[order]
     otext = {"reference": "list order (bit-exact)", "coloured": "coloured, FP64 sweeps",
              "mixed": "coloured, FP32 sweeps on the correction to an FP64 base point, FP64 refinement "
-                      "every 50 sweeps"}[order]
+                      "every 100 sweeps"}[order]
     if name in ("wall", "wall_nomerge"):
         merging = name == "wall"
         sc = scenes.wall(cols=40, rows=25, seed=2)

@@ -373,7 +373,7 @@ int32_t am_set_residual_target(void* ctx, double residual_target, int32_t check_
  * step from the colours and sizes; 0: a cooperative grid; 1: one block, body
  * data in shared memory; 2: one block, contact records in shared memory too,
  * taken only when they fit) and the FP64 refinement interval in sweeps (0,
- * default: every 50 sweeps, or at every residual check when a residual target
+ * default: every 100 sweeps, or at every residual check when a residual target
  * is set).  Results do not depend on the form beyond FP32 rounding.  No
  * reference counterpart. */
 int32_t am_set_mixed_form(void* ctx, int32_t form, int32_t refine);
