@@ -1,6 +1,8 @@
 // capi.cu -- the extern "C" entry points declared in include/am.h.
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 #include <cstring>
 #include <new>
 #include <vector>
@@ -466,6 +468,38 @@ int32_t am_get_bodies(void* ctx, am_body_state* out) {
     Ctx* c = (Ctx*)ctx;
     if (!c->stream) return AM_E_STATE;
     return c->getBodies(out);
+}
+
+int Ctx::setKinematic(int body, const double* axis, double amp, double freq, double dt) {
+    if (nScenes > 0) { err = "prescribed motion is for single scenes"; return AM_E_STATE; }
+    if (body < 0 || body >= nScene || !axis || !(amp >= 0) || !(freq >= 0) || !(dt > 0) || !std::isfinite(amp) ||
+        !std::isfinite(freq) || !std::isfinite(dt)) { err = "bad kinematic body"; return AM_E_ARG; }
+    if (!(host.flags[body] & F_PINNED)) { err = "a kinematic body must be pinned"; return AM_E_ARG; }
+    for (size_t i = 0; i < kin.size(); i++)
+        if (kin[i].body == body) { kin.erase(kin.begin() + i); break; }
+    if (amp == 0) return AM_OK;
+    if ((int)kin.size() >= MAXKIN) { err = "too many kinematic bodies"; return AM_E_CAPACITY; }
+    Kinematic q;
+    q.body = body;
+    if (cudaMemcpyAsync(q.x0, B.x + 3 * body, sizeof(double) * 3, cudaMemcpyDeviceToHost, stream) != cudaSuccess)
+        return AM_E_CUDA;
+    int r = syncErr();
+    if (r) return r;
+    for (int k = 0; k < 3; k++) q.axis[k] = axis[k];
+    q.amp = amp;
+    q.omega = 2.0 * 3.141592653589793 * freq;
+    q.dt = dt;
+    kin.push_back(q);
+    kinSteps = 0;
+    return AM_OK;
+}
+
+int32_t am_set_kinematic(void* ctx, int32_t body, const double* axis, double amplitude, double frequency_hz,
+                         double dt) {
+    if (!ctx) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (!c->stream) return AM_E_STATE;
+    return c->setKinematic(body, axis, amplitude, frequency_hz, dt);
 }
 
 int32_t am_put_bodies(void* ctx, const am_body_state* in) {

@@ -364,6 +364,16 @@ struct Ctx {
     int readCounts();
     void gravityDir(double g[3]) const;
     int beginStep(int mode);
+    // pinned bodies moved by a prescribed oscillation (am_set_kinematic)
+    static const int MAXKIN = 8;
+    struct Kinematic {
+        int body;
+        double x0[3], axis[3], amp, omega, dt;
+    };
+    std::vector<Kinematic> kin;
+    int kinSteps = 0;   // steps started since the last am_set_kinematic
+    void applyKinematic();
+    int setKinematic(int body, const double* axis, double amp, double freq, double dt);
     int collisionDetection();
     int warmStart();
     int wake();

@@ -33,7 +33,7 @@ struct Header {
     char magic[4];
     int32_t version;
     int32_t n, cap, nNodes, nScenes;
-    int32_t nContacts, nSlots, mergingEvent, pad;
+    int32_t nContacts, nSlots, mergingEvent, kinSteps;
     int64_t totalSteps, mergeEvents, unmergeEvents;
 };
 
@@ -127,6 +127,7 @@ int Ctx::getState(std::vector<uint8_t>& out) {
     h.nContacts = nContacts;
     h.nSlots = M.nSlots;
     h.mergingEvent = mergingEvent ? 1 : 0;
+    h.kinSteps = kinSteps;
     h.totalSteps = totalSteps;
     h.mergeEvents = mergeEvents;
     h.unmergeEvents = unmergeEvents;
@@ -284,6 +285,7 @@ int Ctx::putState(const uint8_t* in, size_t size) {
     nPairs = 0;
     totalSteps = (int)h.totalSteps;
     mergingEvent = h.mergingEvent != 0;
+    kinSteps = h.kinSteps;
     mergeEvents = h.mergeEvents;
     unmergeEvents = h.unmergeEvents;
     // the device's top-level list and collection members follow the host

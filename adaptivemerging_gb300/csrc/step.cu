@@ -609,7 +609,48 @@ void Ctx::gravityDir(double g[3]) const {
     g[2] = 0;
 }
 
+// Pinned bodies with a prescribed oscillation (am_set_kinematic): at the start
+// of the n-th step since the call, x = x0 + axis * (amp * sin(w n dt)) and
+// v = axis * ((amp * w) * cos(w n dt)), evaluated on the host with the same
+// sine and cosine as the integrator's rotation update, and written to the
+// device with one small launch
+struct KinSet {
+    int n;
+    int body[Ctx::MAXKIN];
+    double x[Ctx::MAXKIN][3], v[Ctx::MAXKIN][3];
+};
+__global__ void k_set_kin(DBodies B, KinSet K) {
+    int i = threadIdx.x;
+    if (i >= K.n) return;
+    const int b = K.body[i];
+    for (int k = 0; k < 3; k++) {
+        B.x[3 * b + k] = K.x[i][k];
+        B.v[3 * b + k] = K.v[i][k];
+    }
+}
+
+void Ctx::applyKinematic() {
+    if (kin.empty()) return;
+    KinSet K{};
+    K.n = (int)kin.size();
+    for (int i = 0; i < K.n; i++) {
+        const Kinematic& q = kin[i];
+        const double t = (double)kinSteps * q.dt;
+        double sn, cs;
+        amd::det_sincos(q.omega * t, &sn, &cs);
+        K.body[i] = q.body;
+        for (int k = 0; k < 3; k++) {
+            K.x[i][k] = q.x0[k] + q.axis[k] * (q.amp * sn);
+            K.v[i][k] = q.axis[k] * ((q.amp * q.omega) * cs);
+        }
+    }
+    k_set_kin<<<1, 32, 0, stream>>>(B, K);
+    AM_LAUNCHED(1);
+    kinSteps++;
+}
+
 int Ctx::beginStep(int mode) {
+    if (mode == 0) applyKinematic();
     double g[3];
     gravityDir(g);
     if (ntop > 0) {

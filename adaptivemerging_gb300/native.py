@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libam.so")
 EXPORTS = [
     "am_params_default", "am_create", "am_destroy", "am_last_error", "am_set_params", "am_set_scene",
     "am_step", "am_collide", "am_warm_start", "am_solve", "am_integrate", "am_get_bodies",
-    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_get_step_phases", "am_get_state", "am_put_state", "am_merge_tests", "am_step_phase", "am_single_sweep_order", "am_single_sweep", "am_check_barrier_timeout", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats", "am_get_batch_scene_times", "am_get_batch_scene_ctas", "am_get_batch_scene_chain", "am_set_residual_target", "am_set_mixed_form", "am_get_mixed_form",
+    "am_num_contacts", "am_get_contacts", "am_get_stats", "am_get_perf", "am_reset_perf", "am_get_stream", "am_get_step_phases", "am_get_state", "am_put_state", "am_merge_tests", "am_step_phase", "am_single_sweep_order", "am_single_sweep", "am_check_barrier_timeout", "am_put_bodies", "am_get_topology", "am_set_batch", "am_set_batch_options", "am_get_batch_stats", "am_get_batch_scene_stats", "am_get_batch_scene_times", "am_get_batch_scene_ctas", "am_get_batch_scene_chain", "am_set_residual_target", "am_set_mixed_form", "am_get_mixed_form", "am_set_kinematic",
     "am_set_batch_local_sweeps", "am_set_batch_accel", "am_set_batch_critical", "am_set_batch_clusters", "am_set_batch_stage", "am_set_batch_relaxation",
     "am_set_batch_cluster_stage", "am_set_batch_size_classes", "am_set_phase_timing", "am_get_phase_times",
     "am_learned_collect", "am_learned_train", "am_learned_use", "am_learned_scope", "am_learned_weights", "am_learned_info",
@@ -73,6 +73,7 @@ def lib():
         L.am_set_residual_target.argtypes = [vp, C.c_double, C.c_int32]
         L.am_set_mixed_form.argtypes = [vp, C.c_int32, C.c_int32]
         L.am_get_mixed_form.argtypes = [vp, C.POINTER(C.c_int32)]
+        L.am_set_kinematic.argtypes = [vp, C.c_int32, C.POINTER(C.c_double), C.c_double, C.c_double, C.c_double]
         L.am_set_batch_local_sweeps.argtypes = [vp, C.c_int32]
         L.am_set_batch_accel.argtypes = [vp, C.c_int32]
         L.am_set_batch_critical.argtypes = [vp, C.c_double, C.c_int32]
@@ -391,6 +392,11 @@ class System:
         """AM_ORDER_MIXED: kernel form (-1 auto, 0 grid, 1 one block, 2 one
         block with the contact records in shared memory) and refinement interval."""
         self._check(lib().am_set_mixed_form(self.h, form, refine))
+
+    def set_kinematic(self, body, axis, amplitude, frequency_hz, dt):
+        """Prescribed oscillation of pinned body `body` (am_set_kinematic)."""
+        ax = (C.c_double * 3)(*[float(a) for a in axis])
+        self._check(lib().am_set_kinematic(self.h, int(body), ax, float(amplitude), float(frequency_hz), float(dt)))
 
     def mixed_form(self):
         """Form of the last AM_ORDER_MIXED solve (-1 before the first)."""

@@ -185,16 +185,19 @@ def random_pile(n=30, seed=0, kinds=("box", "sphere"), extent=3.0, height=4.0):
     return B.build()
 
 
+FUNNEL_PLATFORM = 1   # body index of funnel_clumps' platform
+
+
 def funnel_clumps(n_clumps=200, seed=5, top=3.0, bottom=0.5, height=3.0, base=1.0):
     """Clumps poured into a funnel over a platform (the large-scene workload's
     geometry, scaled by `n_clumps`).  Each clump is a sphere tree of 4-16
     spheres, r U(0.02, 0.08) m, in a compact random cluster, density
     U(500, 2000).  The funnel is four pinned box panels forming a truncated
     pyramid (half-widths `top` to `bottom`) whose lower rim sits `base` m
-    above a pinned platform box on the ground plane.  The clumps start in a
-    jittered grid inside the funnel, so they meet the panels at once.  The
-    platform is static: oscillating (kinematic) bodies are not part of the
-    reference's contact path."""
+    above a pinned platform box (body FUNNEL_PLATFORM) on the ground plane.
+    The clumps start in a jittered grid inside the funnel, so they meet the
+    panels at once.  The platform is pinned; the large-scene workload makes
+    it oscillate with am_set_kinematic (0.5 Hz, 0.05 m, vertical)."""
     rng = np.random.default_rng(seed)
     B = Builder()
     B.plane((0, 0, 0), (0, 1, 0), friction=0.7)

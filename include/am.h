@@ -369,6 +369,19 @@ int32_t am_set_batch_critical(void* ctx, double frac, int32_t cap);
  * check_every sweeps (0 disables; the reference's max-change tolerance still
  * applies).  No reference counterpart: PGS.java stops on max |delta lambda| only. */
 int32_t am_set_residual_target(void* ctx, double residual_target, int32_t check_every);
+/* A pinned body moved by a prescribed oscillation (a shaking platform).  No
+ * reference counterpart: the reference's pinned bodies stand still; a moving
+ * support enters the contact path only through the body velocity that
+ * Contact.computeB reads (Contact.java:290-321), the path a pinned body's zero
+ * velocity already takes (RigidBody.java:50).  At the start of the n-th step
+ * after this call (n = 0, 1, ...), the body's position is
+ *   x0 + axis * (amplitude * sin(w n dt)),  velocity axis * ((amplitude * w) * cos(w n dt)),
+ * w = 2 pi frequency_hz, x0 its position at this call; its orientation is
+ * unchanged.  The body must be pinned (AM_E_ARG otherwise); amplitude 0 removes
+ * it; at most 8 per context (AM_E_CAPACITY); single scenes only (AM_E_STATE
+ * for a batch).  Setting any body restarts the count n of every one. */
+int32_t am_set_kinematic(void* ctx, int32_t body, const double* axis, double amplitude, double frequency_hz,
+                         double dt);
 /* AM_ORDER_MIXED: the form of the solve kernel (-1, default: chosen per
  * step from the colours and sizes; 0: a cooperative grid; 1: one block, body
  * data in shared memory; 2: one block, contact records in shared memory too,

@@ -33,6 +33,7 @@ void or_run(void* h, double dt, int n) {
 /* Phase entry points, in RigidBodySystem.advanceTime order (no collections). */
 void or_begin_step(void* h) {
     World* w = (World*)h;
+    w->applyKinematic();
     w->totalSteps++;
     w->clearBodies();
     w->applyExternalForces();
@@ -140,6 +141,23 @@ int or_top_ids(void* h, int32_t* out, int cap) {
     return n;
 }
 
+int or_set_kinematic(void* h, int body, const double* axis, double amp, double freq, double dt) {
+    World* w = (World*)h;
+    if (body < 0 || body >= w->nScene || !w->bodies[body]->pinned) return -1;
+    for (size_t i = 0; i < w->kin.size(); i++)
+        if (w->kin[i].body == w->bodies[body]) { w->kin.erase(w->kin.begin() + i); break; }
+    if (amp == 0) return 0;
+    World::Kinematic q;
+    q.body = w->bodies[body];
+    q.x0[0] = q.body->x.x; q.x0[1] = q.body->x.y; q.x0[2] = q.body->x.z;
+    for (int k = 0; k < 3; k++) q.axis[k] = axis[k];
+    q.amp = amp;
+    q.omega = 2.0 * 3.141592653589793 * freq;
+    q.dt = dt;
+    w->kin.push_back(q);
+    w->kinSteps = 0;
+    return 0;
+}
 }  // extern "C"
 
 /* The merge and unmerge tests on the current state, in the reference's

@@ -1751,7 +1751,28 @@ void World::viscousDecay() {
     for (Body* b : bodies) { vscale_ip(b->v, P.viscous_linear); vscale_ip(b->omega, P.viscous_angular); }
 }
 
+// the library's prescribed oscillation of pinned bodies, evaluated with the
+// same operations: x = x0 + axis * (amp * sin(w n dt)), v = axis * ((amp * w)
+// * cos(w n dt)) at the start of the n-th step
+void World::applyKinematic() {
+    if (kin.empty()) return;
+    for (const Kinematic& q : kin) {
+        const double t = (double)kinSteps * q.dt;
+        double sn, cs;
+        det_sincos(q.omega * t, &sn, &cs);
+        double x[3], v[3];
+        for (int k = 0; k < 3; k++) {
+            x[k] = q.x0[k] + q.axis[k] * (q.amp * sn);
+            v[k] = q.axis[k] * ((q.amp * q.omega) * cs);
+        }
+        q.body->x = V3(x[0], x[1], x[2]);
+        q.body->v = V3(v[0], v[1], v[2]);
+    }
+    kinSteps++;
+}
+
 void World::step(double dt) {
+    applyKinematic();
     totalSteps++;
     clearBodies();
     applyExternalForces();

@@ -163,6 +163,12 @@ struct World {
     std::unordered_map<uint64_t, BPC*> bpcIndex;   // speeds checkExists (same result as the linear search)
     bool mergingEvent = false;
     int totalSteps = 0;
+    // pinned bodies with a prescribed oscillation (the library's
+    // am_set_kinematic; not part of the reference)
+    struct Kinematic { Body* body; double x0[3], axis[3], amp, omega, dt; };
+    std::vector<Kinematic> kin;
+    int kinSteps = 0;
+    void applyKinematic();
     Stats stats;
     int64_t mergeEvents = 0, unmergeEvents = 0;
     double gdir[3];

@@ -50,6 +50,9 @@ def lib():
         ip = C.POINTER(C.c_int32)
         L.or_merge_tests.argtypes = [C.c_void_p, ip, ip, ip, ip, C.POINTER(C.c_double), C.c_int]
         L.or_merge_tests.restype = C.c_int
+        L.or_set_kinematic.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_double, C.c_double,
+                                       C.c_double]
+        L.or_set_kinematic.restype = C.c_int
         _lib = L
     return _lib
 
@@ -130,6 +133,11 @@ class Oracle:
         k = lib().or_topology(self.h, items.ctypes.data_as(C.POINTER(C.c_int32)),
                               off.ctypes.data_as(C.POINTER(C.c_int32)), cap, C.byref(nt))
         return decode_topology(items[:k], off[:nt.value + 1])
+
+    def set_kinematic(self, body, axis, amplitude, frequency_hz, dt):
+        ax = (C.c_double * 3)(*[float(a) for a in axis])
+        r = lib().or_set_kinematic(self.h, int(body), ax, float(amplitude), float(frequency_hz), float(dt))
+        assert r == 0, "the oracle refused the kinematic body"
 
     def merge_tests(self):
         """Merge / unmerge predicates on the current state, reference order."""

@@ -51,6 +51,43 @@ def test_merging_bit_exact_clumps_in_funnel(gpu_lib):
     assert c["merges"] > 0 and c["unmerges"] > 0, c
 
 
+def test_kinematic_platform_bit_exact(gpu_lib):
+    """The large-scene workload's shaking platform (am_set_kinematic: the
+    pinned platform oscillates vertically, 2 Hz, 0.05 m; sleeping off so no
+    clump rests asleep on it): 120 clumps poured onto it, merging on, stay
+    bit-exact with the oracle's restatement (checked every 10 steps over 1400
+    steps), and the platform's contacts carry its prescribed velocity into the
+    solve."""
+    from adaptivemerging_gb300 import native
+    sc = scenes.funnel_clumps(120, seed=5)
+    P = params(enable_merging=1, enable_sleeping=0, friction=0.7, iterations=60)
+    g = native.System(sc, P)
+    o = Oracle(sc, P)
+    pb = scenes.FUNNEL_PLATFORM
+    dt = 0.002
+    g.set_kinematic(pb, (0, 1, 0), 0.05, 2.0, dt)
+    o.set_kinematic(pb, (0, 1, 0), 0.05, 2.0, dt)
+    on_platform = 0
+    for s in range(1400):
+        g.step(dt)
+        o.step(dt)
+        if s % 10 == 9 or s == 1399:
+            tg, to = g.topology(), o.topology()
+            assert tg == to, f"step {s}: topology differs"
+            cg = g.contacts()
+            msg = compare_contacts(cg, o.contacts())
+            assert msg is None, f"step {s}: {msg}"
+            msg = compare_bodies(g.bodies(), o.bodies())
+            assert msg is None, f"step {s}: {msg}"
+            on_platform = max(on_platform, int(np.sum((cg["body1"] == pb) | (cg["body2"] == pb))))
+    c = o.counters()
+    pg = g.perf()
+    assert (pg.merge_events, pg.unmerge_events) == (c["merges"], c["unmerges"])
+    assert on_platform > 0, "no clump reached the platform"
+    vy = g.bodies()["v"][pb][1]
+    assert vy != 0.0
+
+
 @pytest.mark.parametrize("name", list(CASES))
 def test_merging_bit_exact(gpu_lib, name):
     from adaptivemerging_gb300 import native
