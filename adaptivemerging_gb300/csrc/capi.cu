@@ -57,13 +57,29 @@ int Ctx::putBodies(const am_body_state* in) {
         if (in->v) cudaMemcpyAsync(B.v, in->v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, stream);
         if (in->omega) cudaMemcpyAsync(B.w, in->omega, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, stream);
     } else {
-        for (int i = 0; i < n; i++) {
-            if (host.parent[i] >= 0) continue;
-            if (in->x) cudaMemcpyAsync(B.x + 3 * i, in->x + 3 * i, sizeof(double) * 3, cudaMemcpyHostToDevice, stream);
-            if (in->R) cudaMemcpyAsync(B.R + 9 * i, in->R + 9 * i, sizeof(double) * 9, cudaMemcpyHostToDevice, stream);
-            if (in->v) cudaMemcpyAsync(B.v + 3 * i, in->v + 3 * i, sizeof(double) * 3, cudaMemcpyHostToDevice, stream);
-            if (in->omega) cudaMemcpyAsync(B.w + 3 * i, in->omega + 3 * i, sizeof(double) * 3, cudaMemcpyHostToDevice, stream);
+        // bodies inside collections keep the state their collection gives
+        // them: the whole arrays go to a staging buffer and one kernel copies
+        // the free bodies' rows
+        if (putStageCap < 18 * (size_t)n) {
+            if (alloc(&putStage, 18 * (size_t)n)) return AM_E_CUDA;
+            putStageCap = 18 * (size_t)n;
         }
+        if (!putParent) {
+            if (alloc(&putParent, (size_t)n)) return AM_E_CUDA;
+        }
+        cudaMemcpyAsync(putParent, host.parent.data(), sizeof(int) * n, cudaMemcpyHostToDevice, stream);
+        double* st[4] = {nullptr, nullptr, nullptr, nullptr};
+        const double* src[4] = {in->x, in->R, in->v, in->omega};
+        const int w[4] = {3, 9, 3, 3};
+        size_t off = 0;
+        for (int k = 0; k < 4; k++) {
+            if (src[k]) {
+                st[k] = putStage + off;
+                cudaMemcpyAsync(st[k], src[k], sizeof(double) * w[k] * n, cudaMemcpyHostToDevice, stream);
+            }
+            off += (size_t)w[k] * n;
+        }
+        launch_put_free(B, n, putParent, st[0], st[1], st[2], st[3], stream);
     }
     if (in->R) launch_refresh_inertia(B, n, stream);
     return syncErr();

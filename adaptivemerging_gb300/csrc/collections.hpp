@@ -212,6 +212,9 @@ struct Ctx {
     int* mixG = nullptr;      // AM_ORDER_MIXED: group records, 4 ints per coloured group
     int mixFCap = 0, mixUCap = 0, mixGCap = 0;
     int mixedForm = -1, mixedRefine = 0;   // am_set_mixed_form
+    double* putStage = nullptr;            // am_put_bodies with collections: staged arrays
+    int* putParent = nullptr;              // ... and the collection of every scene body
+    size_t putStageCap = 0;
     int mixedLastForm = -1;                // form of the last mixed solve
     int nScene = 0, ntop = 0, nContacts = 0, nPrev = 0, nPairs = 0;
     int totalSteps = 0;
@@ -501,6 +504,8 @@ int Ctx::alloc(T** p, size_t n) {
     return AM_OK;
 }
 
+void launch_put_free(const DBodies& B, int n, const int* parent, const double* x, const double* R, const double* v,
+                     const double* w, cudaStream_t s);
 const void* pgs_fast_kernel();
 const void* pgs_mixed_kernel();
 const void* gs_levels_kernel();

@@ -344,6 +344,9 @@ void Ctx::release() {
     mixF = mixU = nullptr;
     mixG = nullptr;
     mixFCap = mixUCap = mixGCap = 0;
+    putStage = nullptr;
+    putParent = nullptr;
+    putStageCap = 0;
     levOrder = levOff = nullptr;
     levCap = 0;
     idxA = idxB = nullptr;
@@ -627,6 +630,28 @@ __global__ void k_set_kin(DBodies B, KinSet K) {
         B.x[3 * b + k] = K.x[i][k];
         B.v[3 * b + k] = K.v[i][k];
     }
+}
+
+// am_put_bodies with collections: rows of free bodies (parent < 0) from the
+// staged arrays (any of them may be absent)
+__global__ void k_put_free(DBodies B, int n, const int* parent, const double* x, const double* R, const double* v,
+                           const double* w) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || parent[i] >= 0) return;
+    for (int k = 0; k < 3; k++) {
+        if (x) B.x[3 * i + k] = x[3 * i + k];
+        if (v) B.v[3 * i + k] = v[3 * i + k];
+        if (w) B.w[3 * i + k] = w[3 * i + k];
+    }
+    if (R)
+        for (int k = 0; k < 9; k++) B.R[9 * i + k] = R[9 * i + k];
+}
+
+void launch_put_free(const DBodies& B, int n, const int* parent, const double* x, const double* R, const double* v,
+                     const double* w, cudaStream_t s) {
+    if (n <= 0) return;
+    k_put_free<<<(n + 255) / 256, 256, 0, s>>>(B, n, parent, x, R, v, w);
+    AM_LAUNCHED(1);
 }
 
 void Ctx::applyKinematic() {

@@ -267,6 +267,7 @@ def cpu_baseline(name, max_seconds=15.0, warmup=20, steps=10, n_scenes=BATCH_SCE
         return {"value": v, "unit": "scene-steps/s", "cores": 1, "kind": "port", "sample": desc}
     P.solver_order = abi.AM_ORDER_REFERENCE
     o = Oracle(sc, P)
+    gpu_warmup = warmup
     if name == "funnel":
         # the oracle's all-pairs broad phase makes the pour's warm-up too long
         # for a bounded sample: it times the first steps instead
@@ -279,9 +280,10 @@ def cpu_baseline(name, max_seconds=15.0, warmup=20, steps=10, n_scenes=BATCH_SCE
         o.step(dt)
         n += 1
     el = time.perf_counter() - t0
+    gpu_window = f"{gpu_warmup + 1}..{gpu_warmup + steps}"
     return {"value": n / el, "unit": "steps/s", "cores": 1, "kind": "port",
             "sample": f"steps {warmup + 1}..{warmup + n} of the same scene (the GPU arm times steps "
-                      f"{warmup + 1}..{warmup + steps}), {el:.1f} s, single thread, reference order"}
+                      f"{gpu_window}), {el:.1f} s, single thread, reference order"}
 
 
 _BARRIER = None

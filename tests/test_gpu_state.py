@@ -95,3 +95,32 @@ def test_snapshot_refusals(gpu_lib):
     g.step(0.01)
     same.step(0.01)
     assert np.array_equal(g.bodies()["x"], same.bodies()["x"])
+
+
+def test_put_bodies_with_collections_round_trip(gpu_lib):
+    """am_put_bodies while collections exist: writing back the state just read
+    changes nothing (the members keep the state their collection gives them),
+    and a changed free body's velocity is applied."""
+    from adaptivemerging_gb300 import abi, native
+    sc = scenes.wall(cols=8, rows=6, seed=13)
+    P = params(enable_merging=1, friction=0.5, iterations=80)
+    g = native.System(sc, P)
+    h = native.System(sc, P)
+    g.step(0.005, 97)
+    h.step(0.005, 97)
+    assert any(isinstance(t, tuple) for t in h.topology()), "no collection"
+    st = abi.BodyState(h.n)
+    h.get_bodies_struct(st.struct())
+    h.put_bodies_struct(st.struct())
+    for _ in range(20):
+        g.step(0.005)
+        h.step(0.005)
+    assert np.array_equal(g.bodies()["x"], h.bodies()["x"])
+    assert np.array_equal(g.bodies()["v"], h.bodies()["v"])
+    free = [t for t in h.topology() if not isinstance(t, tuple) and sc.a["pinned"][t] == 0]
+    assert free
+    st = abi.BodyState(h.n)
+    h.get_bodies_struct(st.struct())
+    st.v.reshape(-1, 3)[free[0], 0] += 1.0
+    h.put_bodies_struct(st.struct())
+    assert h.bodies()["v"][free[0], 0] == g.bodies()["v"][free[0], 0] + 1.0
