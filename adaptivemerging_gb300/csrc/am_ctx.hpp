@@ -103,7 +103,8 @@ struct Scratch {
     int cap_int;
     int* tmp;        // scan input scratch
     int* tmp2;       // scan output scratch
-    int* block;      // block sums
+    int* block;      // block sums: cap_int / 1024 + 2 first-level sums, then 1024 second-level ones
+    int cap_block;
 };
 
 // device-side counters and flags (one struct in device memory)
@@ -143,6 +144,8 @@ void launch_pair_order(const DBodies& B, DPairs& P, int n, int* cls, cudaStream_
 int launch_broadphase(const DBodies& B, const DNodes& N, const int* top, int ntop, int* candA, int* candB,
                       int candCap, int* rowCount, int* rowOff, Scratch& sc, DCount* dc, cudaStream_t s,
                       const int* topEnd = nullptr, unsigned* masks = nullptr, int mw = 0);
+// FP32 bounding centre and radius of the members of collections (DBodies::bc)
+void launch_broad_pack_subs(const DBodies& B, const DNodes& N, const int* subIds, int nsub, cudaStream_t s);
 void launch_expand_pairs(const DBodies& B, const int* sub_off, const int* sub_ids, const int* candA,
                          const int* candB, int ncand, DPairs& P, Scratch& sc, DCount* dc, cudaStream_t s);
 void launch_narrow(const DBodies& B, const DNodes& N, DPairs& P, DContacts& C, Scratch& sc, DCount* dc,

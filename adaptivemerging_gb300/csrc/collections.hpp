@@ -204,6 +204,7 @@ struct Ctx {
     int coopBlocks = 0;
     std::vector<int> hColOff;    // colour offsets of the coloured full solve (host copy)
     int* hColPin = nullptr;      // pinned staging of the colour offsets (MAXC + 1)
+    int nSubIds = 0;             // entries of subIds (members of all collections)
     double* Mj = nullptr;     // coloured sweep: M^-1 J^T per row and lane (36 per contact)
     double* invD = nullptr;   // coloured sweep constants per contact: 1/(D + c), A, q per row, couplings, mu
     int mjCap = 0;

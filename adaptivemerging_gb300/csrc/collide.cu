@@ -80,11 +80,19 @@ void launch_scan(const int* in, int* out, int n, Scratch& sc, int* total, cudaSt
         return;
     }
     int nb = (n + SCAN_B - 1) / SCAN_B;
-    // nb <= SCAN_B is guaranteed by the callers' capacities (n <= 2^20)
     k_scan_block<<<nb, SCAN_T, 0, s>>>(in, out, n, sc.block);
     AM_LAUNCHED(1);
-    k_scan_sums<<<1, SCAN_T, 0, s>>>(sc.block, nb, total);
-    AM_LAUNCHED(1);
+    if (nb <= SCAN_B) {
+        k_scan_sums<<<1, SCAN_T, 0, s>>>(sc.block, nb, total);
+        AM_LAUNCHED(1);
+    } else {   // more than 2^20 entries: the block sums are scanned in the same way, in place
+        const int nb2 = (nb + SCAN_B - 1) / SCAN_B;   // <= SCAN_B for n <= 2^30
+        int* b2 = sc.block + sc.cap_block - SCAN_B;
+        k_scan_block<<<nb2, SCAN_T, 0, s>>>(sc.block, sc.block, nb, b2);
+        k_scan_sums<<<1, SCAN_T, 0, s>>>(b2, nb2, total);
+        k_scan_add<<<nb2, SCAN_T, 0, s>>>(sc.block, nb, b2);
+        AM_LAUNCHED(3);
+    }
     if (nb > 1) { k_scan_add<<<nb, SCAN_T, 0, s>>>(out, n, sc.block); AM_LAUNCHED(1); }
 }
 
@@ -168,6 +176,31 @@ __global__ void k_broad_pack(DBodies B, DNodes N, const int* top, int ntop) {
         }
     }
     B.bc[a] = c;
+}
+
+// the same bounds for the bodies inside collections (their own box or tree;
+// the expansion of a collection's candidates tests its members with them)
+__global__ void k_broad_pack_subs(DBodies B, DNodes N, const int* subIds, int nsub) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsub) return;
+    int a = subIds[i];
+    int t = B.type[a];
+    float4 c = make_float4(0.f, 0.f, 0.f, -1.f);
+    if (t == AM_BOX) {
+        v3 x = bodyX(B, a);
+        c = make_float4((float)x.x, (float)x.y, (float)x.z, (float)B.radius[a]);
+    } else if (t != AM_PLANE && B.root[a] >= 0) {
+        int r0 = B.root[a];
+        v3 x = ldv(N.cW + 3 * r0);
+        c = make_float4((float)x.x, (float)x.y, (float)x.z, (float)N.r[r0]);
+    }
+    B.bc[a] = c;
+}
+
+void launch_broad_pack_subs(const DBodies& B, const DNodes& N, const int* subIds, int nsub, cudaStream_t s) {
+    if (nsub <= 0) return;
+    k_broad_pack_subs<<<(nsub + 255) / 256, 256, 0, s>>>(B, N, subIds, nsub);
+    AM_LAUNCHED(1);
 }
 
 // True only when the FP32 distance proves the centres farther apart than the
@@ -282,30 +315,59 @@ __device__ __forceinline__ int subat(const DBodies& B, const int* so, const int*
     return (B.flags[x] & F_COLLECTION) ? si[so[x] + k] : x;
 }
 
-__global__ void k_expand_count(DBodies B, const int* so, const int* candA, const int* candB, const DCount* dc,
-                               int* cnt) {
+// A member pair of a collection's candidate is kept unless the FP32 bounds
+// prove it apart (the first test of every collider would reject it: the
+// broad phase's far_apart32 margin), so the kept pairs are the pairs that
+// can touch, in the reference's order; a collection of m members then costs
+// its touching member pairs instead of m times every body it may meet.
+__device__ __forceinline__ bool sub_pair_kept(const DBodies& B, int a, int b) {
+    const float4 ca = B.bc[a], cb = B.bc[b];
+    return !(ca.w >= 0.f && cb.w >= 0.f && far_apart32(ca, cb));
+}
+
+__global__ void k_expand_count(DBodies B, const int* so, const int* si, const int* candA, const int* candB,
+                               const DCount* dc, int* cnt) {
     int n = dc->n_cand;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        cnt[i] = nsub(B, so, candA[i]) * nsub(B, so, candB[i]);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int A = candA[i], Bb = candB[i];
+        const int na = nsub(B, so, A), nb = nsub(B, so, Bb);
+        if (na == 1 && nb == 1) { cnt[i] = 1; continue; }
+        int k = 0;
+        for (int p = 0; p < na; p++) {
+            const int a = subat(B, so, si, A, p);
+            for (int q = 0; q < nb; q++) k += sub_pair_kept(B, a, subat(B, so, si, Bb, q)) ? 1 : 0;
+        }
+        cnt[i] = k;
+    }
 }
 
 __global__ void k_expand_write(DBodies B, const int* so, const int* si, const int* candA, const int* candB,
                                const DCount* dc, const int* off, DPairs P) {
     int n = dc->n_cand;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int A = candA[i], Bb = candB[i];
-        int na = nsub(B, so, A), nb = nsub(B, so, Bb);
+        const int A = candA[i], Bb = candB[i];
+        const int na = nsub(B, so, A), nb = nsub(B, so, Bb);
         int o = off[i];
-        for (int p = 0; p < na; p++)
-            for (int q = 0; q < nb; q++, o++)
-                if (o < P.cap) { P.a[o] = subat(B, so, si, A, p); P.b[o] = subat(B, so, si, Bb, q); }
+        if (na == 1 && nb == 1) {
+            if (o < P.cap) { P.a[o] = A; P.b[o] = Bb; }
+            continue;
+        }
+        for (int p = 0; p < na; p++) {
+            const int a = subat(B, so, si, A, p);
+            for (int q = 0; q < nb; q++) {
+                const int b = subat(B, so, si, Bb, q);
+                if (!sub_pair_kept(B, a, b)) continue;
+                if (o < P.cap) { P.a[o] = a; P.b[o] = b; }
+                o++;
+            }
+        }
     }
 }
 
 void launch_expand_pairs(const DBodies& B, const int* sub_off, const int* sub_ids, const int* candA,
                          const int* candB, int ncand, DPairs& P, Scratch& sc, DCount* dc, cudaStream_t s) {
     if (ncand <= 0) { cudaMemsetAsync(&dc->n_pairs, 0, sizeof(int), s); return; }
-    k_expand_count<<<(ncand + 255) / 256, 256, 0, s>>>(B, sub_off, candA, candB, dc, sc.tmp);
+    k_expand_count<<<(ncand + 255) / 256, 256, 0, s>>>(B, sub_off, sub_ids, candA, candB, dc, sc.tmp);
     AM_LAUNCHED(1);
     launch_scan(sc.tmp, sc.tmp2, ncand, sc, &dc->n_pairs, s);
     k_expand_write<<<(ncand + 255) / 256, 256, 0, s>>>(B, sub_off, sub_ids, candA, candB, dc, sc.tmp2, P);

@@ -408,7 +408,9 @@ int Ctx::ensureScratch(int need) {
     int cap = std::max(need + need / 2, 4096);
     Scratch s;
     s.cap_int = cap;
-    int r = alloc(&s.tmp, cap) | alloc(&s.tmp2, cap) | alloc(&s.block, 4096);
+    // the scan's two levels of block sums (n up to 2^30; callers scan at most cap entries)
+    s.cap_block = std::max(4096, cap / 1024 + 2 + 1024);
+    int r = alloc(&s.tmp, cap) | alloc(&s.tmp2, cap) | alloc(&s.block, s.cap_block);
     if (r) return AM_E_CUDA;
     SC = s;
     return AM_OK;
@@ -571,6 +573,7 @@ int Ctx::uploadTopology() {
             for (int s : h.subs[b]) si.push_back(s);
     }
     so[h.cap] = (int)si.size();
+    nSubIds = (int)si.size();
     CK(cudaMemcpyAsync(subOff, so.data(), sizeof(int) * (h.cap + 1), cudaMemcpyHostToDevice, stream));
     if (!si.empty())
         CK(cudaMemcpyAsync(subIds, si.data(), sizeof(int) * si.size(), cudaMemcpyHostToDevice, stream));
@@ -710,6 +713,7 @@ int Ctx::collisionDetection() {
             mw = 0;
         }
     }
+    if ((r = ensureScratch(ntop + 1))) return r;   // the rows' scan
     launch_broadphase(B, N, top, ntop, nullptr, nullptr, 0, rowCount, rowOff, SC, dc, stream, topEnd, masks, mw);
     if ((r = readCounts())) return r;
     int ncand = hc->n_cand;
@@ -719,6 +723,7 @@ int Ctx::collisionDetection() {
                           mw);
     }
     if ((r = ensureScratch(ncand + 1))) return r;
+    launch_broad_pack_subs(B, N, subIds, nSubIds, stream);   // bounds of collection members for the expansion
     launch_expand_pairs(B, subOff, subIds, candA, candB, ncand, PR, SC, dc, stream);
     if ((r = readCounts())) return r;
     int npairs = ncand > 0 ? hc->n_pairs : 0;
