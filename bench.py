@@ -70,12 +70,9 @@ FUNNEL_PLATFORM_MOTION = ((0.0, 1.0, 0.0), 0.05, 0.5)   # axis, amplitude (m), f
 
 
 def workload(name, n_scenes=BATCH_SCENES, order=None):
-    # the full-solve order of single scenes: the mixed-precision coloured solve,
-    # except on the funnel, whose jammed frictional pile makes the coloured
-    # orders diverge (measured: both coloured kernels blow up on the 20k-clump
-    # pour where list order stays bounded); there, the reference's list order
+    # the full-solve order of single scenes: the mixed-precision coloured solve
     if order is None:
-        order = "reference" if name == "funnel" else "mixed"
+        order = "mixed"
     """Scene (or list of scenes), parameters, dt and a description of the named
     workload.  `n_scenes` shrinks the batch for profiling runs only; the
     benchmark figure is the 512-bin batch."""
