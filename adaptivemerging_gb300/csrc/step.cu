@@ -723,17 +723,25 @@ int Ctx::collisionDetection() {
                           mw);
     }
     if ((r = ensureScratch(ncand + 1))) return r;
-    launch_broad_pack_subs(B, N, subIds, nSubIds, stream);   // bounds of collection members for the expansion
-    launch_expand_pairs(B, subOff, subIds, candA, candB, ncand, PR, SC, dc, stream);
-    if ((r = readCounts())) return r;
-    int npairs = ncand > 0 ? hc->n_pairs : 0;
-    if (npairs > PR.cap) {
-        if ((r = ensurePairs(npairs))) return r;
+    // the expansion's scan leaves the pair count in dc->n_pairs for the
+    // narrow phase.  Without collections every candidate is one pair, so the
+    // host knows the count without waiting for it
+    int npairs = 0;
+    if (nSubIds == 0) {
+        npairs = ncand;
+        if (npairs > PR.cap && (r = ensurePairs(npairs))) return r;
         launch_expand_pairs(B, subOff, subIds, candA, candB, ncand, PR, SC, dc, stream);
+    } else {
+        launch_broad_pack_subs(B, N, subIds, nSubIds, stream);   // bounds of collection members for the expansion
+        launch_expand_pairs(B, subOff, subIds, candA, candB, ncand, PR, SC, dc, stream);
+        if ((r = readCounts())) return r;
+        npairs = ncand > 0 ? hc->n_pairs : 0;
+        if (npairs > PR.cap) {
+            if ((r = ensurePairs(npairs))) return r;
+            launch_expand_pairs(B, subOff, subIds, candA, candB, ncand, PR, SC, dc, stream);
+        }
     }
     nPairs = npairs;
-    cudaMemsetAsync(&dc->n_pairs, 0, sizeof(int), stream);
-    cudaMemcpyAsync(&dc->n_pairs, &nPairs, sizeof(int), cudaMemcpyHostToDevice, stream);
     // staged narrow phase (colliders run once) when no pair can exceed the
     // staging slots and the staging fits 512 MB; otherwise count, then emit
     double* sd = nullptr;
