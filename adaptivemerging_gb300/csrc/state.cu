@@ -303,6 +303,7 @@ int Ctx::putState(const uint8_t* in, size_t size) {
     }
     so[cap] = (int)si.size();
     if (si.size() > cap) { err = "malformed snapshot (collection members)"; return AM_E_ARG; }
+    nSubIds = (int)si.size();
     cudaMemcpyAsync(subOff, so.data(), sizeof(int) * (cap + 1), cudaMemcpyHostToDevice, stream);
     if (!si.empty()) cudaMemcpyAsync(subIds, si.data(), sizeof(int) * si.size(), cudaMemcpyHostToDevice, stream);
     return syncErr();
