@@ -768,7 +768,12 @@ __device__ void box_box(const DBodies& B, int b1, int b2, E& emit) {
 
 // Sphere-tree traversals with an explicit stack (children pushed in reverse
 // so they pop in index order, matching the recursive reference).
-static const int STACK = 96;
+// Depth-first traversal stacks of the tree colliders.  A stack holds, for
+// each descent on the current path, the siblings still to visit, so it needs
+// at most (descents on a path) x (largest child count - 1) + 1 entries: for
+// two trees of depth 3 whose nodes have up to 30 children (the reference's
+// .sph hierarchies), 6 x 29 + 1 = 175.  A deeper need raises AM_E_CAPACITY.
+static const int STACK = 192;
 
 // collideSphereTreeAndPlane (CollisionProcessor.java:793-826); tree body is body 1
 template <class E>

@@ -4,7 +4,12 @@ The supported subset is what the contact path simulates:
 - ``<body type="box">`` with ``dim``, optional ``density`` (1) and ``scale``
   (XMLParser.java:360-397);
 - ``<body type="sphere">`` with ``r`` and optional ``density`` (:420-447);
-- ``<body type="plane">`` with ``p`` and ``n``, always pinned (:405-416).
+- ``<body type="plane">`` with ``p`` and ``n``, always pinned (:405-416);
+- ``<body type="mesh">`` with ``obj``, ``st``, ``scale`` and optional
+  ``density`` (createMesh, :449-539): mass, centre of mass and inertia of the
+  scaled triangle soup, and the sphere tree of the ``.sph`` file, scaled and
+  moved to the centre of mass.  The mesh itself only draws; the sphere tree
+  is what collides.
 
 Each body may carry the child elements ``x``, ``R`` (axis x y z and angle),
 ``v``, ``omega``, ``friction``, ``restitution`` and ``pinned``
@@ -15,11 +20,13 @@ The ``<collision>`` element sets ``iterations``, ``feedbackStiffness``,
 ``enableCompliance``, and ``restitution`` / ``friction``. The last two also
 switch the corresponding override on, as the reference does (:100-137).
 
-Composite and mesh bodies, springs and spinners are not part of this
-implementation. They raise ``NotSupported`` instead of being skipped, so a
+Composite bodies, springs and spinners are not part of this implementation. They raise ``NotSupported`` instead of being skipped, so a
 scene never loads silently different from the reference.
 """
+import os
 import xml.etree.ElementTree as ET
+
+import numpy as np
 
 from . import abi
 from .scenes import IDENT, Builder, axis_angle
@@ -66,10 +73,91 @@ def _common(el):
     return out
 
 
-def load(source, params=None):
+def read_obj(path):
+    """Vertices and faces of a Wavefront OBJ file as PolygonSoup reads it
+    (tools/moments/PolygonSoup.java:40-115): ``v x y z`` lines, and ``f``
+    lines whose tokens start with a 1-based vertex index (texture and normal
+    indices after a slash are ignored)."""
+    verts, faces = [], []
+    with open(path) as f:
+        for line in f:
+            if line.startswith("v "):
+                t = line.split()
+                verts.append((float(t[1]), float(t[2]), float(t[3])))
+            elif line.startswith("f "):
+                faces.append([int(tok.split("/")[0]) - 1 for tok in line[2:].split()])
+    return np.array(verts, float).reshape(-1, 3), faces
+
+
+def mesh_mass_properties(verts, faces, density):
+    """Mass, centre of mass and inertia about it (VolInt.computeMassProperties,
+    tools/moments/VolInt.java:316-380), from the volume integrals of the
+    closed triangle soup that getPolyhedron builds from the first three
+    vertices of every face (PolygonSoup.java:157-166).  The integrals T0, T1,
+    T2 and TP are Mirtich's (1996); here they are summed over the signed
+    tetrahedra spanned by the origin and each triangle, which gives the same
+    values up to rounding.  As the reference does, an inside-out soup (negative
+    mass) gets its mass negated and nothing else."""
+    tri = np.array([f[:3] for f in faces], int)
+    a, b, c = verts[tri[:, 0]], verts[tri[:, 1]], verts[tri[:, 2]]
+    d = np.einsum("ij,ij->i", a, np.cross(b, c))          # 6 x signed volume
+    S = a + b + c
+    T0 = d.sum() / 6.0
+    T1 = (d[:, None] * S).sum(0) / 24.0
+    # integral of x_i x_j over the tetrahedron (0, a, b, c): d/120 (sum of v_i v_j over a, b, c + S_i S_j)
+    Q = (np.einsum("k,ki,kj->ij", d, a, a) + np.einsum("k,ki,kj->ij", d, b, b) + np.einsum("k,ki,kj->ij", d, c, c)
+         + np.einsum("k,ki,kj->ij", d, S, S)) / 120.0
+    T2 = np.diag(Q)
+    TP = np.array([Q[0, 1], Q[1, 2], Q[2, 0]])
+    mass = density * T0
+    r = T1 / T0
+    J = np.zeros((3, 3))
+    J[0, 0] = density * (T2[1] + T2[2])
+    J[1, 1] = density * (T2[2] + T2[0])
+    J[2, 2] = density * (T2[0] + T2[1])
+    J[0, 1] = J[1, 0] = -density * TP[0]
+    J[1, 2] = J[2, 1] = -density * TP[1]
+    J[2, 0] = J[0, 2] = -density * TP[2]
+    J[0, 0] -= mass * (r[1] * r[1] + r[2] * r[2])
+    J[1, 1] -= mass * (r[2] * r[2] + r[0] * r[0])
+    J[2, 2] -= mass * (r[0] * r[0] + r[1] * r[1])
+    J[0, 1] = J[1, 0] = J[0, 1] + mass * r[0] * r[1]
+    J[1, 2] = J[2, 1] = J[1, 2] + mass * r[1] * r[2]
+    J[2, 0] = J[0, 2] = J[2, 0] + mass * r[2] * r[0]
+    if mass < 0:
+        mass = -mass
+    return float(mass), r, J
+
+
+def read_sphere_tree(path):
+    """A ``.sph`` sphere tree as createMesh reads it (XMLParser.java:499-534):
+    the number of spheres, one ``x y z r`` line per sphere, then lines
+    ``parent count child ...`` with 1-based indices.  Sphere 1 is the root.
+    Returns (centres, radii, children as lists of 0-based indices)."""
+    with open(path) as f:
+        lines = f.read().splitlines()
+    n = int(lines[0].split()[0])
+    cr = np.array([[float(t) for t in lines[1 + k].split()[:4]] for k in range(n)], float).reshape(-1, 4)
+    children = {k: [] for k in range(n)}
+    for line in lines[1 + n:]:
+        t = line.split()
+        if len(t) < 2:
+            break          # the reference's scanner stops at the first line without a parent and a count
+        p, cnt = int(t[0]) - 1, int(t[1])
+        children[p] = [int(q) - 1 for q in t[2:2 + cnt]]
+    return cr[:, :3], cr[:, 3], children
+
+
+def load(source, params=None, data_root=None):
     """Parse an XML scene (a path, or the document text when it starts with
-    '<').  Returns (SceneArrays, am_params, body names in list order)."""
-    root = ET.fromstring(source) if source.lstrip().startswith("<") else ET.parse(source).getroot()
+    '<').  Mesh bodies name their ``obj`` and ``st`` files relative to the
+    reference project's root, which `data_root` gives (default: the parent of
+    the XML file's directory, as for ``scenes3D/*.xml``).  Returns
+    (SceneArrays, am_params, body names in list order)."""
+    text = source.lstrip().startswith("<")
+    root = ET.fromstring(source) if text else ET.parse(source).getroot()
+    if data_root is None and not text:
+        data_root = os.path.dirname(os.path.dirname(os.path.abspath(source)))
     P = params if params is not None else abi.default_params()
     for el in root:
         if el.tag.lower() != "collision":
@@ -109,6 +197,15 @@ def load(source, params=None):
         elif kind == "plane":
             b.plane(tuple(_vec(el.get("p"))), tuple(_vec(el.get("n"))), friction=c["friction"],
                     restitution=c["restitution"])
+        elif kind == "mesh":
+            if data_root is None:
+                raise NotSupported(f"mesh body {name!r}: no data root for its files")
+            scale = float(el.get("scale"))
+            verts, faces = read_obj(os.path.join(data_root, el.get("obj")))
+            mass, com, J = mesh_mass_properties(verts * scale, faces, density)
+            cs, rs, children = read_sphere_tree(os.path.join(data_root, el.get("st")))
+            b.tree(cs * scale - com, rs * scale, children, c["x"], mass, J, R=c["R"], v=c["v"], omega=c["omega"],
+                   friction=c["friction"], restitution=c["restitution"], pinned=c["pinned"])
         else:
             raise NotSupported(f"body type {kind!r} ({name!r})")
         names.append(name)

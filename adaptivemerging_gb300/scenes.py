@@ -97,6 +97,29 @@ class Builder:
                          inertia=list(I.reshape(-1)), friction=friction,
                          restitution=restitution, root=root)
 
+    def tree(self, centres, radii, children, x, mass, inertia, R=IDENT, v=(0, 0, 0), omega=(0, 0, 0),
+             friction=0.8, restitution=0.0, pinned=False):
+        """Sphere-tree body of any depth: node k has centre centres[k] and
+        radius radii[k] in body coordinates and the child nodes children[k]
+        (in their order); node 0 is the root.  The nodes are stored breadth
+        first, so every node's children sit together in that order."""
+        order, pos = [0], {0: 0}
+        for k in order:
+            for q in children[k]:
+                if q not in pos:
+                    pos[q] = len(order)
+                    order.append(q)
+        base = len(self.nodes)
+        for k in order:
+            ch = list(children[k])
+            if [pos[q] for q in ch] != list(range(pos[ch[0]], pos[ch[0]] + len(ch))) if ch else False:
+                raise ValueError("sphere tree: a node is the child of more than one node")
+            c0 = base + pos[ch[0]] if ch else -1
+            self.nodes.append((tuple(float(t) for t in centres[k]), float(radii[k]), c0, len(ch)))
+        return self._add(type=AM_TREE, x=tuple(float(t) for t in x), R=R, v=v, omega=omega, mass=float(mass),
+                         inertia=[float(t) for t in np.asarray(inertia, float).reshape(-1)], friction=friction,
+                         restitution=restitution, root=base, pinned=int(bool(pinned)))
+
     def build(self):
         n = len(self.b)
         f = lambda k, w: np.array([d[k] for d in self.b], float).reshape(n * w)

@@ -7,7 +7,11 @@ Two of the reference's XML scenes, `scenes3D/tower30.xml` (135 boxes in a
 ring tower on a plane) and `scenes3D/denseTower25.xml` (78 boxes), are parsed
 by this repository's loader (adaptivemerging_gb300.scene_xml) and stored as
 the loader's output: the am_scene arrays, the am_params fields the scene sets,
-and the body names.  The reference tree is not present where the GPU tests
+and the body names.  A third, "meshes", is `scenes3D/allBodyTypes.xml`
+without its first body (a platform hung on four springs, which this
+implementation does not model): two boxes, a sphere, a plane and four mesh
+bodies whose sphere trees come from the reference's `data/*.sph` files and
+whose mass properties come from its `data/*.obj` meshes.  The reference tree is not present where the GPU tests
 run, so the tests read this fixture instead of the XML files.  The first rows
 (#bodies, #contacts) of the reference's recorded metrics for tower30
 (`scenes3D/csv/conditional_acceptance_revisions/tower30_merged.csv`) are kept
@@ -16,6 +20,7 @@ beside them as recorded.
 import csv
 import json
 import os
+import re
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -24,6 +29,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from adaptivemerging_gb300 import abi, scene_xml  # noqa: E402
 
 SCENES = ("tower30", "denseTower25")
+MESHES_FROM = "allBodyTypes"
 CSV = "scenes3D/csv/conditional_acceptance_revisions/tower30_merged.csv"
 
 
@@ -35,6 +41,12 @@ def main():
         arrays = {k: v.tolist() for k, v in sc.a.items()}
         prm = {f: getattr(P, f) for f, _ in abi.am_params._fields_}
         out["scenes"][name] = {"arrays": arrays, "params": prm, "names": names}
+    with open(os.path.join(root, "scenes3D", MESHES_FROM + ".xml")) as f:
+        doc = f.read()
+    doc = re.sub(r'<body type="box" name="platform".*?</body>', "", doc, count=1, flags=re.S)
+    sc, P, names = scene_xml.load(doc, data_root=root)
+    out["scenes"]["meshes"] = {"arrays": {k: v.tolist() for k, v in sc.a.items()},
+                               "params": {f: getattr(P, f) for f, _ in abi.am_params._fields_}, "names": names}
     with open(os.path.join(root, CSV)) as f:
         rows = list(csv.reader(f))[1:]
     out["tower30_csv_bodies_contacts"] = [[int(r[0]), int(r[1])] for r in rows[:60] if len(r) > 2]

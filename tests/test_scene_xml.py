@@ -89,3 +89,62 @@ def test_loaded_scene_bit_exact_on_device(gpu_lib):
         o.step(0.01)
         assert compare_contacts(g.contacts(), o.contacts()) is None
         assert compare_bodies(g.bodies(), o.bodies()) is None
+
+
+def _cube_files(tmp_path):
+    """A 1 m cube (vertices 0..1, 12 outward triangles) and a 3-sphere tree."""
+    obj = tmp_path / "cube.obj"
+    v = [(x, y, z) for x in (0, 1) for y in (0, 1) for z in (0, 1)]
+    idx = {p: i + 1 for i, p in enumerate(v)}
+    quads = [((0, 0, 0), (0, 1, 0), (1, 1, 0), (1, 0, 0)), ((0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)),
+             ((0, 0, 0), (1, 0, 0), (1, 0, 1), (0, 0, 1)), ((0, 1, 0), (0, 1, 1), (1, 1, 1), (1, 1, 0)),
+             ((0, 0, 0), (0, 0, 1), (0, 1, 1), (0, 1, 0)), ((1, 0, 0), (1, 1, 0), (1, 1, 1), (1, 0, 1))]
+    lines = [f"v {x} {y} {z}" for x, y, z in v]
+    for q in quads:
+        a, b, c, d = (idx[p] for p in q)
+        lines += [f"f {a}/1/1 {b}/1/1 {c}/1/1", f"f {a} {c} {d}"]
+    obj.write_text("\n".join(lines) + "\n")
+    sph = tmp_path / "cube.sph"
+    sph.write_text("3\n0.5 0.5 0.5 0.9\n0.5 0.5 0.25 0.45\n0.5 0.5 0.75 0.45\n1 2 2 3\n")
+    return obj, sph
+
+
+def test_mesh_body_mass_properties_and_tree(tmp_path):
+    """createMesh (XMLParser.java:449-539): a cube soup scaled by 2 at
+    density 3 has mass 24, its centre of mass at (1, 1, 1) and inertia
+    m (2^2 + 2^2) / 12 = 16 about each axis; the sphere tree is scaled and
+    moved to the centre of mass, the root first and its two children after
+    it in file order."""
+    obj, sph = _cube_files(tmp_path)
+    doc = (f'<root><body type="mesh" name="cube" scale="2" density="3" obj="{obj.name}" st="{sph.name}">'
+           f'<x>0 5 0</x></body></root>')
+    sc, _, names = scene_xml.load(doc, data_root=str(tmp_path))
+    a = sc.a
+    assert names == ["cube"] and a["type"][0] == abi.AM_TREE
+    assert abs(a["mass"][0] - 24.0) < 1e-12
+    I = np.asarray(a["inertia"][:9]).reshape(3, 3)
+    assert np.allclose(I, 16.0 * np.eye(3), atol=1e-12)
+    r0 = a["body_root"][0]
+    assert a["node_child0"][r0] == r0 + 1 and a["node_nchild"][r0] == 2
+    c = np.asarray(a["node_c"]).reshape(-1, 3)
+    assert np.allclose(c[r0], 0.0) and np.allclose(c[r0 + 1], (0, 0, -0.5)) and np.allclose(c[r0 + 2], (0, 0, 0.5))
+    assert np.allclose(np.asarray(a["node_r"])[r0:r0 + 3], (1.8, 0.9, 0.9))
+
+
+def test_mesh_body_settles_on_oracle(tmp_path):
+    """The cube mesh body dropped on a plane lands on its sphere tree's leaves
+    in the oracle and comes to rest on them."""
+    from oracle_binding import Oracle
+    obj, sph = _cube_files(tmp_path)
+    doc = (f'<root><body type="mesh" name="cube" scale="1" density="1000" obj="{obj.name}" st="{sph.name}">'
+           f'<x>0 1 0</x></body><body type="plane" name="floor" p="0 0 0" n="0 1 0"/></root>')
+    sc, P, _ = scene_xml.load(doc, data_root=str(tmp_path))
+    o = Oracle(sc, P)
+    most = 0
+    for _ in range(300):
+        o.step(0.01)
+        most = max(most, o.num_contacts())
+    b = o.bodies()
+    assert most > 0
+    assert abs(b["v"][0]).max() < 1e-2
+    assert 0.4 < b["x"][0][1] < 0.46         # resting on the leaves (r 0.45, at the centre's height)
