@@ -14,8 +14,9 @@ bodies whose sphere trees come from the reference's `data/*.sph` files and
 whose mass properties come from its `data/*.obj` meshes.  The reference tree is not present where the GPU tests
 run, so the tests read this fixture instead of the XML files.  The first rows
 (#bodies, #contacts) of the reference's recorded metrics for tower30
-(`scenes3D/csv/conditional_acceptance_revisions/tower30_merged.csv`) are kept
-beside them as recorded.
+(`scenes3D/csv/conditional_acceptance_revisions/tower30_merged.csv`, and an
+earlier run's `scenes3D/csv/old/tower30_merged.csv`) are kept beside them as
+recorded.
 """
 import csv
 import json
@@ -31,6 +32,7 @@ from adaptivemerging_gb300 import abi, scene_xml  # noqa: E402
 SCENES = ("tower30", "denseTower25")
 MESHES_FROM = "allBodyTypes"
 CSV = "scenes3D/csv/conditional_acceptance_revisions/tower30_merged.csv"
+CSV_OLD = "scenes3D/csv/old/tower30_merged.csv"
 
 
 def main():
@@ -50,6 +52,9 @@ def main():
     with open(os.path.join(root, CSV)) as f:
         rows = list(csv.reader(f))[1:]
     out["tower30_csv_bodies_contacts"] = [[int(r[0]), int(r[1])] for r in rows[:60] if len(r) > 2]
+    with open(os.path.join(root, CSV_OLD)) as f:
+        rows = list(csv.reader(f))[1:]
+    out["tower30_old_csv_bodies_contacts"] = [[int(r[0]), int(r[1])] for r in rows[:20] if len(r) > 2]
     with open(os.path.join(HERE, "reference_scenes.json"), "w") as f:
         json.dump(out, f, separators=(",", ":"))
 
