@@ -491,6 +491,7 @@ int Ctx::setKinematic(int body, const double* axis, double amp, double freq, dou
     if (body < 0 || body >= nScene || !axis || !(amp >= 0) || !(freq >= 0) || !(dt > 0) || !std::isfinite(amp) ||
         !std::isfinite(freq) || !std::isfinite(dt)) { err = "bad kinematic body"; return AM_E_ARG; }
     if (!(host.flags[body] & F_PINNED)) { err = "a kinematic body must be pinned"; return AM_E_ARG; }
+    if (host.parent[body] >= 0) { err = "a kinematic body cannot be inside a collection"; return AM_E_STATE; }
     for (size_t i = 0; i < kin.size(); i++)
         if (kin[i].body == body) { kin.erase(kin.begin() + i); break; }
     if (amp == 0) return AM_OK;

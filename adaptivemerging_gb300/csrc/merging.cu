@@ -871,6 +871,13 @@ static void listRemove(std::vector<int>& v, int b) {
 
 bool Ctx::checkMergeCondition(int p) {             // BodyPairContact.java:151-224
     HBPC& q = M.bpc[p];
+    // A body with a prescribed motion (am_set_kinematic) never merges: a
+    // collection that holds a pinned body stays put, so the motion would stop
+    // acting on the body's contacts while it moved through the members merged
+    // with it.  The reference's pinned bodies never move; this is the only
+    // addition to its test.
+    for (const Kinematic& k : kin)
+        if (k.body == q.a || k.body == q.b) return false;
     if (sleeping(host, q.a) && sleeping(host, q.b)) return true;
     if (P.enable_merge_let_it_breathe)
         for (int ref : q.list) {

@@ -379,7 +379,11 @@ int32_t am_set_residual_target(void* ctx, double residual_target, int32_t check_
  * w = 2 pi frequency_hz, x0 its position at this call; its orientation is
  * unchanged.  The body must be pinned (AM_E_ARG otherwise); amplitude 0 removes
  * it; at most 8 per context (AM_E_CAPACITY); single scenes only (AM_E_STATE
- * for a batch).  Setting any body restarts the count n of every one. */
+ * for a batch).  Setting any body restarts the count n of every one.  A
+ * kinematic body never merges (its pairs fail the merge test, the one
+ * addition to BodyPairContact.checkMergeCondition): a collection holding a
+ * pinned body stays put, so the motion would stop acting on its contacts.  A
+ * body already inside a collection is refused (AM_E_STATE). */
 int32_t am_set_kinematic(void* ctx, int32_t body, const double* axis, double amplitude, double frequency_hz,
                          double dt);
 /* AM_ORDER_MIXED: the form of the solve kernel (-1, default: chosen per

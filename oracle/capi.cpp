@@ -143,12 +143,14 @@ int or_top_ids(void* h, int32_t* out, int cap) {
 
 int or_set_kinematic(void* h, int body, const double* axis, double amp, double freq, double dt) {
     World* w = (World*)h;
-    if (body < 0 || body >= w->nScene || !w->bodies[body]->pinned) return -1;
+    if (body < 0 || body >= w->nScene) return -1;
+    Body* b = &w->store[body];   // scene bodies by id (the top-level list changes with merges)
+    if (!b->pinned || b->parent) return -1;
     for (size_t i = 0; i < w->kin.size(); i++)
-        if (w->kin[i].body == w->bodies[body]) { w->kin.erase(w->kin.begin() + i); break; }
+        if (w->kin[i].body == b) { w->kin.erase(w->kin.begin() + i); break; }
     if (amp == 0) return 0;
     World::Kinematic q;
-    q.body = w->bodies[body];
+    q.body = b;
     q.x0[0] = q.body->x.x; q.x0[1] = q.body->x.y; q.x0[2] = q.body->x.z;
     for (int k = 0; k < 3; k++) q.axis[k] = axis[k];
     q.amp = amp;

@@ -1431,7 +1431,19 @@ void World::collUpdateBodiesPositions(Body* c) {   // updateBodiesPositionAndTra
 
 // ---------------------------------------------------------------------------
 // Merging (Merging.java:73-163, 215-393)
-static bool checkMergeCondition(const am_params& P, BPC* p) {   // BodyPairContact.java:151-177
+// A body with a prescribed motion never merges: a collection that holds a
+// pinned body stays put, so the body's motion would stop acting on its
+// contacts while it moved through the members merged with it.  The
+// reference's pinned bodies never move, and this test is the only addition.
+static bool kinematicPair(const std::vector<World::Kinematic>& kin, const BPC* p) {
+    for (const World::Kinematic& q : kin)
+        if (q.body == p->body1 || q.body == p->body2) return true;
+    return false;
+}
+
+static bool checkMergeCondition(const am_params& P, const std::vector<World::Kinematic>& kin,
+                                BPC* p) {   // BodyPairContact.java:151-177
+    if (kinematicPair(kin, p)) return false;
     if (p->body1->sleeping && p->body2->sleeping) return true;
     if (P.enable_merge_let_it_breathe)
         for (Contact* c : p->contactList)
@@ -1449,7 +1461,7 @@ static bool checkMergeCondition(const am_params& P, BPC* p) {   // BodyPairConta
     return true;
 }
 
-bool World::mergeTest(BPC* p) const { return checkMergeCondition(P, p); }
+bool World::mergeTest(BPC* p) const { return checkMergeCondition(P, kin, p); }
 
 bool World::unmergeTest(BPC* p) const {   // the selection in Merging.unmerge (:222-240)
     for (Contact* c : p->contactList) {
@@ -1467,7 +1479,7 @@ void World::merge() {
     if (!P.enable_merging) return;
     std::vector<BPC*> removal;
     for (BPC* p : bodyPairContacts.v) {
-        if (p->inCollection || !checkMergeCondition(P, p)) continue;
+        if (p->inCollection || !checkMergeCondition(P, kin, p)) continue;
         mergingEvent = true;
         mergeEvents++;
         p->inCollection = true;
