@@ -1,5 +1,5 @@
-// grid_sync.cuh -- bounded grid barrier for the cooperative FP64 sweeps
-// (k_pgs_fast, k_gs_levels).
+// grid_sync.cuh -- bounded grid barrier for the cooperative sweeps
+// (k_pgs_fast, k_gs_levels, and the grid form of k_pgs_mixed).
 //
 // Arrivals count up monotonically in DCount::bar_count (zeroed before each
 // launch); a block leaves once the count reaches its own target, so the last
