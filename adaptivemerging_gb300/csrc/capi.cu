@@ -169,6 +169,7 @@ int32_t am_set_params(void* ctx, const am_params* p) {
     if (!ctx || !p) return AM_E_ARG;
     Ctx* c = (Ctx*)ctx;
     if (check_params(p, c->err)) return AM_E_ARG;
+    if (p->enable_sleeping && !c->kin.empty()) { c->err = "kinematic bodies need sleeping off"; return AM_E_STATE; }
     c->P = *p;
     c->host.P = &c->P;
     return AM_OK;
@@ -495,6 +496,7 @@ int Ctx::setKinematic(int body, const double* axis, double amp, double freq, dou
     for (size_t i = 0; i < kin.size(); i++)
         if (kin[i].body == body) { kin.erase(kin.begin() + i); break; }
     if (amp == 0) return AM_OK;
+    if (P.enable_sleeping) { err = "kinematic bodies need sleeping off"; return AM_E_STATE; }
     if ((int)kin.size() >= MAXKIN) { err = "too many kinematic bodies"; return AM_E_CAPACITY; }
     Kinematic q;
     q.body = body;

@@ -428,6 +428,8 @@ int Ctx::ensureCand(int need) {
 // ---- scene upload ------------------------------------------------------------
 int Ctx::setScene(const am_scene& s) {
     release();
+    kin.clear();   // prescribed motions name bodies of the previous scene
+    kinSteps = 0;
     nScenes = 0;
     topEnd = nullptr;
     bRecCap = bPairCap = 0;

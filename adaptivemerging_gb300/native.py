@@ -382,8 +382,8 @@ class System:
         return s.value
 
     def set_params(self, params):
-        self.params = params
         self._check(lib().am_set_params(self.h, C.byref(params)))
+        self.params = params
 
     def set_residual_target(self, target, check_every=10):
         self._check(lib().am_set_residual_target(self.h, target, check_every))

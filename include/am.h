@@ -383,7 +383,13 @@ int32_t am_set_residual_target(void* ctx, double residual_target, int32_t check_
  * kinematic body never merges (its pairs fail the merge test, the one
  * addition to BodyPairContact.checkMergeCondition): a collection holding a
  * pinned body stays put, so the motion would stop acting on its contacts.  A
- * body already inside a collection is refused (AM_E_STATE). */
+ * body already inside a collection is refused (AM_E_STATE), and so is a
+ * kinematic body while sleeping is on, here and in am_set_params: the
+ * reference's sleeping treats every pinned body as static (the broad phase
+ * skips pinned-sleeping pairs, CollisionProcessor.java:693-694, and contacts
+ * with pinned bodies neither keep a body awake nor wake it,
+ * Sleeping.java:65-72, 107-121), so a moving support would pass through a body asleep
+ * on it.  Loading a new scene or batch clears every kinematic body. */
 int32_t am_set_kinematic(void* ctx, int32_t body, const double* axis, double amplitude, double frequency_hz,
                          double dt);
 /* AM_ORDER_MIXED: the form of the solve kernel (-1, default: chosen per

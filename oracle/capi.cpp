@@ -149,6 +149,7 @@ int or_set_kinematic(void* h, int body, const double* axis, double amp, double f
     for (size_t i = 0; i < w->kin.size(); i++)
         if (w->kin[i].body == b) { w->kin.erase(w->kin.begin() + i); break; }
     if (amp == 0) return 0;
+    if (w->P.enable_sleeping) return -1;
     World::Kinematic q;
     q.body = b;
     q.x0[0] = q.body->x.x; q.x0[1] = q.body->x.y; q.x0[2] = q.body->x.z;

@@ -88,6 +88,43 @@ def test_kinematic_platform_bit_exact(gpu_lib):
     assert vy != 0.0
 
 
+def test_kinematic_body_rules(gpu_lib):
+    """am_set_kinematic refuses a moving support while sleeping is on (and
+    am_set_params refuses turning sleeping on under one): the reference's
+    sleeping treats pinned bodies as static.  A new scene loaded into the
+    context clears every kinematic body, so it steps as a fresh context."""
+    import ctypes as C
+    from adaptivemerging_gb300 import native
+    pb = scenes.FUNNEL_PLATFORM
+    sc = scenes.funnel_clumps(6, seed=5)
+    P_sleep = params(enable_merging=1, enable_sleeping=1, friction=0.7, iterations=40)
+    P = params(enable_merging=1, enable_sleeping=0, friction=0.7, iterations=40)
+    g = native.System(sc, P_sleep)
+    with pytest.raises(native.AmError) as e:
+        g.set_kinematic(pb, (0, 1, 0), 0.05, 0.5, 0.002)
+    assert e.value.code == -6
+    g.close()
+    g = native.System(sc, P)
+    g.set_kinematic(pb, (0, 1, 0), 0.05, 0.5, 0.002)
+    with pytest.raises(native.AmError) as e:
+        g.set_params(P_sleep)
+    assert e.value.code == -6
+    g.set_params(P)
+    g.step(0.002, 5)
+    second = scenes.tower(6, seed=1)
+    s2 = second.struct()
+    g._check(native.lib().am_set_scene(g.h, C.byref(s2)))
+    g._s, g.n, g.scene = s2, second.n, second
+    g.set_params(P_sleep)   # no kinematic body is left
+    fresh = native.System(second, P_sleep)
+    for _ in range(20):
+        g.step(0.01)
+        fresh.step(0.01)
+    assert np.array_equal(g.bodies()["x"], fresh.bodies()["x"])
+    g.close()
+    fresh.close()
+
+
 @pytest.mark.parametrize("name", list(CASES))
 def test_merging_bit_exact(gpu_lib, name):
     from adaptivemerging_gb300 import native

@@ -76,3 +76,14 @@ def test_body_inside_a_collection_cannot_become_kinematic():
     assert _in_collection(o, pb)
     with pytest.raises(AssertionError):
         o.set_kinematic(pb, (0, 1, 0), 0.05, 0.5, 0.002)
+
+
+def test_kinematic_body_refused_while_sleeping():
+    """The reference's sleeping treats pinned bodies as static (pinned-asleep
+    pairs are skipped, and contacts with pinned bodies neither keep a body
+    awake nor wake it), so a moving support needs sleeping off."""
+    sc = scenes.funnel_clumps(6, seed=5)
+    o = Oracle(sc, params(enable_sleeping=1))
+    with pytest.raises(AssertionError):
+        o.set_kinematic(scenes.FUNNEL_PLATFORM, (0, 1, 0), 0.05, 0.5, 0.002)
+    o.set_kinematic(scenes.FUNNEL_PLATFORM, (0, 1, 0), 0.0, 0.5, 0.002)   # removing is always allowed
