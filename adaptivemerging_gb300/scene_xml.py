@@ -19,9 +19,11 @@ Each body may carry the child elements ``x``, ``R`` (axis x y z and angle),
 The ``<collision>`` element sets ``iterations``, ``feedbackStiffness``,
 ``enableCompliance``, and ``restitution`` / ``friction``. The last two also
 switch the corresponding override on, as the reference does (:100-137).
+The ``<system>`` element only sets the mouse spring (:69-89) and is ignored.
 
-Composite bodies, springs and spinners are not part of this implementation. They raise ``NotSupported`` instead of being skipped, so a
-scene never loads silently different from the reference.
+Composite bodies, springs, spinners and ``enablePostStabilization="true"``
+are not part of this implementation. They raise ``NotSupported`` instead of
+being skipped, so a scene never loads silently different from the reference.
 """
 import os
 import xml.etree.ElementTree as ET
@@ -175,6 +177,9 @@ def load(source, params=None, data_root=None):
             P.friction_override = 1
         if "enableCompliance" in a:
             P.enable_compliance = int(a["enableCompliance"].lower() == "true")
+        if a.get("enablePostStabilization", "").lower() == "true":
+            raise NotSupported("enablePostStabilization (the post-stabilization solve, "
+                               "RigidBodySystem.java:354-376)")
     b = Builder()
     names = []
     for el in root:

@@ -62,6 +62,12 @@ def test_loader_refuses_unsupported_elements():
         scene_xml.load('<root><body type="composite" name="c"/></root>')
     with pytest.raises(scene_xml.NotSupported):
         scene_xml.load('<root><body type="box" dim="1 1 1"><spring pB="0 0 0" pW="0 1 0"/></body></root>')
+    with pytest.raises(scene_xml.NotSupported):
+        scene_xml.load('<root><collision enablePostStabilization="true" iterations="10"/>'
+                       '<body type="box" dim="1 1 1"/></root>')
+    sc, P, _ = scene_xml.load('<root><collision enablePostStabilization="false" iterations="10"/>'
+                              '<system mouseSpringStiffness="3"/><body type="box" dim="1 1 1"/></root>')
+    assert sc.n == 1 and P.iterations == 10
 
 
 def test_loaded_scene_runs_on_the_oracle():
