@@ -97,6 +97,7 @@ class am_scene(C.Structure):
         ("inertia", _P(_f64)), ("friction", _P(_f64)), ("restitution", _P(_f64)),
         ("shape", _P(_f64)), ("n_nodes", _i32), ("body_root", _P(_i32)), ("node_c", _P(_f64)),
         ("node_r", _P(_f64)), ("node_child0", _P(_i32)), ("node_nchild", _P(_i32)),
+        ("bbox", _P(_f64)),
     ]
 
 

@@ -1954,10 +1954,15 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     std::vector<int> type, pinned, root, c0, nch;
     std::vector<double> x, R, v, w, mass, inertia, fr, re, shape, nc, nr;
     std::vector<int> bodyOff(n + 1, 0), sceneOf;
+    std::vector<double> bbox;   // am_scene.bbox of every scene, NaN (derived) where a scene has none
+    bool anyBox = false;
+    for (int s = 0; s < n; s++) anyBox = anyBox || sc[s].bbox;
     int nodeBase = 0;
     maxSceneBodies = 0;
     for (int s = 0; s < n; s++) {
         const am_scene& a = sc[s];
+        if (anyBox)
+            for (int k = 0; k < 6 * a.n_bodies; k++) bbox.push_back(a.bbox ? a.bbox[k] : NAN);
         bodyOff[s + 1] = bodyOff[s] + a.n_bodies;
         maxSceneBodies = std::max(maxSceneBodies, a.n_bodies);
         for (int i = 0; i < a.n_bodies; i++) {
@@ -1983,6 +1988,7 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     all.omega = w.data(); all.mass = mass.data(); all.inertia = inertia.data(); all.friction = fr.data();
     all.restitution = re.data(); all.shape = shape.data(); all.n_nodes = nodeBase; all.body_root = root.data();
     all.node_c = nc.data(); all.node_r = nr.data(); all.node_child0 = c0.data(); all.node_nchild = nch.data();
+    all.bbox = anyBox ? bbox.data() : nullptr;
     int r = setScene(all);
     if (r) return r;
     nScenes = n;

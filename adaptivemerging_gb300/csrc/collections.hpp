@@ -7,6 +7,7 @@
 // the per-step state live on the device.
 #pragma once
 #include <chrono>
+#include <cmath>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -25,6 +26,14 @@ inline double __longlong_as_double_host(unsigned long long b) {
     double d;
     std::memcpy(&d, &b, sizeof(d));
     return d;
+}
+
+// am_scene.bbox holds body i's boundingBoxB (six finite numbers)
+inline bool given_bbox(const am_scene& s, int i) {
+    if (!s.bbox) return false;
+    for (int k = 0; k < 6; k++)
+        if (!std::isfinite(s.bbox[6 * i + k])) return false;
+    return true;
 }
 
 struct HostWorld {
@@ -92,6 +101,9 @@ struct HostWorld {
             } else if (type[i] == AM_SPHERE) {
                 double r = s.shape[4 * i];
                 ll = mk(-r, -r, -r); ur = mk(r, r, r);
+            } else if (given_bbox(s, i)) {   // sphere tree with its mesh's box
+                const double* q = s.bbox + 6 * i;
+                ll = mk(q[0], q[1], q[2]); ur = mk(q[3], q[4], q[5]);
             } else {   // sphere tree: box of the leaf spheres
                 ll = mk(1e300, 1e300, 1e300); ur = mk(-1e300, -1e300, -1e300);
                 std::vector<int> st{s.body_root[i]};

@@ -7,9 +7,10 @@ The supported subset is what the contact path simulates:
 - ``<body type="plane">`` with ``p`` and ``n``, always pinned (:405-416);
 - ``<body type="mesh">`` with ``obj``, ``st``, ``scale`` and optional
   ``density`` (createMesh, :449-539): mass, centre of mass and inertia of the
-  scaled triangle soup, and the sphere tree of the ``.sph`` file, scaled and
-  moved to the centre of mass.  The mesh itself only draws; the sphere tree
-  is what collides.
+  scaled triangle soup, the box of its vertices about the centre of mass
+  (the body's boundingBoxB, where the motion metric samples velocities), and
+  the sphere tree of the ``.sph`` file, scaled and moved to the centre of
+  mass.  Otherwise the mesh only draws; the sphere tree is what collides.
 
 Each body may carry the child elements ``x``, ``R`` (axis x y z and angle),
 ``v``, ``omega``, ``friction``, ``restitution`` and ``pinned``
@@ -25,6 +26,7 @@ Composite bodies, springs, spinners and ``enablePostStabilization="true"``
 are not part of this implementation. They raise ``NotSupported`` instead of
 being skipped, so a scene never loads silently different from the reference.
 """
+import math
 import os
 import xml.etree.ElementTree as ET
 
@@ -131,6 +133,43 @@ def mesh_mass_properties(verts, faces, density):
     return float(mass), r, J
 
 
+_DOUBLE_MIN_VALUE = float.fromhex("0x0.0000000000001p-1022")   # java.lang.Double.MIN_VALUE
+
+
+def _jmin(a, b):
+    """java.lang.Math.min for doubles: NaN first, -0.0 below +0.0."""
+    if a != a:
+        return a
+    if a == 0.0 and b == 0.0 and math.copysign(1.0, b) < 0:
+        return b
+    return a if a <= b else b
+
+
+def _jmax(a, b):
+    """java.lang.Math.max for doubles: NaN first, +0.0 above -0.0."""
+    if a != a:
+        return a
+    if a == 0.0 and b == 0.0 and math.copysign(1.0, a) < 0:
+        return b
+    return a if a >= b else b
+
+
+def mesh_box(points):
+    """The mesh body's boundingBoxB corners as (ll, ur) (XMLParser.java:
+    474-493): over the scaled vertices moved to the centre of mass, in the
+    file's order.  As in the reference, the upper corner starts at
+    Double.MIN_VALUE (the smallest positive double), so an axis on which
+    every vertex is negative keeps that value."""
+    ll = [1.7976931348623157e308] * 3
+    ur = [_DOUBLE_MIN_VALUE] * 3
+    for p in points:
+        for k in range(3):
+            q = float(p[k])
+            ll[k] = _jmin(q, ll[k])
+            ur[k] = _jmax(q, ur[k])
+    return ll + ur
+
+
 def read_sphere_tree(path):
     """A ``.sph`` sphere tree as createMesh reads it (XMLParser.java:499-534):
     the number of spheres, one ``x y z r`` line per sphere, then lines
@@ -210,7 +249,8 @@ def load(source, params=None, data_root=None):
             mass, com, J = mesh_mass_properties(verts * scale, faces, density)
             cs, rs, children = read_sphere_tree(os.path.join(data_root, el.get("st")))
             b.tree(cs * scale - com, rs * scale, children, c["x"], mass, J, R=c["R"], v=c["v"], omega=c["omega"],
-                   friction=c["friction"], restitution=c["restitution"], pinned=c["pinned"])
+                   friction=c["friction"], restitution=c["restitution"], pinned=c["pinned"],
+                   bbox=mesh_box(verts * scale - com))
         else:
             raise NotSupported(f"body type {kind!r} ({name!r})")
         names.append(name)

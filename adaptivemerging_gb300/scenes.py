@@ -42,7 +42,7 @@ class Builder:
     def _add(self, **kw):
         d = dict(type=AM_BOX, pinned=0, x=(0, 0, 0), R=IDENT, v=(0, 0, 0), omega=(0, 0, 0),
                  mass=0.0, inertia=[0.0] * 9, friction=0.8, restitution=0.0,
-                 shape=(0, 0, 0, 0), root=-1)
+                 shape=(0, 0, 0, 0), root=-1, bbox=None)
         d.update(kw)
         self.b.append(d)
         return len(self.b) - 1
@@ -98,11 +98,14 @@ class Builder:
                          restitution=restitution, root=root)
 
     def tree(self, centres, radii, children, x, mass, inertia, R=IDENT, v=(0, 0, 0), omega=(0, 0, 0),
-             friction=0.8, restitution=0.0, pinned=False):
+             friction=0.8, restitution=0.0, pinned=False, bbox=None):
         """Sphere-tree body of any depth: node k has centre centres[k] and
         radius radii[k] in body coordinates and the child nodes children[k]
         (in their order); node 0 is the root.  The nodes are stored breadth
-        first, so every node's children sit together in that order."""
+        first, so every node's children sit together in that order.  `bbox`
+        (ll, ur: six numbers in body coordinates) is the body's bounding box
+        for the motion metric, a mesh body's mesh box; without it the box of
+        the leaf spheres is used."""
         order, pos = [0], {0: 0}
         for k in order:
             for q in children[k]:
@@ -118,12 +121,17 @@ class Builder:
             self.nodes.append((tuple(float(t) for t in centres[k]), float(radii[k]), c0, len(ch)))
         return self._add(type=AM_TREE, x=tuple(float(t) for t in x), R=R, v=v, omega=omega, mass=float(mass),
                          inertia=[float(t) for t in np.asarray(inertia, float).reshape(-1)], friction=friction,
-                         restitution=restitution, root=base, pinned=int(bool(pinned)))
+                         restitution=restitution, root=base, pinned=int(bool(pinned)),
+                         bbox=None if bbox is None else [float(t) for t in bbox])
 
     def build(self):
         n = len(self.b)
         f = lambda k, w: np.array([d[k] for d in self.b], float).reshape(n * w)
         nodes = self.nodes if self.nodes else []
+        extra = {}
+        if any(d["bbox"] is not None for d in self.b):
+            extra["bbox"] = np.array([d["bbox"] if d["bbox"] is not None else [np.nan] * 6 for d in self.b],
+                                     float).reshape(-1)
         return SceneArrays(
             type=[d["type"] for d in self.b], pinned=[d["pinned"] for d in self.b],
             x=f("x", 3), R=f("R", 9), v=f("v", 3), omega=f("omega", 3),
@@ -133,6 +141,7 @@ class Builder:
             node_c=np.array([c for c, _, _, _ in nodes], float).reshape(-1),
             node_r=np.array([r for _, r, _, _ in nodes], float),
             node_child0=[c0 for _, _, c0, _ in nodes], node_nchild=[nc for _, _, _, nc in nodes],
+            **extra,
         )
 
 

@@ -134,6 +134,13 @@ typedef struct am_scene {
     const double*  node_r;      /* [n_nodes]                                    */
     const int32_t* node_child0; /* [n_nodes] first child index or -1 (leaf)     */
     const int32_t* node_nchild; /* [n_nodes] children are contiguous            */
+    /* optional, may be NULL: boundingBoxB of AM_TREE bodies as (ll, ur) in
+     * body coordinates, [6n].  The motion metric of merging and sleeping
+     * samples the velocity at its 8 corners (MotionMetricProcessor.java:
+     * 39-73).  A mesh body's box is its mesh's (XMLParser.java:474-493);
+     * NULL, non-finite entries and other body types take the box of the
+     * geometry (AM_TREE: the box of its leaf spheres). */
+    const double*  bbox;
 } am_scene;
 
 /* Per-body state read back after a step. */

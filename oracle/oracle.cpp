@@ -81,7 +81,14 @@ void World::init(const am_params& p, const am_scene& s) {
             double r = s.shape[4 * i];
             b.bbB = {V3(-r, -r, -r), V3(-r, -r, r), V3(-r, r, -r), V3(-r, r, r),
                      V3(r, -r, -r), V3(r, -r, r), V3(r, r, -r), V3(r, r, r)};
-        } else {  // sphere tree: box of the leaf spheres (stand-in for the mesh AABB)
+        } else if (s.bbox && std::isfinite(s.bbox[6 * i]) && std::isfinite(s.bbox[6 * i + 1]) &&
+                   std::isfinite(s.bbox[6 * i + 2]) && std::isfinite(s.bbox[6 * i + 3]) &&
+                   std::isfinite(s.bbox[6 * i + 4]) && std::isfinite(s.bbox[6 * i + 5])) {
+            // a mesh body: the box of its mesh's vertices (XMLParser.java:474-493)
+            const double* q = s.bbox + 6 * i;
+            b.bbB = {V3(q[0], q[1], q[2]), V3(q[0], q[1], q[5]), V3(q[0], q[4], q[2]), V3(q[0], q[4], q[5]),
+                     V3(q[3], q[1], q[2]), V3(q[3], q[1], q[5]), V3(q[3], q[4], q[2]), V3(q[3], q[4], q[5])};
+        } else {  // sphere tree without a mesh (a clump): the box of its leaf spheres
             V3 ll(1e300, 1e300, 1e300), ur(-1e300, -1e300, -1e300);
             std::vector<int> st{s.body_root[i]};
             while (!st.empty()) {

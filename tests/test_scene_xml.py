@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from adaptivemerging_gb300 import abi, scene_xml
+from helpers import params
 
 DOC = """<?xml version="1.0" ?>
 <root>
@@ -135,6 +136,39 @@ def test_mesh_body_mass_properties_and_tree(tmp_path):
     c = np.asarray(a["node_c"]).reshape(-1, 3)
     assert np.allclose(c[r0], 0.0) and np.allclose(c[r0 + 1], (0, 0, -0.5)) and np.allclose(c[r0 + 2], (0, 0, 0.5))
     assert np.allclose(np.asarray(a["node_r"])[r0:r0 + 3], (1.8, 0.9, 0.9))
+    # boundingBoxB is the box of the scaled vertices about the centre of mass,
+    # not the box of the leaf spheres (which reach 0.45 + 0.9 = 1.35 above it)
+    assert list(a["bbox"][:6]) == [-1.0, -1.0, -1.0, 1.0, 1.0, 1.0]
+
+
+def test_mesh_box_follows_the_reference_arithmetic():
+    """XMLParser.java:474-493: Math.min / Math.max from MAX_VALUE and
+    Double.MIN_VALUE.  An axis on which no vertex is positive keeps
+    MIN_VALUE (the smallest positive double) as its upper bound, and the
+    sign of a zero follows Java's min (-0.0 below +0.0)."""
+    box = scene_xml.mesh_box([(-1.0, 0.0, -2.0), (-0.5, -0.0, 3.0)])
+    assert box[:3] == [-1.0, -0.0, -2.0] and math.copysign(1, box[1]) < 0
+    assert box[3:] == [5e-324, 5e-324, 3.0]
+
+
+def test_mesh_box_moves_the_motion_metric():
+    """The merge test's relative-velocity metric samples the corners of the
+    body's boundingBoxB (MotionMetricProcessor.java:39-73), so a mesh body's
+    box must be its mesh's.  Two identical tumbling mesh bodies, one given
+    the mesh box and one the leaf-sphere box, resting on a plane: the
+    metric of each body's pair with the plane differs."""
+    from oracle_binding import Oracle
+    from adaptivemerging_gb300.scenes import Builder
+    out = []
+    for box in ([-0.5, -0.5, -0.5, 0.5, 0.5, 0.5], None):
+        b = Builder()
+        b.tree([(0, 0, 0), (0, 0, -0.25), (0, 0, 0.25)], [0.9, 0.45, 0.45], [[1, 2], [], []], (0, 0.45, 0),
+               1000.0, 1000.0 / 6 * np.eye(3), omega=(0.0, 0.3, 0.0), bbox=box)
+        b.plane((0, 0, 0), (0, 1, 0))
+        o = Oracle(b.build(), params(enable_merging=1, enable_sleeping=0, gravity_amount=9.81))
+        o.step(0.01, 5)
+        out.append(o.merge_tests()["metric"])
+    assert len(out[0]) == 1 and len(out[1]) == 1 and out[0][0] != out[1][0]
 
 
 def test_mesh_body_settles_on_oracle(tmp_path):
