@@ -175,17 +175,46 @@ int32_t am_set_params(void* ctx, const am_params* p) {
     return AM_OK;
 }
 
-int32_t am_set_scene(void* ctx, const am_scene* s) {
-    if (!ctx || !s) return AM_E_ARG;
-    Ctx* c = (Ctx*)ctx;
-    for (int i = 0; i < s->n_bodies; i++) {
-        int t = s->type[i];
-        if (t < AM_BOX || t > AM_TREE) { c->err = "unknown body type"; return AM_E_ARG; }
-        if ((t == AM_SPHERE || t == AM_TREE) && (s->body_root[i] < 0 || s->body_root[i] >= s->n_nodes)) {
-            c->err = "sphere / tree body without a valid root node";
+// A scene is checked on the host before anything reaches the device: the
+// tree colliders follow node_child0 / node_nchild, so a child index outside
+// the node array would read out of bounds, and a node that is its own
+// descendant would never end a traversal.  Every node's children must
+// therefore lie after it in the array (as in breadth-first order), which
+// also makes every path from a root finite.
+static int check_scene(const am_scene& s, std::string& err) {
+    if (s.n_bodies < 0 || s.n_nodes < 0) { err = "negative body or node count"; return AM_E_ARG; }
+    if (s.n_bodies > 0 && (!s.type || !s.pinned || !s.x || !s.R || !s.v || !s.omega || !s.mass || !s.inertia ||
+                           !s.friction || !s.restitution || !s.shape || !s.body_root)) {
+        err = "a body array is missing";
+        return AM_E_ARG;
+    }
+    if (s.n_nodes > 0 && (!s.node_c || !s.node_r || !s.node_child0 || !s.node_nchild)) {
+        err = "a node array is missing";
+        return AM_E_ARG;
+    }
+    for (int i = 0; i < s.n_bodies; i++) {
+        int t = s.type[i];
+        if (t < AM_BOX || t > AM_TREE) { err = "unknown body type"; return AM_E_ARG; }
+        if ((t == AM_SPHERE || t == AM_TREE) && (s.body_root[i] < 0 || s.body_root[i] >= s.n_nodes)) {
+            err = "sphere / tree body without a valid root node";
             return AM_E_ARG;
         }
     }
+    for (int k = 0; k < s.n_nodes; k++) {
+        int c0 = s.node_child0[k], nc = s.node_nchild[k];
+        if (c0 < 0) continue;   // a leaf
+        if (nc < 1 || c0 <= k || c0 > s.n_nodes - nc) {
+            err = "sphere-tree node " + std::to_string(k) + ": its children must follow it inside the node array";
+            return AM_E_ARG;
+        }
+    }
+    return AM_OK;
+}
+
+int32_t am_set_scene(void* ctx, const am_scene* s) {
+    if (!ctx || !s) return AM_E_ARG;
+    Ctx* c = (Ctx*)ctx;
+    if (check_scene(*s, c->err)) return AM_E_ARG;
     return c->setScene(*s);
 }
 
@@ -194,10 +223,7 @@ int32_t am_set_batch(void* ctx, const am_scene* scenes, int32_t n) {
     Ctx* c = (Ctx*)ctx;
     if (c->P.enable_merging) { c->err = "batched scenes need enable_merging = 0"; return AM_E_ARG; }
     for (int s = 0; s < n; s++)
-        for (int i = 0; i < scenes[s].n_bodies; i++) {
-            int t = scenes[s].type[i];
-            if (t < AM_BOX || t > AM_TREE) { c->err = "unknown body type"; return AM_E_ARG; }
-        }
+        if (check_scene(scenes[s], c->err)) return AM_E_ARG;
     return c->setBatch(scenes, n);
 }
 

@@ -7,6 +7,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 from adaptivemerging_gb300 import abi
@@ -92,3 +93,34 @@ def test_argument_errors_without_gpu(lib):
     assert lib.am_create(C.byref(p), C.byref(h)) == abi.AM_E_ARG
     lib.am_step.argtypes = [C.c_void_p, C.c_double]
     assert lib.am_step(None, 0.01) == abi.AM_E_ARG
+
+
+def test_malformed_sphere_trees_are_refused_on_the_host(lib):
+    """am_set_scene checks the node arrays before anything reaches the
+    device: a node that lists itself (or an earlier node) as a child would
+    never end a traversal, and a child range past the node array would read
+    out of bounds.  Both come back as AM_E_ARG, with no CUDA call made."""
+    from adaptivemerging_gb300 import scenes
+    lib.am_create.argtypes = [C.POINTER(abi.am_params), C.POINTER(C.c_void_p)]
+    lib.am_set_scene.argtypes = [C.c_void_p, C.POINTER(abi.am_scene)]
+    lib.am_set_batch.argtypes = [C.c_void_p, C.POINTER(abi.am_scene), C.c_int32]
+    lib.am_destroy.argtypes = [C.c_void_p]
+    lib.am_last_error.argtypes = [C.c_void_p]
+    lib.am_last_error.restype = C.c_char_p
+    good = scenes.funnel_clumps(2, seed=5)
+    root = int(good.a["body_root"][good.a["type"].tolist().index(abi.AM_TREE)])
+    h = C.c_void_p()
+    assert lib.am_create(C.byref(abi.default_params(enable_merging=0)), C.byref(h)) == 0
+    try:
+        for child0, nchild in ((root, 1), (root + 1, len(good.a["node_r"]))):
+            arr = {k: np.array(v, copy=True) for k, v in good.a.items()}
+            arr["node_child0"][root] = child0
+            arr["node_nchild"][root] = nchild
+            bad = abi.SceneArrays(**arr)
+            s = bad.struct()
+            assert lib.am_set_scene(h, C.byref(s)) == abi.AM_E_ARG
+            assert b"children must follow it" in lib.am_last_error(h)
+            batch = (abi.am_scene * 2)(good.struct(), s)
+            assert lib.am_set_batch(h, batch, 2) == abi.AM_E_ARG
+    finally:
+        lib.am_destroy(h)
