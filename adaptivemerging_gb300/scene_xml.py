@@ -47,19 +47,23 @@ def _vec(text, n=3):
     return v
 
 
-def _common(el):
-    """x, R, v, omega, friction, restitution, pinned of one body element."""
+def _common(el, composite=False):
+    """x, R, v, omega, friction, restitution, pinned of one body element.
+    ``events`` records the order of x, R and pinned, which decides when the
+    reference refreshes the rotational inertia (setCommonAttributes)."""
     out = {"x": (0.0, 0.0, 0.0), "R": IDENT, "v": (0.0, 0.0, 0.0), "omega": (0.0, 0.0, 0.0),
-           "friction": 0.8, "restitution": 0.0, "pinned": False}
+           "friction": 0.8, "restitution": 0.0, "pinned": False, "events": []}
     for ch in el:
         tag = ch.tag.lower()
         text = (ch.text or "").strip()
         if tag == "x":
             out["x"] = tuple(_vec(text))
+            out["events"].append(("x", out["R"], out["pinned"]))
         elif tag == "r":
             ax = _vec(text, 4)
             norm = (ax[0] ** 2 + ax[1] ** 2 + ax[2] ** 2) ** 0.5
             out["R"] = IDENT if norm == 0.0 else axis_angle(ax[:3], ax[3])
+            out["events"].append(("R", out["R"], out["pinned"]))
         elif tag == "v":
             out["v"] = tuple(_vec(text))
         elif tag == "omega":
@@ -72,9 +76,114 @@ def _common(el):
             out["pinned"] = text.split()[0].lower() == "true"
         elif tag in ("magnetic", "factorypart", "temporarilypinned", "col"):
             pass
+        elif tag == "body" and composite:
+            pass   # a composite's sub-body, read by _composite
         elif tag in ("spring", "spinner", "body"):
             raise NotSupported(f"<{ch.tag}> in body {el.get('name')!r}")
     return out
+
+
+def _mul(A, B):
+    """javax.vecmath Matrix3d.mul(A, B), row-major lists of 9."""
+    return [A[3 * r] * B[c] + A[3 * r + 1] * B[3 + c] + A[3 * r + 2] * B[6 + c] for r in range(3) for c in range(3)]
+
+
+def _mul_tr(A, B):
+    """Matrix3d.mulTransposeRight(A, B) = A B^T."""
+    return [A[3 * r] * B[3 * c] + A[3 * r + 1] * B[3 * c + 1] + A[3 * r + 2] * B[3 * c + 2]
+            for r in range(3) for c in range(3)]
+
+
+def _rm0rt(R, M0):
+    """RigidTransform3D.computeRM0RT: R M0 R^T."""
+    return _mul_tr(_mul(R, M0), R)
+
+
+def _transform(R, t, p):
+    """RigidTransform3D.transform(Point3d): R p + t, Matrix3d.transform order."""
+    return [R[3 * r] * p[0] + R[3 * r + 1] * p[1] + R[3 * r + 2] * p[2] + t[r] for r in range(3)]
+
+
+def _sub_body(el):
+    """One box or sphere inside a composite, as createBox / createSphere and
+    setCommonAttributes leave it (XMLParser.java:360-447, 545-590): mass,
+    massAngular (refreshed to R M0 R^T at each x and R element while not
+    pinned, and once more at the end for a box), pose and boundingBoxB.
+    Other types give no sub-body, as in the reference (:216-231)."""
+    kind = el.get("type", "").lower()
+    c = _common(el)
+    density = float(el.get("density", "1"))
+    if kind == "box":
+        s = _vec(el.get("dim"))
+        if "scale" in el.attrib:
+            k = float(el.get("scale"))
+            s = [q * k for q in s]
+        m = s[0] * s[1] * s[2] * density
+        M0 = [1.0 / 12 * m * (s[1] * s[1] + s[2] * s[2]), 0.0, 0.0,
+              0.0, 1.0 / 12 * m * (s[0] * s[0] + s[2] * s[2]), 0.0,
+              0.0, 0.0, 1.0 / 12 * m * (s[0] * s[0] + s[1] * s[1])]
+        h = [q * 0.5 for q in s]
+        shape = [s[0], s[1], s[2], 0.0]
+        typ = abi.AM_BOX
+    elif kind == "sphere":
+        r = float(el.get("r"))
+        m = 4.0 / 3 * math.pi * r * r * r * density
+        i = 2.0 / 5 * m * r * r
+        M0 = [i, 0.0, 0.0, 0.0, i, 0.0, 0.0, 0.0, i]
+        h = [r, r, r]
+        shape = [r, 0.0, 0.0, 0.0]
+        typ = abi.AM_SPHERE
+    else:
+        return None
+    Ma = list(M0)
+    for _, R, pinned in c["events"]:
+        if not pinned:
+            Ma = _rm0rt(R, M0)
+    if kind == "box" and not c["pinned"]:
+        Ma = _rm0rt(c["R"], M0)
+    bb = [(-h[0], -h[1], -h[2]), (-h[0], -h[1], h[2]), (-h[0], h[1], -h[2]), (-h[0], h[1], h[2]),
+          (h[0], -h[1], -h[2]), (h[0], -h[1], h[2]), (h[0], h[1], -h[2]), (h[0], h[1], h[2])]
+    return {"type": typ, "shape": shape, "m": m, "M": Ma, "R": list(c["R"]), "x": list(c["x"]), "bbB": bb}
+
+
+def _composite(el):
+    """createComposite (XMLParser.java:180-352): the sub-bodies' total mass,
+    centre of mass, inertia (their massAngular plus the parallel-axis term,
+    summed in list order) and box (corners placed by each sub-body's pose,
+    Math.min / Math.max from MAX_VALUE and Double.MIN_VALUE, then moved to the
+    centre of mass); the composite's x is its element's x plus that centre,
+    unrotated, as the reference adds it (:311-312); each sub-body's pose in
+    the composite is its own rotation and its position less the centre."""
+    subs = [q for q in (_sub_body(ch) for ch in el if ch.tag.lower() == "body") if q is not None]
+    if not subs:
+        raise NotSupported(f"composite {el.get('name')!r} without box or sphere bodies")
+    mass = 0.0
+    com = [0.0, 0.0, 0.0]
+    for q in subs:
+        mass += q["m"]
+        com = [q["m"] * q["x"][k] + com[k] for k in range(3)]
+    com = [v * (1.0 / mass) for v in com]
+    M = [0.0] * 9
+    for q in subs:
+        M = [M[k] + q["M"][k] for k in range(9)]
+        x, y, z = (q["x"][0] - com[0], q["x"][1] - com[1], q["x"][2] - com[2])
+        x2, y2, z2 = x * x, y * y, z * z
+        op = [y2 + z2, -x * y, -x * z, -y * x, x2 + z2, -y * z, -z * x, -z * y, x2 + y2]
+        M = [M[k] + op[k] * q["m"] for k in range(9)]
+    ll = [1.7976931348623157e308] * 3
+    ur = [_DOUBLE_MIN_VALUE] * 3
+    for q in subs:
+        for p in q["bbB"]:
+            w = _transform(q["R"], q["x"], p)
+            for k in range(3):
+                ll[k] = _jmin(w[k], ll[k])
+                ur[k] = _jmax(w[k], ur[k])
+    ll = [ll[k] - com[k] for k in range(3)]
+    ur = [ur[k] - com[k] for k in range(3)]
+    c = _common(el, composite=True)
+    x = [c["x"][k] + com[k] for k in range(3)]
+    parts = [(q["type"], q["shape"], q["R"], [q["x"][k] - com[k] for k in range(3)]) for q in subs]
+    return c, x, mass, M, ll + ur, parts
 
 
 def read_obj(path):
@@ -189,7 +298,7 @@ def read_sphere_tree(path):
     return cr[:, :3], cr[:, 3], children
 
 
-def load(source, params=None, data_root=None):
+def load(source, params=None, data_root=None, composites=False):
     """Parse an XML scene (a path, or the document text when it starts with
     '<').  Mesh bodies name their ``obj`` and ``st`` files relative to the
     reference project's root, which `data_root` gives (default: the parent of
@@ -226,7 +335,7 @@ def load(source, params=None, data_root=None):
             continue
         kind = el.get("type", "").lower()
         name = el.get("name", "")
-        c = _common(el)
+        c = _common(el, composite=(kind == "composite" and composites))
         density = float(el.get("density", "1"))
         if kind == "box":
             s = _vec(el.get("dim"))
@@ -251,6 +360,10 @@ def load(source, params=None, data_root=None):
             b.tree(cs * scale - com, rs * scale, children, c["x"], mass, J, R=c["R"], v=c["v"], omega=c["omega"],
                    friction=c["friction"], restitution=c["restitution"], pinned=c["pinned"],
                    bbox=mesh_box(verts * scale - com))
+        elif kind == "composite" and composites:
+            cc, x, mass, M, box, parts = _composite(el)
+            b.composite(x, mass, M, box, parts, R=cc["R"], v=cc["v"], omega=cc["omega"], friction=cc["friction"],
+                        restitution=cc["restitution"], pinned=cc["pinned"])
         else:
             raise NotSupported(f"body type {kind!r} ({name!r})")
         names.append(name)

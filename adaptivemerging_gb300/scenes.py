@@ -33,11 +33,16 @@ def axis_angle(ax, theta):
 
 IDENT = [1.0, 0, 0, 0, 1.0, 0, 0, 0, 1.0]
 
+# Body type of a composite body.  It is not part of the C ABI: the oracle
+# steps composites, and the library refuses the type.
+COMPOSITE = 4
+
 
 class Builder:
     def __init__(self):
         self.b = []          # per-body dicts
         self.nodes = []      # (c, r, child0, nchild)
+        self.subs = []       # composite sub-bodies: (parent, type, shape[4], R[9], t[3])
 
     def _add(self, **kw):
         d = dict(type=AM_BOX, pinned=0, x=(0, 0, 0), R=IDENT, v=(0, 0, 0), omega=(0, 0, 0),
@@ -124,6 +129,19 @@ class Builder:
                          restitution=restitution, root=base, pinned=int(bool(pinned)),
                          bbox=None if bbox is None else [float(t) for t in bbox])
 
+    def composite(self, x, mass, inertia, bbox, subs, R=IDENT, v=(0, 0, 0), omega=(0, 0, 0), friction=0.8,
+                  restitution=0.0, pinned=False):
+        """A composite body (the reference's RigidBodyGeomComposite): rigid
+        body data as given, and its box and sphere sub-bodies as (type,
+        shape[4], R[9], t[3]) with their pose in the composite's frame.  Only
+        the oracle steps composites; the library refuses their body type."""
+        i = self._add(type=COMPOSITE, pinned=int(bool(pinned)), x=tuple(float(t) for t in x), R=R, v=v,
+                      omega=omega, mass=float(mass), inertia=[float(t) for t in np.asarray(inertia).reshape(-1)],
+                      friction=friction, restitution=restitution, bbox=[float(t) for t in bbox])
+        for typ, shape, Rs, ts in subs:
+            self.subs.append((i, typ, list(shape), list(Rs), list(ts)))
+        return i
+
     def build(self):
         n = len(self.b)
         f = lambda k, w: np.array([d[k] for d in self.b], float).reshape(n * w)
@@ -132,7 +150,7 @@ class Builder:
         if any(d["bbox"] is not None for d in self.b):
             extra["bbox"] = np.array([d["bbox"] if d["bbox"] is not None else [np.nan] * 6 for d in self.b],
                                      float).reshape(-1)
-        return SceneArrays(
+        sc = SceneArrays(
             type=[d["type"] for d in self.b], pinned=[d["pinned"] for d in self.b],
             x=f("x", 3), R=f("R", 9), v=f("v", 3), omega=f("omega", 3),
             mass=[d["mass"] for d in self.b], inertia=f("inertia", 9),
@@ -143,6 +161,13 @@ class Builder:
             node_child0=[c0 for _, _, c0, _ in nodes], node_nchild=[nc for _, _, _, nc in nodes],
             **extra,
         )
+        if self.subs:
+            sc.composite_subs = {
+                "parent": [q[0] for q in self.subs], "type": [q[1] for q in self.subs],
+                "shape": np.array([q[2] for q in self.subs], float).reshape(-1),
+                "R": np.array([q[3] for q in self.subs], float).reshape(-1),
+                "t": np.array([q[4] for q in self.subs], float).reshape(-1)}
+        return sc
 
 
 # --------------------------------------------------------------------------

@@ -81,6 +81,13 @@ void World::init(const am_params& p, const am_scene& s) {
             double r = s.shape[4 * i];
             b.bbB = {V3(-r, -r, -r), V3(-r, -r, r), V3(-r, r, -r), V3(-r, r, r),
                      V3(r, -r, -r), V3(r, -r, r), V3(r, r, -r), V3(r, r, r)};
+        } else if (b.type == ORC_COMPOSITE) {
+            // createComposite's box of the sub-bodies' corners, in its own corner
+            // order (XMLParser.java:280-306)
+            const double* q = s.bbox ? s.bbox + 6 * i : nullptr;
+            if (q)
+                b.bbB = {V3(q[0], q[1], q[2]), V3(q[0], q[1], q[5]), V3(q[0], q[4], q[2]), V3(q[0], q[4], q[5]),
+                         V3(q[3], q[4], q[5]), V3(q[3], q[1], q[2]), V3(q[3], q[1], q[5]), V3(q[3], q[4], q[2])};
         } else if (s.bbox && std::isfinite(s.bbox[6 * i]) && std::isfinite(s.bbox[6 * i + 1]) &&
                    std::isfinite(s.bbox[6 * i + 2]) && std::isfinite(s.bbox[6 * i + 3]) &&
                    std::isfinite(s.bbox[6 * i + 4]) && std::isfinite(s.bbox[6 * i + 5])) {
@@ -129,6 +136,58 @@ void World::init(const am_params& p, const am_scene& s) {
     }
 }
 
+// A sub-body of composite `parent` (XMLParser.createComposite, :180-352): a box
+// (shape = size) or a sphere (shape[0] = r, one BV leaf at its centre, as
+// createSphere builds it), with transformB2C = (R, t), its pose in the
+// composite's frame.  Sub-bodies never enter the body list: collisions with
+// the composite run on them, placed from the parent first.
+int World::addCompositeSub(int parent, int type, const double* shape, const double* R, const double* t) {
+    if (parent < 0 || parent >= nScene || store[parent].type != ORC_COMPOSITE) return -1;
+    if (type != AM_BOX && type != AM_SPHERE) return -1;
+    Body* p = &store[parent];
+    subStore.emplace_back();
+    Body* b = &subStore.back();
+    b->id = ORC_SUB_ID0 + (int)subStore.size() - 1;
+    b->type = type;
+    b->friction = p->friction;
+    b->restitution = p->restitution;
+    M3 Rm;
+    double* pr = &Rm.m00;
+    for (int k = 0; k < 9; k++) pr[k] = R[k];
+    b->B2Cc = RT{Rm, V3(t[0], t[1], t[2])};
+    b->compParent = p;
+    if (type == AM_BOX) {
+        b->size = V3(shape[0], shape[1], shape[2]);
+        b->radius = vlength(vscale(0.5, b->size));
+    } else {
+        Node n;
+        n.cB = V3();
+        n.r = shape[0];
+        n.body = b;
+        n.id = (int)nodes.size();
+        nodes.push_back(n);
+        b->root = n.id;
+        // nodes[k].body of the scene's trees point into `store`, which does not move
+    }
+    p->subs.push_back(b);
+    RT T = rt_mult(p->T(), b->B2Cc);
+    b->theta = T.R;
+    b->x = T.t;
+    return 0;
+}
+
+// RigidBodyGeomComposite.updateBodyPositionsFromParent (:32-36): transformB2W =
+// parent.transformB2W * transformB2C.  The reference runs it in narrowPhase
+// before each composite's sub-body collisions; a parent does not move during
+// detection, so once before the pass gives the same poses.
+void World::updateCompositeSubs() {
+    for (Body& b : subStore) {
+        RT T = rt_mult(b.compParent->T(), b.B2Cc);
+        b.theta = T.R;
+        b.x = T.t;
+    }
+}
+
 Contact* World::newContact() {  // ContactPool.get (ContactPool.java:46-53)
     pool[cur].emplace_back();
     return &pool[cur].back();
@@ -168,6 +227,11 @@ static void recomputeJacobian(Contact* c, bool inColl) {
 void World::emit(Body* b1, Body* b2, const V3& pW, const V3& nW, int bv1, int bv2, int info, double cv) {
     Contact* c = newContact();
     c->state = CLEAR;
+    // a composite's sub-body hands the contact to its composite and stays as
+    // the contact's csb for the warm-start key (Contact.java:167-181)
+    c->csb1 = c->csb2 = -1;
+    if (b1->compParent) { c->csb1 = b1->id; b1 = b1->compParent; }
+    if (b2->compParent) { c->csb2 = b2->id; b2 = b2->compParent; }
     c->body1 = b1;
     c->body2 = b2;
     c->info = info;
@@ -611,6 +675,14 @@ void World::narrowPhase(Body* b1, Body* b2) {
         else { for (Body* b : b2->bodies) narrowPhase(b1, b); }
         return;
     }
+    if (b1->type == ORC_COMPOSITE) {           // CollisionProcessor.java:711-716
+        for (Body* b : b1->subs) narrowPhase(b, b2);
+        return;
+    }
+    if (b2->type == ORC_COMPOSITE) {           // :717-722
+        for (Body* b : b2->subs) narrowPhase(b1, b);
+        return;
+    }
     if (b1->type == AM_PLANE) {
         if (b2->type == AM_PLANE) return;
         if (b2->type == AM_BOX) boxPlane(b2, b1);
@@ -631,6 +703,7 @@ void World::collisionDetection() {
     contacts.clear();
     cur ^= 1;
     pool[cur].clear();
+    updateCompositeSubs();
     for (auto& n : nodes) n.cW = rt_point(n.body->T(), n.cB);   // BVSphere.updatecW
     size_t N = bodies.size();
     for (size_t i = 0; i + 1 < N; i++) {
@@ -736,12 +809,23 @@ static void takeOld(Contact* c, Contact* o) {
 }
 
 void World::warmStart() {
+    auto vanilla = [&](Contact* c) {   // vanillaWarmStart (:646-665)
+        auto it = last.find(ckey(c, c->info));
+        if (it != last.end()) { takeOld(c, it->second); c->prevCv = it->second->cv; }
+        else c->fresh = true;
+    };
+    // RigidBodyGeomBox or RigidBodyGeomComposite (:488-493)
+    auto boxy = [](const Body* b) { return (b->type == AM_BOX || b->type == ORC_COMPOSITE) && !b->isCollection; };
+    auto nonBoxSub = [&](int csb) { return csb >= 0 && subStore[csb - ORC_SUB_ID0].type != AM_BOX; };
     for (BPC* bpc : bodyPairContacts.v) {
         if (bpc->inCollection) continue;
-        bool bothBox = bpc->body1->type == AM_BOX && bpc->body2->type == AM_BOX &&
-                       !bpc->body1->isCollection && !bpc->body2->isCollection;
-        if (bothBox) {
+        if (boxy(bpc->body1) && boxy(bpc->body2)) {
             for (Contact* c : bpc->contactList) {
+                // a composite's non-box sub-body takes the plain warm start; for
+                // csb2 the reference does not skip the box-box search afterwards
+                // (:494-503)
+                if (nonBoxSub(c->csb1)) { vanilla(c); continue; }
+                if (nonBoxSub(c->csb2)) vanilla(c);
                 V3 pNew = rt_point(c->body1->T(), c->cB1);
                 auto look = [&](int info) -> Contact* {
                     auto it = last.find(ckey(c, info));
@@ -796,11 +880,7 @@ void World::warmStart() {
                 }
             }
         } else {
-            for (Contact* c : bpc->contactList) {
-                auto it = last.find(ckey(c, c->info));
-                if (it != last.end()) { takeOld(c, it->second); c->prevCv = it->second->cv; }
-                else c->fresh = true;
-            }
+            for (Contact* c : bpc->contactList) vanilla(c);
         }
     }
 }

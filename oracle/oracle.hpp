@@ -26,6 +26,14 @@ namespace orc {
 struct Body;
 struct BPC;
 
+// A composite body (RigidBodyGeomComposite, XMLParser.createComposite): a
+// rigid body whose geometry is a list of box and sphere sub-bodies.  The type
+// value is the oracle's own; the library refuses it (unknown body type).
+constexpr int ORC_COMPOSITE = 4;
+// ids of composite sub-bodies (the csb1 / csb2 of Contact), apart from the
+// scene bodies and collections
+constexpr int ORC_SUB_ID0 = 1 << 24;
+
 // Insertion-ordered set (LinkedHashSet semantics: remove + add moves to end).
 template <class T>
 struct OSet {
@@ -69,6 +77,7 @@ struct Contact {         // Contact.java
     V3 jna_v, jna_w, jnb_v, jnb_w, jt1a_v, jt1a_w, jt1b_v, jt1b_w, jt2a_v, jt2a_w, jt2b_v, jt2b_w;
     double l0 = 0, l1 = 0, l2 = 0, l0w = 0, l1w = 0, l2w = 0;
     double bn = 0, bt1 = 0, bt2 = 0, D00 = 0, D11 = 0, D22 = 0, w1 = 0, w2 = 0;
+    int csb1 = -1, csb2 = -1;    // ids of the composite sub-bodies that touched (csb1 / csb2), -1: none
 };
 
 struct Body {            // RigidBody.java / PlaneRigidBody.java / RigidCollection.java
@@ -93,6 +102,9 @@ struct Body {            // RigidBody.java / PlaneRigidBody.java / RigidCollecti
     OSet<BPC*> bpcs;                   // bodyPairContacts
     std::vector<double> metricHistory;
     std::vector<Body*> bodies;         // RigidCollection.bodies
+    std::vector<Body*> subs;           // RigidBodyGeomComposite.bodies
+    Body* compParent = nullptr;        // compositeBodyParent of a sub-body
+    RT B2Cc;                           // a sub-body's transformB2C (pose in its composite)
     RT T() const { return RT{theta, x}; }
 };
 
@@ -108,12 +120,13 @@ struct BPC {             // BodyPairContact.java
     Body* getOtherBody(Body* b) const { return body1 == b ? body2 : (body2 == b ? body1 : nullptr); }
 };
 
-// Contact.hashCode/equals (Contact.java:543-572): unordered (body, bv) pair
-// plus info.  Composite sub-bodies are not supported, so csb1/csb2 are null.
+// Contact.hashCode/equals (Contact.java:543-572): unordered (body, bv,
+// composite sub-body) pair plus info.
 struct CKey {
-    int a, bva, b, bvb, info;
+    int a, bva, b, bvb, info, csba = -1, csbb = -1;
     bool operator==(const CKey& o) const {
-        return a == o.a && bva == o.bva && b == o.b && bvb == o.bvb && info == o.info;
+        return a == o.a && bva == o.bva && b == o.b && bvb == o.bvb && info == o.info && csba == o.csba &&
+               csbb == o.csbb;
     }
 };
 struct CKeyHash {
@@ -123,14 +136,18 @@ struct CKeyHash {
         h ^= (uint64_t)(uint32_t)k.b * 0xC2B2AE3D27D4EB4Full + (h << 6) + (h >> 2);
         h ^= (uint64_t)(uint32_t)k.bvb + (h << 6) + (h >> 2);
         h ^= (uint64_t)(uint32_t)k.info * 0x165667B19E3779F9ull + (h << 6) + (h >> 2);
+        h ^= (uint64_t)(uint32_t)k.csba + ((uint64_t)(uint32_t)k.csbb << 32) + (h << 6) + (h >> 2);
         return (size_t)h;
     }
 };
 inline CKey ckey(const Contact* c, int info) {
     CKey k;
     int a = c->body1->id, b = c->body2->id;
-    if (a < b || (a == b && c->bv1 <= c->bv2)) { k.a = a; k.bva = c->bv1; k.b = b; k.bvb = c->bv2; }
-    else { k.a = b; k.bva = c->bv2; k.b = a; k.bvb = c->bv1; }
+    if (a < b || (a == b && (c->bv1 < c->bv2 || (c->bv1 == c->bv2 && c->csb1 <= c->csb2)))) {
+        k.a = a; k.bva = c->bv1; k.b = b; k.bvb = c->bv2; k.csba = c->csb1; k.csbb = c->csb2;
+    } else {
+        k.a = b; k.bva = c->bv2; k.b = a; k.bvb = c->bv1; k.csba = c->csb2; k.csbb = c->csb1;
+    }
     k.info = info;
     return k;
 }
@@ -174,6 +191,11 @@ struct World {
     double gdir[3];
 
     void init(const am_params& p, const am_scene& s);
+    // composite bodies: sub-bodies in their own store, placed from their
+    // parents before every collision pass (updateBodyPositionsFromParent)
+    std::deque<Body> subStore;
+    int addCompositeSub(int parent, int type, const double* shape, const double* R, const double* t);
+    void updateCompositeSubs();
     // steps (RigidBodySystem.advanceTime and its phases)
     void step(double dt);
     void clearBodies();

@@ -124,3 +124,26 @@ def test_malformed_sphere_trees_are_refused_on_the_host(lib):
             assert lib.am_set_batch(h, batch, 2) == abi.AM_E_ARG
     finally:
         lib.am_destroy(h)
+
+
+def test_composite_bodies_are_refused_on_the_host(lib):
+    """The library has no composite path yet: a scene with a composite body
+    (the oracle's type 4) is refused with AM_E_ARG before any device work."""
+    from adaptivemerging_gb300 import scenes
+    lib.am_create.argtypes = [C.POINTER(abi.am_params), C.POINTER(C.c_void_p)]
+    lib.am_set_scene.argtypes = [C.c_void_p, C.POINTER(abi.am_scene)]
+    lib.am_destroy.argtypes = [C.c_void_p]
+    lib.am_last_error.argtypes = [C.c_void_p]
+    lib.am_last_error.restype = C.c_char_p
+    b = scenes.Builder()
+    b.composite((0.0, 1.0, 0.0), 1.0, np.eye(3) / 6, [-0.5, -0.5, -0.5, 0.5, 0.5, 0.5],
+                [(abi.AM_BOX, [1.0, 1.0, 1.0, 0.0], scenes.IDENT, [0.0, 0.0, 0.0])])
+    b.plane((0, 0, 0), (0, 1, 0))
+    s = b.build().struct()
+    h = C.c_void_p()
+    assert lib.am_create(C.byref(abi.default_params(enable_merging=0)), C.byref(h)) == 0
+    try:
+        assert lib.am_set_scene(h, C.byref(s)) == abi.AM_E_ARG
+        assert lib.am_last_error(h) == b"unknown body type"
+    finally:
+        lib.am_destroy(h)
