@@ -20,6 +20,8 @@ tests/golden/reference_scenes.json by make_reference_scenes.py.
   children a node) with two boxes and a sphere, falling 30 m onto a plane
   under the reference's default gravity (1 m/s^2): the oracle lands them, and
   the device matches it bit for bit through the landing (steps 700-1000).
+- seesaw.xml and chariot.xml, composite bodies without springs: on the
+  oracle only (CPU), deterministic, at rest, contacts naming composites.
 """
 import json
 import os
