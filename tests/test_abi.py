@@ -6,6 +6,7 @@ import ctypes as C
 import os
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -147,3 +148,63 @@ def test_composite_bodies_are_refused_on_the_host(lib):
         assert lib.am_last_error(h) == b"unknown body type"
     finally:
         lib.am_destroy(h)
+
+
+_SWEEP_CALLS = {
+ "am_step": "(h, 0.01)", "am_collide": "(h, 0.01)", "am_warm_start": "(h,)", "am_solve": "(h, 0.01, None)",
+ "am_integrate": "(h, 0.01)", "am_step_phase": "(h, 0, 0.01)", "am_step_phase_bad": "(h, 99, 0.01)",
+ "am_single_sweep_order": "(h, None, 0, C.byref(i32))", "am_single_sweep": "(h, None, 0, 0.01)",
+ "am_merge_tests": "(h, None, 0, C.byref(i32))", "am_get_state": "(h, None, 0, C.byref(i64))",
+ "am_put_state": "(h, None, 0)", "am_get_bodies": "(h, None)", "am_put_bodies": "(h, None)",
+ "am_num_contacts": "(h, C.byref(i32))", "am_get_contacts": "(h, None, 0, C.byref(i32))", "am_get_stats": "(h, None)",
+ "am_set_batch": "(h, None, 0)", "am_set_batch_options": "(h, 0, 1e-6, 10)", "am_get_batch_stats": "(h, None)",
+ "am_set_batch_local_sweeps": "(h, 1)", "am_set_batch_clusters": "(h, 1)", "am_set_batch_size_classes": "(h, 1)",
+ "am_set_batch_stage": "(h, 64)", "am_set_batch_cluster_stage": "(h, 64)", "am_set_batch_relaxation": "(h, 1.0, 0)",
+ "am_set_batch_accel": "(h, 1)", "am_set_batch_critical": "(h, 0.5, 640)", "am_set_residual_target": "(h, 1e-6, 10)",
+ "am_set_kinematic": "(h, 0, None, 0.1, 1.0, 0.01)", "am_set_mixed_form": "(h, -1, 0)", "am_get_mixed_form": "(h, C.byref(i32))",
+ "am_get_batch_scene_stats": "(h, None, None, None, None)", "am_get_batch_scene_times": "(h, None, None, None)",
+ "am_get_batch_scene_ctas": "(h, None)", "am_get_batch_scene_chain": "(h, None)",
+ "am_learned_collect": "(h, 1, 100)", "am_learned_train": "(h, 1, 32, 1e-3, 1, None)", "am_learned_use": "(h, 1)",
+ "am_learned_scope": "(h, 0)", "am_learned_weights": "(h, None, None, None, None)",
+ "am_learned_info": "(h, None, None, None)", "am_learned_grad": "(h, None, None, 0, None, None)",
+ "am_learned_infer": "(h, None, 0, None, 1)", "am_learned_infer_noalloc": "(h, None, 0, None, 1)",
+ "am_get_topology": "(h, None, None, 0, C.byref(i32), C.byref(i32))", "am_get_perf": "(h, None)", "am_reset_perf": "(h,)",
+ "am_set_phase_timing": "(h, 1)", "am_get_phase_times": "(h, None)", "am_get_step_phases": "(h, None)",
+ "am_check_barrier_timeout": "(h, 4, C.byref(i32))", "am_get_stream": "(h, None)",
+}
+
+_SWEEP_CHILD = r"""
+import ctypes as C, sys
+sys.path.insert(0, sys.argv[1])
+from adaptivemerging_gb300 import abi
+from tests.test_abi import _SWEEP_CALLS
+L = C.CDLL(sys.argv[2])
+L.am_create.argtypes = [C.POINTER(abi.am_params), C.POINTER(C.c_void_p)]
+L.am_destroy.argtypes = [C.c_void_p]
+h = C.c_void_p()
+assert L.am_create(C.byref(abi.default_params()), C.byref(h)) == 0
+i32 = C.c_int32(0); i64 = C.c_int64(0)
+for name, args in _SWEEP_CALLS.items():
+    fn = getattr(L, name.replace("_bad", ""))
+    fn.restype = C.c_int32
+    a = tuple(C.c_void_p(x.value) if isinstance(x, C.c_void_p) else (C.c_double(x) if isinstance(x, float) else x)
+              for x in eval(args))
+    print(name, fn(*a), flush=True)
+L.am_destroy(h)
+"""
+
+
+def test_every_entry_point_answers_without_a_scene(lib):
+    """Every entry point on a context with no scene loaded, with null
+    pointers and zero sizes, returns a status (AM_OK, AM_E_ARG or
+    AM_E_STATE): nothing crashes, and nothing reaches a CUDA call (no GPU
+    is needed).  The calls run in a child process, so a crash fails the
+    test instead of the test session."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    so = os.path.join(root, "adaptivemerging_gb300", "libam.so")
+    r = subprocess.run([sys.executable, "-c", _SWEEP_CHILD, root, so], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = dict(line.rsplit(" ", 1) for line in r.stdout.split("\n") if line.strip())
+    assert set(got) == set(_SWEEP_CALLS)
+    allowed = {str(abi.AM_OK), str(abi.AM_E_ARG), str(abi.AM_E_STATE)}
+    assert all(v in allowed for v in got.values()), got
