@@ -93,3 +93,45 @@ def test_two_part_composite_rests_on_both_parts():
     c = o.contacts()
     xs = [float(p) for p in c["frame"].reshape(-1, 12)[:, 0]] if len(c["body1"]) else []
     assert len(c["body1"]) == 8 and min(xs) < -1.0 and max(xs) > 1.0   # four corners under each box
+
+
+def test_sphere_sub_body_against_a_box():
+    """A box resting on a composite's sphere sub-body: the contact's
+    composite side is a non-box sub-body, the warm-start branch where the
+    reference takes the plain warm start and then also runs the box-box
+    search (CollisionProcessor.java:494-503).  The pile comes to rest,
+    persisting contacts are warm started (not fresh), and two runs agree bit
+    for bit."""
+    def scene():
+        b = scenes.Builder()
+        m_box, m_sph = 8.0 * 100.0, 4.0 / 3 * np.pi * 0.5 ** 3 * 100.0
+        # composite: a 2 x 0.5 x 2 slab with a sphere of radius 0.5 on top of it
+        com_y = (m_box * 0.0 + m_sph * 0.75) / (m_box + m_sph)
+        I_box = np.diag([m_box / 12 * (0.25 + 4), m_box / 12 * 8, m_box / 12 * (4 + 0.25)])
+        I_sph = np.eye(3) * 0.4 * m_sph * 0.25
+        d = np.array([0.0, com_y, 0.0])
+        par = lambda m, r: m * (np.dot(r, r) * np.eye(3) - np.outer(r, r))
+        I = I_box + par(m_box, d) + I_sph + par(m_sph, np.array([0.0, 0.75, 0.0]) - d)
+        b.composite((0.0, 0.25 + com_y, 0.0), m_box + m_sph, I, [-1.0, -0.25 - com_y, -1.0, 1.0, 1.25 - com_y, 1.0],
+                    [(abi.AM_BOX, [2.0, 0.5, 2.0, 0.0], scenes.IDENT, [0.0, -com_y, 0.0]),
+                     (abi.AM_SPHERE, [0.5, 0.0, 0.0, 0.0], scenes.IDENT, [0.0, 0.75 - com_y, 0.0])])
+        b.box((0.6, 0.3, 0.6), (0.0, 1.5 + 0.15 + 0.005, 0.0), density=100.0)
+        b.plane((0, 0, 0), (0, 1, 0))
+        return b.build()
+    P = params(gravity_amount=9.81, enable_merging=0, iterations=60)
+    runs = []
+    for _ in range(2):
+        o = Oracle(scene(), P)
+        warm = 0
+        for s in range(200):
+            o.step(0.01)
+            c = o.contacts()
+            on_sphere = (c["body1"] == 1) & (c["body2"] == 0) | (c["body1"] == 0) & (c["body2"] == 1)
+            warm += int(np.sum(on_sphere & (c["fresh"] == 0)))
+        runs.append((o.bodies(), warm))
+    (b1, w1), (b2, w2) = runs
+    assert w1 == w2 and w1 > 0
+    for k in ("x", "v"):
+        assert np.array_equal(b1[k], b2[k])
+    # the box rests on the sphere (sunk a little under the default contact compliance)
+    assert abs(b1["v"][1]).max() < 1e-2 and abs(b1["x"][1][1] - 1.65) < 0.05
