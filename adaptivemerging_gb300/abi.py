@@ -19,7 +19,7 @@ AM_E_TIMEOUT = -4
 AM_E_CUDA = -5
 AM_E_STATE = -6
 
-AM_BOX, AM_SPHERE, AM_PLANE, AM_TREE = 0, 1, 2, 3
+AM_BOX, AM_SPHERE, AM_PLANE, AM_TREE, AM_COMPOSITE = 0, 1, 2, 3, 4
 AM_STATE_BROKEN, AM_STATE_ONEDGE, AM_STATE_CLEAR = 0, 1, 2
 AM_BV_NULL = -1
 # phases of the merging step (am_step_phase, AM_MPHASE_*)
@@ -98,6 +98,8 @@ class am_scene(C.Structure):
         ("shape", _P(_f64)), ("n_nodes", _i32), ("body_root", _P(_i32)), ("node_c", _P(_f64)),
         ("node_r", _P(_f64)), ("node_child0", _P(_i32)), ("node_nchild", _P(_i32)),
         ("bbox", _P(_f64)),
+        ("n_subs", _i32), ("sub_parent", _P(_i32)), ("sub_type", _P(_i32)), ("sub_shape", _P(_f64)),
+        ("sub_R", _P(_f64)), ("sub_t", _P(_f64)),
     ]
 
 
@@ -141,7 +143,7 @@ def ptr(a, ctype):
 class SceneArrays:
     """Owns the numpy arrays behind one am_scene (keeps them alive)."""
 
-    FIELDS_I = ("type", "pinned", "body_root", "node_child0", "node_nchild")
+    FIELDS_I = ("type", "pinned", "body_root", "node_child0", "node_nchild", "sub_parent", "sub_type")
 
     def __init__(self, **arrays):
         self.a = {}
@@ -158,6 +160,7 @@ class SceneArrays:
         s = am_scene()
         s.n_bodies = self.n
         s.n_nodes = self.n_nodes
+        s.n_subs = len(self.a["sub_parent"]) if "sub_parent" in self.a else 0
         for k, v in self.a.items():
             setattr(s, k, ptr(v, _i32 if k in self.FIELDS_I else _f64))
         return s

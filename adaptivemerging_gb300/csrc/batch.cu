@@ -1989,6 +1989,9 @@ int Ctx::setBatch(const am_scene* sc, int n) {
     all.restitution = re.data(); all.shape = shape.data(); all.n_nodes = nodeBase; all.body_root = root.data();
     all.node_c = nc.data(); all.node_r = nr.data(); all.node_child0 = c0.data(); all.node_nchild = nch.data();
     all.bbox = anyBox ? bbox.data() : nullptr;
+    all.n_subs = 0;   // composite bodies are refused before this point
+    all.sub_parent = all.sub_type = nullptr;
+    all.sub_shape = all.sub_R = all.sub_t = nullptr;
     int r = setScene(all);
     if (r) return r;
     nScenes = n;

@@ -192,8 +192,10 @@ static int check_scene(const am_scene& s, std::string& err) {
         err = "a node array is missing";
         return AM_E_ARG;
     }
+    if (s.n_subs != 0) { err = "composite bodies have no device path yet"; return AM_E_ARG; }
     for (int i = 0; i < s.n_bodies; i++) {
         int t = s.type[i];
+        if (t == AM_COMPOSITE) { err = "composite bodies have no device path yet"; return AM_E_ARG; }
         if (t < AM_BOX || t > AM_TREE) { err = "unknown body type"; return AM_E_ARG; }
         if ((t == AM_SPHERE || t == AM_TREE) && (s.body_root[i] < 0 || s.body_root[i] >= s.n_nodes)) {
             err = "sphere / tree body without a valid root node";

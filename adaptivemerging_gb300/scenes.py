@@ -11,7 +11,7 @@ import math
 
 import numpy as np
 
-from .abi import AM_BOX, AM_PLANE, AM_SPHERE, AM_TREE, SceneArrays
+from .abi import AM_BOX, AM_COMPOSITE, AM_PLANE, AM_SPHERE, AM_TREE, SceneArrays
 
 
 def yaw(theta):
@@ -33,9 +33,9 @@ def axis_angle(ax, theta):
 
 IDENT = [1.0, 0, 0, 0, 1.0, 0, 0, 0, 1.0]
 
-# Body type of a composite body.  It is not part of the C ABI: the oracle
-# steps composites, and the library refuses the type.
-COMPOSITE = 4
+# Composite bodies (AM_COMPOSITE): the oracle steps them; the library has no
+# device path for them yet and refuses the type.
+COMPOSITE = AM_COMPOSITE
 
 
 class Builder:
@@ -133,8 +133,9 @@ class Builder:
                   restitution=0.0, pinned=False):
         """A composite body (the reference's RigidBodyGeomComposite): rigid
         body data as given, and its box and sphere sub-bodies as (type,
-        shape[4], R[9], t[3]) with their pose in the composite's frame.  Only
-        the oracle steps composites; the library refuses their body type."""
+        shape[4], R[9], t[3]) with their pose in the composite's frame (the
+        am_scene sub-body arrays).  Only the oracle steps composites; the
+        library refuses their body type."""
         i = self._add(type=COMPOSITE, pinned=int(bool(pinned)), x=tuple(float(t) for t in x), R=R, v=v,
                       omega=omega, mass=float(mass), inertia=[float(t) for t in np.asarray(inertia).reshape(-1)],
                       friction=friction, restitution=restitution, bbox=[float(t) for t in bbox])
@@ -147,6 +148,11 @@ class Builder:
         f = lambda k, w: np.array([d[k] for d in self.b], float).reshape(n * w)
         nodes = self.nodes if self.nodes else []
         extra = {}
+        if self.subs:
+            extra.update(sub_parent=[q[0] for q in self.subs], sub_type=[q[1] for q in self.subs],
+                         sub_shape=np.array([q[2] for q in self.subs], float).reshape(-1),
+                         sub_R=np.array([q[3] for q in self.subs], float).reshape(-1),
+                         sub_t=np.array([q[4] for q in self.subs], float).reshape(-1))
         if any(d["bbox"] is not None for d in self.b):
             extra["bbox"] = np.array([d["bbox"] if d["bbox"] is not None else [np.nan] * 6 for d in self.b],
                                      float).reshape(-1)
@@ -161,12 +167,6 @@ class Builder:
             node_child0=[c0 for _, _, c0, _ in nodes], node_nchild=[nc for _, _, _, nc in nodes],
             **extra,
         )
-        if self.subs:
-            sc.composite_subs = {
-                "parent": [q[0] for q in self.subs], "type": [q[1] for q in self.subs],
-                "shape": np.array([q[2] for q in self.subs], float).reshape(-1),
-                "R": np.array([q[3] for q in self.subs], float).reshape(-1),
-                "t": np.array([q[4] for q in self.subs], float).reshape(-1)}
         return sc
 
 

@@ -35,6 +35,8 @@ extern "C" {
 #define AM_SPHERE  1   /* RigidBodyGeomSphere: shape = (r, 0, 0, 0); 1-node tree */
 #define AM_PLANE   2   /* PlaneRigidBody: x = point p, shape = (nx, ny, nz, 0) */
 #define AM_TREE    3   /* sphere-tree body (mesh / clump), shape unused      */
+#define AM_COMPOSITE 4 /* RigidBodyGeomComposite: geometry from am_scene's sub-bodies;
+                          no device path yet, am_set_scene refuses it (AM_E_ARG) */
 
 /* ---- contact state (Contact.ContactState) ------------------------------- */
 #define AM_STATE_BROKEN 0
@@ -116,7 +118,7 @@ typedef struct am_params {
  */
 typedef struct am_scene {
     int32_t        n_bodies;
-    const int32_t* type;        /* [n] AM_BOX / AM_SPHERE / AM_PLANE / AM_TREE */
+    const int32_t* type;        /* [n] AM_BOX / AM_SPHERE / AM_PLANE / AM_TREE / AM_COMPOSITE */
     const int32_t* pinned;      /* [n] */
     const double*  x;           /* [3n] centre of mass (plane: point p)        */
     const double*  R;           /* [9n] orientation (theta)                     */
@@ -141,6 +143,18 @@ typedef struct am_scene {
      * NULL, non-finite entries and other body types take the box of the
      * geometry (AM_TREE: the box of its leaf spheres). */
     const double*  bbox;
+    /* composite bodies (RigidBodyGeomComposite, XMLParser.java:180-352): the
+     * sub-bodies of the AM_COMPOSITE bodies, in each composite's list order,
+     * with stable ids (their index here) in place of Java object identity.
+     * A sub-body is a box (sub_shape = size) or a sphere (sub_shape[0] = r)
+     * with its pose in the composite's frame (transformB2C: sub_R, sub_t).
+     * n_subs = 0 without composites. */
+    int32_t        n_subs;
+    const int32_t* sub_parent;  /* [n_subs] index of the composite body       */
+    const int32_t* sub_type;    /* [n_subs] AM_BOX / AM_SPHERE                 */
+    const double*  sub_shape;   /* [4*n_subs]                                  */
+    const double*  sub_R;       /* [9*n_subs] rotation in the composite frame  */
+    const double*  sub_t;       /* [3*n_subs] position in the composite frame  */
 } am_scene;
 
 /* Per-body state read back after a step. */

@@ -11,22 +11,11 @@ extern "C" {
 void* or_create(const am_params* p, const am_scene* s) {
     World* w = new World();
     w->init(*p, *s);
+    if (w->badSubs) { delete w; return nullptr; }   // a composite sub-body it cannot place
     return w;
 }
 
 void or_destroy(void* h) { delete (World*)h; }
-
-// Sub-bodies of composite scene bodies (type ORC_COMPOSITE), in each
-// composite's list order: type AM_BOX (shape = size) or AM_SPHERE (shape[0] =
-// radius), R[9] and t[3] the pose in the composite's frame (transformB2C).
-// Call before the first step.  0, or -1 when a sub-body is refused.
-int or_add_composite_subs(void* h, int n, const int32_t* parent, const int32_t* type, const double* shape,
-                          const double* R, const double* t) {
-    World* w = (World*)h;
-    for (int k = 0; k < n; k++)
-        if (w->addCompositeSub(parent[k], type[k], shape + 4 * k, R + 9 * k, t + 3 * k)) return -1;
-    return 0;
-}
 
 void or_set_params(void* h, const am_params* p) { ((World*)h)->P = *p; }
 

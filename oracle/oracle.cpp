@@ -124,6 +124,9 @@ void World::init(const am_params& p, const am_scene& s) {
         }
         bodies.push_back(&b);
     }
+    for (int k = 0; k < s.n_subs; k++)
+        if (addCompositeSub(s.sub_parent[k], s.sub_type[k], s.sub_shape + 4 * k, s.sub_R + 9 * k, s.sub_t + 3 * k))
+            badSubs++;
     for (int i = 0; i < s.n_bodies; i++) {
         int r0 = s.body_root[i];
         if (r0 < 0) continue;

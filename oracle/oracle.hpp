@@ -27,9 +27,9 @@ struct Body;
 struct BPC;
 
 // A composite body (RigidBodyGeomComposite, XMLParser.createComposite): a
-// rigid body whose geometry is a list of box and sphere sub-bodies.  The type
-// value is the oracle's own; the library refuses it (unknown body type).
-constexpr int ORC_COMPOSITE = 4;
+// rigid body whose geometry is a list of box and sphere sub-bodies
+// (am_scene's sub-body arrays).
+constexpr int ORC_COMPOSITE = AM_COMPOSITE;
 // ids of composite sub-bodies (the csb1 / csb2 of Contact), apart from the
 // scene bodies and collections
 constexpr int ORC_SUB_ID0 = 1 << 24;
@@ -194,6 +194,7 @@ struct World {
     // composite bodies: sub-bodies in their own store, placed from their
     // parents before every collision pass (updateBodyPositionsFromParent)
     std::deque<Body> subStore;
+    int badSubs = 0;   // sub-bodies refused at init (bad parent or type)
     int addCompositeSub(int parent, int type, const double* shape, const double* R, const double* t);
     void updateCompositeSubs();
     // steps (RigidBodySystem.advanceTime and its phases)

@@ -13,8 +13,8 @@ implementation does not model): two boxes, a sphere, a plane and four mesh
 bodies whose sphere trees come from the reference's `data/*.sph` files and
 whose mass properties come from its `data/*.obj` meshes.  Two more,
 `scenes3D/seesaw.xml` and `scenes3D/chariot.xml`, hold composite bodies
-(RigidBodyGeomComposite) without springs; they are stored with their
-composite sub-bodies, which only the oracle steps so far.  The reference tree is not present where the GPU tests
+(RigidBodyGeomComposite) without springs; their arrays include the
+composite sub-bodies (am_scene's sub_* arrays), which only the oracle steps so far.  The reference tree is not present where the GPU tests
 run, so the tests read this fixture instead of the XML files.  The first rows
 (#bodies, #contacts) of the reference's recorded metrics for tower30
 (`scenes3D/csv/conditional_acceptance_revisions/tower30_merged.csv`, and an
@@ -55,10 +55,8 @@ def main():
                                "params": {f: getattr(P, f) for f, _ in abi.am_params._fields_}, "names": names}
     for name in COMPOSITE_SCENES:
         sc, P, names = scene_xml.load(os.path.join(root, "scenes3D", name + ".xml"), composites=True)
-        subs = {k: (v.tolist() if hasattr(v, "tolist") else list(v)) for k, v in sc.composite_subs.items()}
         out["scenes"][name] = {"arrays": {k: v.tolist() for k, v in sc.a.items()},
-                               "params": {f: getattr(P, f) for f, _ in abi.am_params._fields_}, "names": names,
-                               "composite_subs": subs}
+                               "params": {f: getattr(P, f) for f, _ in abi.am_params._fields_}, "names": names}
     with open(os.path.join(root, CSV)) as f:
         rows = list(csv.reader(f))[1:]
     out["tower30_csv_bodies_contacts"] = [[int(r[0]), int(r[1])] for r in rows[:60] if len(r) > 2]

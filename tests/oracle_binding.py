@@ -53,9 +53,6 @@ def lib():
         L.or_set_kinematic.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_double, C.c_double,
                                        C.c_double]
         L.or_set_kinematic.restype = C.c_int
-        L.or_add_composite_subs.argtypes = [C.c_void_p, C.c_int, ip, ip, C.POINTER(C.c_double),
-                                            C.POINTER(C.c_double), C.POINTER(C.c_double)]
-        L.or_add_composite_subs.restype = C.c_int
         _lib = L
     return _lib
 
@@ -74,16 +71,8 @@ class Oracle:
         self.params = params
         self._s = scene.struct()
         self.h = lib().or_create(C.byref(params), C.byref(self._s))
+        assert self.h, "the oracle refused the scene"
         self.n = scene.n
-        subs = getattr(scene, "composite_subs", None)
-        if subs is not None and len(subs["parent"]):
-            arr = {k: np.ascontiguousarray(v, dtype=np.int32 if k in ("parent", "type") else np.float64)
-                   for k, v in subs.items()}
-            ip, dp = C.POINTER(C.c_int32), C.POINTER(C.c_double)
-            r = lib().or_add_composite_subs(self.h, len(arr["parent"]), arr["parent"].ctypes.data_as(ip),
-                                            arr["type"].ctypes.data_as(ip), arr["shape"].ctypes.data_as(dp),
-                                            arr["R"].ctypes.data_as(dp), arr["t"].ctypes.data_as(dp))
-            assert r == 0, "the oracle refused a composite sub-body"
 
     def __del__(self):
         if getattr(self, "h", None):

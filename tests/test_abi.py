@@ -129,7 +129,8 @@ def test_malformed_sphere_trees_are_refused_on_the_host(lib):
 
 def test_composite_bodies_are_refused_on_the_host(lib):
     """The library has no composite path yet: a scene with a composite body
-    (the oracle's type 4) is refused with AM_E_ARG before any device work."""
+    (AM_COMPOSITE, with its sub-bodies in am_scene) is refused with AM_E_ARG
+    before any device work."""
     from adaptivemerging_gb300 import scenes
     lib.am_create.argtypes = [C.POINTER(abi.am_params), C.POINTER(C.c_void_p)]
     lib.am_set_scene.argtypes = [C.c_void_p, C.POINTER(abi.am_scene)]
@@ -145,7 +146,7 @@ def test_composite_bodies_are_refused_on_the_host(lib):
     assert lib.am_create(C.byref(abi.default_params(enable_merging=0)), C.byref(h)) == 0
     try:
         assert lib.am_set_scene(h, C.byref(s)) == abi.AM_E_ARG
-        assert lib.am_last_error(h) == b"unknown body type"
+        assert lib.am_last_error(h) == b"composite bodies have no device path yet"
     finally:
         lib.am_destroy(h)
 

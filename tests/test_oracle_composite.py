@@ -1,9 +1,9 @@
 """Composite bodies in the oracle (the reference's RigidBodyGeomComposite:
 XMLParser.createComposite, CollisionProcessor.narrowPhase :711-722,
 Contact.set :167-181, the composite branch of warmStart :488-503).  The
-library does not step composites yet and refuses their body type; these CPU
-tests hold the oracle's restatement that a device path will be checked
-against.
+library does not step composites yet and refuses their body type
+(AM_COMPOSITE); these CPU tests hold the oracle's restatement that a device
+path will be checked against.
 
 - createComposite's mass properties on a known answer (two boxes: mass,
   centre, parallel-axis inertia, box, sub-body poses).
@@ -40,9 +40,8 @@ def test_composite_mass_properties():
     I = np.asarray(a["inertia"][:9]).reshape(3, 3)
     assert np.allclose(I, np.diag([2 / 3, 2 / 3 + 4, 2 / 3 + 4]), rtol=0, atol=1e-15)
     assert list(a["bbox"][:6]) == [-1.5, -0.5, -0.5, 1.5, 0.5, 0.5]
-    subs = sc.composite_subs
-    assert list(subs["parent"]) == [0, 0] and list(subs["type"]) == [abi.AM_BOX, abi.AM_BOX]
-    assert list(subs["t"]) == [-1.0, 0.0, 0.0, 1.0, 0.0, 0.0]
+    assert list(a["sub_parent"]) == [0, 0] and list(a["sub_type"]) == [abi.AM_BOX, abi.AM_BOX]
+    assert list(a["sub_t"]) == [-1.0, 0.0, 0.0, 1.0, 0.0, 0.0] and sc.struct().n_subs == 2
 
 
 def test_composites_need_the_option():

@@ -41,8 +41,6 @@ def _load(name):
         d = json.load(f)
     s = d["scenes"][name]
     sc = abi.SceneArrays(**s["arrays"])
-    if "composite_subs" in s:
-        sc.composite_subs = s["composite_subs"]
     P = abi.am_params()
     for k, v in s["params"].items():
         setattr(P, k, v)
