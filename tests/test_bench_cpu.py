@@ -5,6 +5,8 @@ import os
 import subprocess
 import sys
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -23,3 +25,17 @@ def test_reference_arm_json_line():
     assert d["e2e"]["value"] == d["value"] and d["cpu_baseline"]["value"] == d["value"]
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["config"]["scenes"] == 8
+
+
+@pytest.mark.parametrize("workload", ["tower", "wall"])
+def test_single_scene_reference_arm_json_line(workload):
+    """The single-scene workloads' reference arm (the oracle on one core, the
+    reference's list-order solve) prints the same contract line."""
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", workload,
+                        "--steps", "2", "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "steps/s" and d["value"] > 0 and d["dtype"] == "f64"
+    assert d["e2e"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
